@@ -1,0 +1,91 @@
+/*
+ * gb2d_oracle — CPU restatement of the reference hot path (ByungJoonLee/2D_Engine).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker the GPU path is compared with;
+ * it is never the product.  Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg may load it.
+ *
+ * Parity pinning: every function here is checked bit-for-bit (or to the stated
+ * tolerance for the iterative solve) against outputs of the reference itself,
+ * stored as golden fixtures under tests/golden/ and produced by
+ * tests/golden/make_golden.py from the headless reference build in oracle/ref/.
+ *
+ * Array layout is the reference's ARRAY_2D (ARRAY_2D.h:140-146): row-major,
+ * i fastest, ghost cells included, element (i, j) of a field with ghost width g
+ * and interior extent nI at [(i + g) + (j + g) * (nI + 2g)].
+ *   phi : node grid ni x nj, ghost 2      ((ni+4) x (nj+4))
+ *   u   : x-faces (ni+1) x nj, ghost 2     ((ni+5) x (nj+4))
+ *   v   : y-faces ni x (nj+1), ghost 2     ((ni+4) x (nj+5))
+ *   ua  : advecting x-velocity, ghost 3    ((ni+7) x (nj+6))
+ *   va  : advecting y-velocity, ghost 3    ((ni+6) x (nj+7))
+ *   p   : pressure, ghost 1                ((ni+2) x (nj+2))
+ *   kappa : curvature, no ghost            (ni x nj)
+ * All arithmetic is IEEE double with no contraction (build with -ffp-contract=off).
+ */
+#ifndef GB2D_ORACLE_H
+#define GB2D_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int ni, nj;                      /* pressure / level-set nodes */
+  double x_min, y_min, x_max, y_max;
+} or_grid;
+
+typedef struct {
+  double water_density;            /* phi > 0  (air_bubble_rising, PROJECTION_2D.h:350-358) */
+  double air_density;              /* phi <= 0 */
+  double surface_tension;          /* jc = sigma * kappa (PROJECTION_2D.h:826-833) */
+  double weno_epsilon;             /* 1e-6 in the scripts */
+  int reinit_iterations;           /* iteration_number_for_reinitialization */
+  int reinit_scaling;              /* scaling_number_for_reinitialization: dtau = dx / scaling */
+  double pcg_tolerance;            /* stop when r.z < tol^2 (PCG_METHOD.cpp:254) */
+  int pcg_max_iterations;
+} or_params;
+
+typedef struct {
+  int iterations;
+  double residual;                 /* sqrt(r.z) at exit, as the reference prints it */
+  double max_velocity_x, max_velocity_y;
+} or_stats;
+
+/* Status codes (shared meaning with the GPU ABI). */
+#define OR_OK 0
+#define OR_BAD_ARG (-1)
+#define OR_NO_MEMORY (-2)
+#define OR_ZERO_GRADIENT (-3)
+
+/* a7 ghost fills. */
+void or_fill_ghost_copy(double* dst, int gd, const double* src, int gs, int nI, int nJ, int g);
+void or_fill_ghost_extrapolate(double* f, int g, int nI, int nJ);
+
+/* a1+a5: one Levelset_Advection call (WENO5 forward-Euler sweep + ghost extrapolation). */
+int or_levelset_advection(const or_grid* gr, const or_params* pr, double* phi, const double* ua, const double* va, double dt);
+/* a2+a6: one Reinitialization call (S = phi/sqrt(phi^2+dx^2), then reinit_iterations sweeps). */
+int or_reinitialization(const or_grid* gr, const or_params* pr, double* phi);
+/* a4: level-set TVD-RK3 then reinit TVD-RK3, as EULERIAN_FLUID_SOLVER_2D.h:1694-1741. */
+int or_levelset_rk3(const or_grid* gr, const or_params* pr, double* phi, const double* ua, const double* va, double dt);
+/* a3: one Velocity_Advection call (ENO3 on both MAC components; refreshes ua, va first). */
+int or_velocity_advection(const or_grid* gr, const or_params* pr, double* u, double* v, double* ua, double* va, double dt);
+/* a8: ComputeCurvaturesThread (fills phi's ghosts, writes kappa). */
+int or_curvature(const or_grid* gr, double* phi, double* kappa);
+/* a9-a14: one PROJECTION_2D::Solve(dt, tid); p is the warm start and the result. */
+int or_projection(const or_grid* gr, const or_params* pr, double* phi, double* u, double* v, double* p, double* kappa, double dt, or_stats* st);
+
+/* a10 in matrix-free form.  bx: x-faces (ni+1) x nj (face i between nodes i-1 and i),
+ * by: y-faces ni x (nj+1), diag, rhs: ni x nj.  phi must already hold the ghost
+ * state of the projection (or_curvature fills it).  kappa: ni x nj. */
+int or_poisson_assemble(const or_grid* gr, const or_params* pr, const double* phi, const double* u, const double* v, const double* kappa, double dt,
+                        double* bx, double* by, double* diag, double* rhs);
+/* Matrix-free operator apply in the reference CSR row order (l, r, b, t, diag). */
+void or_poisson_apply(const or_grid* gr, const double* bx, const double* by, const double* diag, const double* x, double* y);
+/* The reference PCG with IC(0) (PCG_METHOD.cpp:176-264) on the matrix-free system.
+ * x: warm start in, solution out (ni x nj).  max_iterations < 0 keeps pr's value. */
+int or_pcg_ic0(const or_grid* gr, const or_params* pr, const double* bx, const double* by, const double* diag, const double* rhs, double* x, or_stats* st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

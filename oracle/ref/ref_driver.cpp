@@ -1,0 +1,240 @@
+/*
+ * Headless driver around the reference solver (ByungJoonLee/2D_Engine), built
+ * by oracle/ref/Makefile straight from the reference's own sources into
+ * oracle/_ref/libref2d.so.  It is test infrastructure only: the golden-vector
+ * generator (tests/golden/make_golden.py) and the oracle-vs-reference checks
+ * call it to obtain outputs of the reference itself.
+ *
+ * It replaces what SIMULATION_WORLD.h:86-307 and :1094-1146 do (script parsing,
+ * GLUT, timers) with direct construction of EULERIAN_FLUID_SOLVER_2D
+ * (EULERIAN_FLUID_SOLVER_2D.h:159-727) from a SCRIPT_BLOCK whose values this
+ * file fills in, then exposes the solver's own step functions:
+ *   Levelset_Advection (:1896), Reinitialization (:2402), Velocity_Advection
+ *   (:1886), Projection (:2359), AdvanceOneTimeStepThread (:1140),
+ *   LEVELSET_2D::ComputeCurvaturesThread (LEVELSET_2D.h:898).
+ * Every call runs on one worker (thread_id 0 of a 1-thread MULTITHREADING),
+ * which is how the reference's head thread runs the pressure solve anyway
+ * (PROJECTION_2D.h:250-254).
+ */
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <sstream>
+#include <streambuf>
+#include <string>
+
+#include "EULERIAN_FLUID_SOLVER_2D.h"
+
+/* ---- SCRIPT_BLOCK accessors (declared in SCRIPT_READER.h:112-160) ----------
+ * The reference implements these with a regex parser (SCRIPT_READER.cpp); the
+ * driver stores already-typed text values, so plain lookups are enough. */
+static SCRIPT_BLOCK g_empty_block;
+
+const SCRIPT_VALUE* SCRIPT_BLOCK::SearchValue(const vector<SCRIPT_VALUE*>* vals, const char* name) const {
+  for (size_t k = 0; k < vals->size(); ++k)
+    if ((*vals)[k]->value_name == name) return (*vals)[k];
+  return 0;
+}
+const SCRIPT_BLOCK& SCRIPT_BLOCK::FindBlock(const char* name) const {
+  for (size_t k = 0; k < child_blocks.size(); ++k)
+    if (child_blocks[k]->block_name == name) return *child_blocks[k];
+  return g_empty_block;
+}
+int SCRIPT_BLOCK::GetInteger(const char* name, const int& dflt) const {
+  const SCRIPT_VALUE* v = SearchValue(&values, name);
+  return v ? atoi(v->val.c_str()) : dflt;
+}
+T SCRIPT_BLOCK::GetFloat(const char* name, const T& dflt) const {
+  const SCRIPT_VALUE* v = SearchValue(&values, name);
+  return v ? strtod(v->val.c_str(), 0) : dflt;
+}
+VT SCRIPT_BLOCK::GetVector2(const char* name, const VT& dflt) const {
+  const SCRIPT_VALUE* v = SearchValue(&values, name);
+  if (!v) return dflt;
+  double a = 0, b = 0;
+  sscanf(v->val.c_str(), "%lf %lf", &a, &b);
+  return VT(a, b);
+}
+VI SCRIPT_BLOCK::GetInt2(const char* name, const VI& dflt) const {
+  const SCRIPT_VALUE* v = SearchValue(&values, name);
+  if (!v) return dflt;
+  int a = 0, b = 0;
+  sscanf(v->val.c_str(), "%d %d", &a, &b);
+  return VI(a, b);
+}
+bool SCRIPT_BLOCK::GetBoolean(const char* name, const bool dflt) const {
+  const SCRIPT_VALUE* v = SearchValue(&values, name);
+  return v ? (v->val == "true") : dflt;
+}
+const char* SCRIPT_BLOCK::GetString(const char* name, const char* dflt) const {
+  const SCRIPT_VALUE* v = SearchValue(&values, name);
+  return v ? v->val.c_str() : dflt;
+}
+
+namespace {
+
+struct NullBuffer : std::streambuf {
+  int overflow(int c) override { return c; }
+};
+NullBuffer g_null;
+
+void put(SCRIPT_BLOCK& b, const char* name, const std::string& val) {
+  SCRIPT_VALUE* v = new SCRIPT_VALUE;
+  v->value_name = name;
+  v->val = val;
+  v->val_type = SCRIPT_VALUE::TYPE_NONE;
+  b.values.push_back(v);
+}
+std::string num(double x) {
+  char buf[64];
+  snprintf(buf, sizeof buf, "%.17g", x);
+  return buf;
+}
+SCRIPT_BLOCK* child(SCRIPT_BLOCK& b, const char* name) {
+  SCRIPT_BLOCK* c = new SCRIPT_BLOCK;
+  c->block_name = name;
+  b.child_blocks.push_back(c);
+  return c;
+}
+
+struct RefSim {
+  MULTITHREADING mt;
+  WORLD_DISCRETIZATION_2D world;
+  EULERIAN_FLUID_SOLVER_2D solver;
+  SCRIPT_BLOCK block;
+};
+
+ARRAY_2D<T>* field(RefSim* s, int id) {
+  EULERIAN_FLUID_SOLVER_2D& f = s->solver;
+  switch (id) {
+    case 0: return &f.water_levelset->signed_distance_field.array_for_this;  // phi, ghost 2
+    case 1: return &f.water_velocity_field_mac_x->array_for_this;            // U faces, ghost 2
+    case 2: return &f.water_velocity_field_mac_y->array_for_this;            // V faces, ghost 2
+    case 3: return &f.vector_field_mac_ghost_x.array_for_this;               // advecting U, ghost 3
+    case 4: return &f.vector_field_mac_ghost_y.array_for_this;               // advecting V, ghost 3
+    case 5: return &f.water_projection->pressure_field.array_for_this;       // p, ghost 1
+    case 6: return &f.water_levelset->curvature.array_for_this;              // kappa, ghost 0
+    case 7: return &f.water_projection->projection_density_field.array_for_this;  // rho, ghost 1
+    case 8: return &f.water_projection->jc_on_solution.array_for_this;       // sigma*kappa, ghost 1
+    case 9: return &f.water_projection->divergence_field.array_for_this;     // div/dt, ghost 1
+    case 10: return &f.sign_function.array_for_this;                         // reinit S, ghost 3
+    case 11: return &f.scalar_field_ghost.array_for_this;                    // WENO scratch, ghost 3
+    default: return 0;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+/* prm: [0] water_density (phi > 0), [1] air_density (phi <= 0), [2] water_viscosity,
+ * [3] air_viscosity, [4] surface_tension, [5] gravity_x, [6] gravity_y,
+ * [7] PCG tolerance on sqrt(r.z) (PCG_METHOD.cpp:254), [8] PCG max_iteration,
+ * [9] iteration_number_for_reinitialization, [10] scaling_number_for_reinitialization,
+ * [11] cfl_number, [12] WENO epsilon. */
+void* ref_create(int ni, int nj, double x_min, double y_min, double x_max, double y_max, const double* prm) {
+  std::cout.rdbuf(&g_null);
+  RefSim* s = new RefSim;
+  s->mt.Initialize(1);
+  s->world.large_bubble = true;
+  s->world.small_bubble = false;
+  s->world.air_water_simulation = true;
+
+  SCRIPT_BLOCK& b = s->block;
+  put(b, "ghost_width", "3");
+  put(b, "fastsweeping_reinitialization", "false");
+  put(b, "sussmanstyle_reinitialization", "true");
+  put(b, "scaling_number_for_reinitialization", num(prm[10]));
+  put(b, "iteration_number_for_reinitialization", num(prm[9]));
+  put(b, "water_viscosity", num(prm[2]));
+  put(b, "air_viscosity", num(prm[3]));
+  put(b, "gravity", num(prm[5]) + " " + num(prm[6]));
+  put(b, "water_density", num(prm[0]));
+  put(b, "air_density", num(prm[1]));
+  put(b, "surface_tension", num(prm[4]));
+  put(b, "order_for_time_advancing", "3");
+  put(b, "cfl_number", num(prm[11]));
+  put(b, "use_mac_grid", "true");
+  put(b, "is_velocity_advection_active", "true");
+  put(b, "is_sourcing_active", "true");
+  put(b, "is_projection_active", "true");
+  put(b, "is_levelset_advection_active", "true");
+  put(b, "is_viscosity_active", "true");
+  put(b, "use_delta_function_formulation", "true");
+  put(b, "use_jump_condition_on_viscosity", "false");
+  put(b, "CSF_model", "false");
+  put(b, "curvature_by_normal_vector", "false");
+  put(b, "curvature_by_levelset", "true");
+  SCRIPT_BLOCK* la = child(b, "LEVELSET_ADVECTION");
+  put(*la, "use_5th_weno", "true");
+  put(*la, "epsilon", num(prm[12]));
+  SCRIPT_BLOCK* va = child(b, "VELOCITY_ADVECTION");
+  put(*va, "use_3rd_eno_v", "true");
+  SCRIPT_BLOCK* pr = child(b, "PROJECTION");
+  put(*pr, "tolerance", num(prm[7]));
+  put(*pr, "max_iteration", num(prm[8]));
+  put(*pr, "air_bubble_rising", "true");
+  put(*pr, "poisson_solver_type", "PCG");
+  put(*pr, "Neumann_Boundary_Condition", "true");
+
+  GRID_STRUCTURE_2D grid(ni, nj, 0, 0, x_min, y_min, x_max, y_max);
+  s->solver.world_discretization = &s->world;
+  s->solver.air_water_simulation = true;
+  s->solver.InitializeFromScriptBlock(grid, b, &s->mt);
+  return s;
+}
+
+void ref_destroy(void* h) { delete static_cast<RefSim*>(h); }
+
+/* Shape of a ghost-inclusive array: start indices (negative = ghost width) and extents. */
+int ref_field_shape(void* h, int id, int* i_start, int* j_start, int* i_res, int* j_res) {
+  ARRAY_2D<T>* a = field(static_cast<RefSim*>(h), id);
+  if (!a) return -1;
+  *i_start = a->i_start;
+  *j_start = a->j_start;
+  *i_res = a->i_res;
+  *j_res = a->j_res;
+  return 0;
+}
+int ref_get_field(void* h, int id, double* out) {
+  ARRAY_2D<T>* a = field(static_cast<RefSim*>(h), id);
+  if (!a) return -1;
+  for (int k = 0; k < a->ij_res; ++k) out[k] = a->values[k];
+  return 0;
+}
+int ref_set_field(void* h, int id, const double* in) {
+  ARRAY_2D<T>* a = field(static_cast<RefSim*>(h), id);
+  if (!a) return -1;
+  for (int k = 0; k < a->ij_res; ++k) a->values[k] = in[k];
+  return 0;
+}
+
+void ref_levelset_advection(void* h, double dt) { static_cast<RefSim*>(h)->solver.Levelset_Advection(dt, 0); }
+void ref_reinitialization(void* h, double dt) { static_cast<RefSim*>(h)->solver.Reinitialization(dt, 0); }
+void ref_velocity_advection(void* h, double dt) { static_cast<RefSim*>(h)->solver.Velocity_Advection(dt, 0); }
+void ref_projection(void* h, double dt) { static_cast<RefSim*>(h)->solver.Projection(dt, 0); }
+void ref_curvature(void* h) { static_cast<RefSim*>(h)->solver.water_levelset->ComputeCurvaturesThread(0); }
+void ref_step(void* h, double dt) { static_cast<RefSim*>(h)->solver.AdvanceOneTimeStepThread(dt, 0); }
+double ref_cfl_dt(void* h) { return static_cast<RefSim*>(h)->solver.CFLOneTimeStep(); }
+
+/* Linear system of the most recent projection (POISSON_SOLVER.cpp:714-976):
+ * call with null arrays to get n and nnz, then again to copy. */
+int ref_poisson_system(void* h, int* n, int* nnz, int* row_ptr, int* col, double* val, double* b, double* x) {
+  POISSON_SOLVER& ps = static_cast<RefSim*>(h)->solver.water_projection->poisson_solver;
+  *n = ps.A.N;
+  *nnz = ps.A.nz;
+  if (row_ptr) for (int k = 0; k <= ps.A.N; ++k) row_ptr[k] = ps.A.row_ptr[k];
+  if (col) for (int k = 0; k < ps.A.nz; ++k) col[k] = ps.A.column_index[k];
+  if (val) for (int k = 0; k < ps.A.nz; ++k) val[k] = ps.A.values[k];
+  if (b) for (int k = 0; k < ps.b.num_dimension; ++k) b[k] = ps.b[k];
+  if (x) for (int k = 0; k < ps.x.num_dimension; ++k) x[k] = ps.x[k];
+  return 0;
+}
+int ref_pcg_info(void* h, int* iterations, double* residual) {
+  LINEAR_SOLVER* ls = static_cast<RefSim*>(h)->solver.water_projection->poisson_solver.linear_solver;
+  *iterations = ls->num_iteration;
+  *residual = ls->residual;
+  return 0;
+}
+
+}  // extern "C"
