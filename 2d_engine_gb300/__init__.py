@@ -1,0 +1,240 @@
+"""Python binding of the gb2d C ABI (include/gb2d.h) for sm_103a GPUs.
+
+The product is the CUDA library 2d_engine_gb300/_build/libgb2d.so; this module
+loads it with ctypes and mirrors the step interface of the reference solver's
+EULERIAN_FLUID_SOLVER_2D (Levelset_Advection, Reinitialization,
+Velocity_Advection, Projection).  There is no CPU fallback: if the library is
+missing or no GPU is visible, the calls raise.
+
+Arrays are numpy float64 in the reference's ghost-inclusive ARRAY_2D layout,
+shape (rows = j, cols = i):  phi (nj+4, ni+4), u (nj+4, ni+5), v (nj+5, ni+4),
+ua (nj+6, ni+7), va (nj+7, ni+6), p (nj+2, ni+2), kappa (nj, ni).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libgb2d.so")
+
+FIELD_PHI, FIELD_U, FIELD_V, FIELD_UA, FIELD_VA, FIELD_P, FIELD_KAPPA = range(7)
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+SOLVER_MGPCG, SOLVER_PCG_JACOBI = 0, 1
+
+ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "non-finite value", -4: "iteration cap reached",
+          -5: "zero level-set gradient", -6: "no CUDA device"}
+
+
+class GridT(ctypes.Structure):
+    _fields_ = [("ni", ctypes.c_int), ("nj", ctypes.c_int), ("x_min", ctypes.c_double), ("y_min", ctypes.c_double),
+                ("x_max", ctypes.c_double), ("y_max", ctypes.c_double)]
+
+
+class ParamsT(ctypes.Structure):
+    _fields_ = [("water_density", ctypes.c_double), ("air_density", ctypes.c_double), ("surface_tension", ctypes.c_double),
+                ("weno_epsilon", ctypes.c_double), ("reinit_iterations", ctypes.c_int), ("reinit_scaling", ctypes.c_int),
+                ("advection_precision", ctypes.c_int)]
+
+
+class SolveOptsT(ctypes.Structure):
+    _fields_ = [("solver", ctypes.c_int), ("precision", ctypes.c_int), ("tolerance", ctypes.c_double),
+                ("max_iterations", ctypes.c_int), ("mg_smooth", ctypes.c_int), ("inner_tolerance", ctypes.c_double)]
+
+
+class SolveStatsT(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("outer_iterations", ctypes.c_int), ("rel_residual", ctypes.c_double),
+                ("max_velocity_x", ctypes.c_double), ("max_velocity_y", ctypes.c_double)]
+
+
+class GB2DError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gb2d error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def library():
+    """Load libgb2d.so (built by __graft_entry__.build() / 2d_engine_gb300/build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA library first (python 2d_engine_gb300/build.py)")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, d, i = ctypes.c_void_p, ctypes.c_double, ctypes.c_int
+    G, P, O, S = ctypes.POINTER(GridT), ctypes.POINTER(ParamsT), ctypes.POINTER(SolveOptsT), ctypes.POINTER(SolveStatsT)
+    sig = {
+        "gb2d_create": [G, P, ctypes.POINTER(vp)],
+        "gb2d_destroy": [vp],
+        "gb2d_field_extent": [G, i, ctypes.POINTER(i), ctypes.POINTER(i)],
+        "gb2d_set_field": [vp, i, vp],
+        "gb2d_get_field": [vp, i, vp],
+        "gb2d_field_device_ptr": [vp, i, ctypes.POINTER(vp)],
+        "gb2d_synchronize": [vp],
+        "gb2d_levelset_advection": [vp, d],
+        "gb2d_reinitialization": [vp],
+        "gb2d_levelset_rk3": [vp, d],
+        "gb2d_velocity_advection": [vp, d],
+        "gb2d_curvature": [vp],
+        "gb2d_projection": [vp, d, O, S],
+        "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
+        "gb2d_poisson_apply": [vp, vp, vp],
+        "gb2d_poisson_solve": [vp, vp, vp, O, S],
+        "gb2d_set_stream": [vp, vp],
+        "gb2d_probe_enable": [vp, i],
+        "gb2d_probe_read": [vp, ctypes.POINTER(i), ctypes.POINTER(d), ctypes.POINTER(d)],
+        "gb2d_kernel_launches": [ctypes.POINTER(ctypes.c_ulonglong)],
+        "gb2d_checkpoint_save": [vp],
+        "gb2d_checkpoint_restore": [vp],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = i
+    L.gb2d_last_error.argtypes = [vp]
+    L.gb2d_last_error.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def kernel_launches():
+    """Kernels launched by libgb2d.so in this process so far."""
+    n = ctypes.c_ulonglong()
+    library().gb2d_kernel_launches(ctypes.byref(n))
+    return n.value
+
+
+def _ptr(a):
+    if a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise ValueError("arrays must be C-contiguous float64")
+    return a.ctypes.data
+
+
+def solve_opts(solver=SOLVER_MGPCG, precision=PRECISION_FP64, tolerance=1e-8, max_iterations=10000, mg_smooth=2,
+               inner_tolerance=1e-4):
+    return SolveOptsT(solver, precision, tolerance, max_iterations, mg_smooth, inner_tolerance)
+
+
+class Context:
+    """One simulation state on the GPU (a gb2d_ctx)."""
+
+    def __init__(self, ni, nj, x_min=0.0, y_min=0.0, x_max=1.0, y_max=1.0, water_density=1000.0, air_density=1.0,
+                 surface_tension=0.0728, weno_epsilon=1e-6, reinit_iterations=25, reinit_scaling=5,
+                 advection_precision=PRECISION_FP64):
+        self.L = library()
+        self.grid = GridT(ni, nj, x_min, y_min, x_max, y_max)
+        self.params = ParamsT(water_density, air_density, surface_tension, weno_epsilon, reinit_iterations,
+                              reinit_scaling, advection_precision)
+        h = ctypes.c_void_p()
+        rc = self.L.gb2d_create(ctypes.byref(self.grid), ctypes.byref(self.params), ctypes.byref(h))
+        if rc != 0:
+            raise GB2DError(rc, "gb2d_create failed")
+        self.h = h
+        self.ni, self.nj = ni, nj
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gb2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc):
+        if rc != 0:
+            raise GB2DError(rc, self.L.gb2d_last_error(self.h).decode(errors="replace"))
+        return rc
+
+    def shape(self, field):
+        ir, jr = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.gb2d_field_extent(ctypes.byref(self.grid), field, ctypes.byref(ir), ctypes.byref(jr)))
+        return (jr.value, ir.value)
+
+    def set(self, field, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.shape != self.shape(field):
+            raise ValueError(f"field {field}: expected shape {self.shape(field)}, got {a.shape}")
+        self._check(self.L.gb2d_set_field(self.h, field, _ptr(a)))
+
+    def get(self, field, out=None):
+        out = np.empty(self.shape(field)) if out is None else out
+        self._check(self.L.gb2d_get_field(self.h, field, _ptr(out)))
+        return out
+
+    def synchronize(self):
+        self._check(self.L.gb2d_synchronize(self.h))
+
+    def set_stream(self, stream_handle):
+        """Use a caller's CUDA stream (integer cudaStream_t, e.g. torch.cuda.Stream().cuda_stream); None = own."""
+        self._check(self.L.gb2d_set_stream(self.h, ctypes.c_void_p(stream_handle) if stream_handle else None))
+
+    def device_ptr(self, field):
+        p = ctypes.c_void_p()
+        self._check(self.L.gb2d_field_device_ptr(self.h, field, ctypes.byref(p)))
+        return p.value
+
+    def checkpoint_save(self):
+        self._check(self.L.gb2d_checkpoint_save(self.h))
+
+    def checkpoint_restore(self):
+        self._check(self.L.gb2d_checkpoint_restore(self.h))
+
+    def probe(self, enable):
+        self._check(self.L.gb2d_probe_enable(self.h, 1 if enable else 0))
+
+    def probe_read(self):
+        n, ms, by = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.gb2d_probe_read(self.h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(by)))
+        return n.value, ms.value, by.value
+
+    # Step interface of EULERIAN_FLUID_SOLVER_2D
+    def levelset_advection(self, dt):
+        self._check(self.L.gb2d_levelset_advection(self.h, dt))
+
+    def reinitialization(self):
+        self._check(self.L.gb2d_reinitialization(self.h))
+
+    def levelset_rk3(self, dt):
+        self._check(self.L.gb2d_levelset_rk3(self.h, dt))
+
+    def velocity_advection(self, dt):
+        self._check(self.L.gb2d_velocity_advection(self.h, dt))
+
+    def curvature(self):
+        self._check(self.L.gb2d_curvature(self.h))
+
+    def projection(self, dt, opts=None, allow_max_iters=False):
+        opts = opts or solve_opts()
+        st = SolveStatsT()
+        rc = self.L.gb2d_projection(self.h, dt, ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return st
+
+    # Pressure system (a10/a15)
+    def poisson_assemble(self, dt):
+        ni, nj = self.ni, self.nj
+        bx, by = np.zeros((nj, ni + 1)), np.zeros((nj + 1, ni))
+        dg, rhs = np.zeros((nj, ni)), np.zeros((nj, ni))
+        self._check(self.L.gb2d_poisson_assemble(self.h, dt, _ptr(bx), _ptr(by), _ptr(dg), _ptr(rhs)))
+        return bx, by, dg, rhs
+
+    def poisson_apply(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        self._check(self.L.gb2d_poisson_apply(self.h, _ptr(x), _ptr(y)))
+        return y
+
+    def poisson_solve(self, rhs, x0=None, opts=None):
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        x = np.zeros_like(rhs) if x0 is None else np.ascontiguousarray(x0, dtype=np.float64).copy()
+        opts = opts or solve_opts()
+        st = SolveStatsT()
+        self._check(self.L.gb2d_poisson_solve(self.h, _ptr(rhs), _ptr(x), ctypes.byref(opts), ctypes.byref(st)))
+        return x, st

@@ -1,0 +1,501 @@
+// C ABI of gb2d: context, state transfer and the step entry points.  The
+// orchestration mirrors EULERIAN_FLUID_SOLVER_2D's calls (see include/gb2d.h).
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "gb2d_internal.cuh"
+
+namespace gb2d {
+
+unsigned long long g_launches = 0;
+
+Space make_space(int ires, int jres, double x_min, double y_min, double x_max, double y_max) {
+  Space s;
+  double diff_x = x_max - x_min, diff_y = y_max - y_min;
+  s.dx = diff_x / (ires - 1);
+  s.dy = diff_y / (jres - 1);
+  double two_dx = 2 * s.dx, two_dy = 2 * s.dy;
+  double dx2 = s.dx * s.dx, dy2 = s.dy * s.dy;
+  s.odx = 1.0 / s.dx;
+  s.ody = 1.0 / s.dy;
+  s.o2dx = 1.0 / two_dx;
+  s.o2dy = 1.0 / two_dy;
+  s.odx2 = 1.0 / dx2;
+  s.ody2 = 1.0 / dy2;
+  return s;
+}
+
+}  // namespace gb2d
+
+using namespace gb2d;
+
+namespace {
+
+struct FieldDesc {
+  int g, nI, nJ;
+};
+
+bool field_desc(const gb2d_grid* g, int field, FieldDesc* d) {
+  int ni = g->ni, nj = g->nj;
+  switch (field) {
+    case GB2D_FIELD_PHI: *d = {2, ni, nj}; return true;
+    case GB2D_FIELD_U: *d = {2, ni + 1, nj}; return true;
+    case GB2D_FIELD_V: *d = {2, ni, nj + 1}; return true;
+    case GB2D_FIELD_UA: *d = {3, ni + 1, nj}; return true;
+    case GB2D_FIELD_VA: *d = {3, ni, nj + 1}; return true;
+    case GB2D_FIELD_P: *d = {1, ni, nj}; return true;
+    case GB2D_FIELD_KAPPA: *d = {0, ni, nj}; return true;
+    default: return false;
+  }
+}
+
+size_t field_count(const FieldDesc& d) { return (size_t)(d.nI + 2 * d.g) * (d.nJ + 2 * d.g); }
+
+double* field_ptr(gb2d_ctx* c, int field) {
+  switch (field) {
+    case GB2D_FIELD_PHI: return c->phi_buf[c->phi_cur];
+    case GB2D_FIELD_U: return c->u;
+    case GB2D_FIELD_V: return c->v;
+    case GB2D_FIELD_UA: return c->ua;
+    case GB2D_FIELD_VA: return c->va;
+    case GB2D_FIELD_P: return c->p;
+    case GB2D_FIELD_KAPPA: return c->kappa;
+    default: return nullptr;
+  }
+}
+
+int check_launch(gb2d_ctx* c, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(c->err, sizeof(c->err), "%s: %s", what, cudaGetErrorString(e));
+    return GB2D_ERR_CUDA;
+  }
+  return GB2D_OK;
+}
+
+int sync_check(gb2d_ctx* c, const char* what) {
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(c->err, sizeof(c->err), "%s: %s", what, cudaGetErrorString(e));
+    return GB2D_ERR_CUDA;
+  }
+  return GB2D_OK;
+}
+
+int spare(const gb2d_ctx* c, int a, int b = -1, int d = -1) {
+  for (int k = 0; k < 4; ++k)
+    if (k != a && k != b && k != d) return k;
+  return -1;
+  (void)c;
+}
+
+// One Levelset_Advection from buffer src into dst: WENO5 sweep, then phi's ghost extrapolation.
+void levelset_advection_into(gb2d_ctx* c, int src, int dst, double dt) {
+  int mixed = c->prm.advection_precision == GB2D_PRECISION_MIXED;
+  launch_weno5_advect(c->stream, c, c->phi_buf[src], c->phi_buf[dst], dt, mixed);
+  launch_extrapolate_ghosts(c->stream, c->phi_buf[dst], 2, c->grid.ni, c->grid.nj);
+}
+
+// One Reinitialization reading src (never written); sweeps alternate between a and b.
+int reinit_run(gb2d_ctx* c, int src, int a, int b) {
+  int mixed = c->prm.advection_precision == GB2D_PRECISION_MIXED;
+  double dtau = c->base.dx / (double)c->prm.reinit_scaling;
+  launch_reinit_sign(c->stream, c, c->phi_buf[src], c->sign);
+  int cur = src, nxt = a;
+  for (int it = 0; it < c->prm.reinit_iterations; ++it) {
+    launch_reinit_sweep(c->stream, c, c->phi_buf[cur], c->phi_buf[nxt], c->sign, dtau, mixed);
+    int prev = cur;
+    cur = nxt;
+    nxt = (prev == src) ? b : prev;
+  }
+  return cur;
+}
+
+void free_ctx(gb2d_ctx* c) {
+  if (!c) return;
+  if (c->solver) solver_destroy(c->solver);
+  double* bufs[] = {c->phi_buf[0], c->phi_buf[1], c->phi_buf[2], c->phi_buf[3], c->u, c->v, c->ua, c->va, c->p,
+                    c->kappa, c->sign, c->bx, c->by, c->diag, c->rhs, c->tmp_a, c->tmp_b, c->xw};
+  for (auto b : bufs)
+    if (b) cudaFree(b);
+  for (auto b : c->ckpt)
+    if (b) cudaFree(b);
+  if (c->sc) cudaFree(c->sc);
+  if (c->host_stage) cudaFreeHost(c->host_stage);
+  if (c->probe.ev) {
+    for (int k = 0; k < 2 * c->probe.cap; ++k) cudaEventDestroy(c->probe.ev[k]);
+    delete[] c->probe.ev;
+  }
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gb2d_field_extent(const gb2d_grid* grid, int field, int* ires, int* jres) {
+  FieldDesc d;
+  if (!grid || !ires || !jres || !field_desc(grid, field, &d)) return GB2D_ERR_ARG;
+  *ires = d.nI + 2 * d.g;
+  *jres = d.nJ + 2 * d.g;
+  return GB2D_OK;
+}
+
+int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out) {
+  if (!grid || !params || !out) return GB2D_ERR_ARG;
+  *out = nullptr;
+  if (grid->ni < 4 || grid->nj < 4 || !(grid->x_max > grid->x_min) || !(grid->y_max > grid->y_min)) return GB2D_ERR_ARG;
+  if ((long long)grid->ni * grid->nj > (1LL << 30)) return GB2D_ERR_ARG;
+  if (params->reinit_scaling <= 0 || params->reinit_iterations < 0 || !(params->water_density > 0) || !(params->air_density > 0))
+    return GB2D_ERR_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return GB2D_ERR_NO_DEVICE;
+  }
+  gb2d_ctx* c = new (std::nothrow) gb2d_ctx();
+  if (!c) return GB2D_ERR_ARG;
+  c->grid = *grid;
+  c->prm = *params;
+  int ni = grid->ni, nj = grid->nj;
+  c->base = make_space(ni, nj, grid->x_min, grid->y_min, grid->x_max, grid->y_max);
+  c->xs = make_space(ni + 1, nj, grid->x_min - 0.5 * c->base.dx, grid->y_min, grid->x_max + 0.5 * c->base.dx, grid->y_max);
+  c->ys = make_space(ni, nj + 1, grid->x_min, grid->y_min - 0.5 * c->base.dy, grid->x_max, grid->y_max + 0.5 * c->base.dy);
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+  c->stream = c->own_stream;
+  struct A {
+    double** p;
+    size_t n;
+  } allocs[] = {
+      {&c->phi_buf[0], (size_t)(ni + 4) * (nj + 4)}, {&c->phi_buf[1], (size_t)(ni + 4) * (nj + 4)},
+      {&c->phi_buf[2], (size_t)(ni + 4) * (nj + 4)}, {&c->phi_buf[3], (size_t)(ni + 4) * (nj + 4)},
+      {&c->u, (size_t)(ni + 5) * (nj + 4)},          {&c->v, (size_t)(ni + 4) * (nj + 5)},
+      {&c->ua, (size_t)(ni + 7) * (nj + 6)},         {&c->va, (size_t)(ni + 6) * (nj + 7)},
+      {&c->p, (size_t)(ni + 2) * (nj + 2)},          {&c->kappa, (size_t)ni * nj},
+      {&c->sign, (size_t)ni * nj},                   {&c->bx, (size_t)(ni + 1) * nj},
+      {&c->by, (size_t)ni * (nj + 1)},               {&c->diag, (size_t)ni * nj},
+      {&c->rhs, (size_t)ni * nj},                    {&c->tmp_a, (size_t)ni * nj},
+      {&c->tmp_b, (size_t)ni * nj},                  {&c->xw, (size_t)(ni + 2) * (nj + 2)},
+  };
+  for (auto& a : allocs) {
+    if (e != cudaSuccess) break;
+    e = cudaMalloc(a.p, a.n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(*a.p, 0, a.n * sizeof(double));
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&c->sc, sizeof(Scalars));
+  if (e == cudaSuccess) e = cudaMemset(c->sc, 0, sizeof(Scalars));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->host_stage, 64 * sizeof(double));
+  if (e != cudaSuccess) {
+    free_ctx(c);
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? GB2D_ERR_ARG : GB2D_ERR_CUDA;
+  }
+  c->phi_cur = 0;
+  char err[256];
+  c->solver = solver_create(ni, nj, err, sizeof err);
+  if (!c->solver) {
+    free_ctx(c);
+    cudaGetLastError();
+    return GB2D_ERR_CUDA;
+  }
+  *out = c;
+  return GB2D_OK;
+}
+
+int gb2d_destroy(gb2d_ctx* c) {
+  if (!c) return GB2D_ERR_ARG;
+  cudaStreamSynchronize(c->stream);
+  free_ctx(c);
+  return GB2D_OK;
+}
+
+const char* gb2d_last_error(const gb2d_ctx* c) { return c ? c->err : "null context"; }
+
+int gb2d_set_field(gb2d_ctx* c, int field, const double* host) {
+  FieldDesc d;
+  if (!c || !host || !field_desc(&c->grid, field, &d)) return GB2D_ERR_ARG;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(field_ptr(c, field), host, field_count(d) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  return sync_check(c, "set_field");
+}
+
+int gb2d_get_field(gb2d_ctx* c, int field, double* host) {
+  FieldDesc d;
+  if (!c || !host || !field_desc(&c->grid, field, &d)) return GB2D_ERR_ARG;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(host, field_ptr(c, field), field_count(d) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return sync_check(c, "get_field");
+}
+
+int gb2d_field_device_ptr(gb2d_ctx* c, int field, double** dptr) {
+  FieldDesc d;
+  if (!c || !dptr || !field_desc(&c->grid, field, &d)) return GB2D_ERR_ARG;
+  *dptr = field_ptr(c, field);
+  return GB2D_OK;
+}
+
+int gb2d_synchronize(gb2d_ctx* c) {
+  if (!c) return GB2D_ERR_ARG;
+  return sync_check(c, "synchronize");
+}
+
+int gb2d_set_stream(gb2d_ctx* c, void* stream) {
+  if (!c) return GB2D_ERR_ARG;
+  int rc = sync_check(c, "set_stream");
+  if (rc) return rc;
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return GB2D_OK;
+}
+
+int gb2d_probe_enable(gb2d_ctx* c, int enable) {
+  if (!c) return GB2D_ERR_ARG;
+  int rc = sync_check(c, "probe_enable");
+  if (rc) return rc;
+  if (enable && !c->probe.ev) {
+    c->probe.cap = 4096;
+    c->probe.ev = new (std::nothrow) cudaEvent_t[2 * c->probe.cap];
+    if (!c->probe.ev) return GB2D_ERR_ARG;
+    for (int k = 0; k < 2 * c->probe.cap; ++k) GB2D_CUDA_TRY(c, cudaEventCreate(&c->probe.ev[k]));
+  }
+  c->probe.on = enable ? 1 : 0;
+  c->probe.n = 0;
+  return GB2D_OK;
+}
+
+// Launches queued after convergence return at entry; they are excluded as the
+// ones shorter than half the median duration.
+int gb2d_probe_read(gb2d_ctx* c, int* launches, double* total_ms, double* bytes_per_launch) {
+  if (!c || !launches || !total_ms || !bytes_per_launch) return GB2D_ERR_ARG;
+  int rc = sync_check(c, "probe_read");
+  if (rc) return rc;
+  int n = c->probe.n;
+  float* ms = new (std::nothrow) float[n > 0 ? n : 1];
+  float* srt = new (std::nothrow) float[n > 0 ? n : 1];
+  if (!ms || !srt) {
+    delete[] ms;
+    delete[] srt;
+    return GB2D_ERR_ARG;
+  }
+  for (int k = 0; k < n; ++k) {
+    cudaError_t e = cudaEventElapsedTime(&ms[k], c->probe.ev[2 * k], c->probe.ev[2 * k + 1]);
+    if (e != cudaSuccess) {
+      delete[] ms;
+      delete[] srt;
+      snprintf(c->err, sizeof(c->err), "probe_read: %s", cudaGetErrorString(e));
+      return GB2D_ERR_CUDA;
+    }
+    srt[k] = ms[k];
+  }
+  // insertion sort is fine for a few thousand launches
+  for (int a = 1; a < n; ++a)
+    for (int b = a; b > 0 && srt[b - 1] > srt[b]; --b) {
+      float t = srt[b];
+      srt[b] = srt[b - 1];
+      srt[b - 1] = t;
+    }
+  double med = n > 0 ? srt[n / 2] : 0.0, tot = 0;
+  int used = 0;
+  for (int k = 0; k < n; ++k)
+    if (ms[k] >= 0.5 * med) {
+      tot += ms[k];
+      used++;
+    }
+  delete[] ms;
+  delete[] srt;
+  *launches = used;
+  *total_ms = tot;
+  *bytes_per_launch = c->probe.bytes;
+  c->probe.n = 0;
+  return GB2D_OK;
+}
+
+int gb2d_kernel_launches(unsigned long long* count) {
+  if (!count) return GB2D_ERR_ARG;
+  *count = gb2d::g_launches;
+  return GB2D_OK;
+}
+
+static double* ckpt_field(gb2d_ctx* c, int k) {
+  switch (k) {
+    case 0: return c->phi_buf[c->phi_cur];
+    case 1: return c->u;
+    case 2: return c->v;
+    case 3: return c->ua;
+    case 4: return c->va;
+    default: return c->p;
+  }
+}
+static const int kCkptFields[6] = {GB2D_FIELD_PHI, GB2D_FIELD_U, GB2D_FIELD_V, GB2D_FIELD_UA, GB2D_FIELD_VA, GB2D_FIELD_P};
+
+int gb2d_checkpoint_save(gb2d_ctx* c) {
+  if (!c) return GB2D_ERR_ARG;
+  for (int k = 0; k < 6; ++k) {
+    FieldDesc d;
+    field_desc(&c->grid, kCkptFields[k], &d);
+    size_t bytes = field_count(d) * sizeof(double);
+    if (!c->ckpt[k]) GB2D_CUDA_TRY(c, cudaMalloc(&c->ckpt[k], bytes));
+    GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->ckpt[k], ckpt_field(c, k), bytes, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  c->ckpt_phi_cur = c->phi_cur;
+  return check_launch(c, "checkpoint_save");
+}
+
+int gb2d_checkpoint_restore(gb2d_ctx* c) {
+  if (!c) return GB2D_ERR_ARG;
+  if (!c->ckpt[0]) {
+    snprintf(c->err, sizeof(c->err), "checkpoint_restore: no checkpoint saved");
+    return GB2D_ERR_ARG;
+  }
+  c->phi_cur = c->ckpt_phi_cur;
+  for (int k = 0; k < 6; ++k) {
+    FieldDesc d;
+    field_desc(&c->grid, kCkptFields[k], &d);
+    GB2D_CUDA_TRY(c, cudaMemcpyAsync(ckpt_field(c, k), c->ckpt[k], field_count(d) * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  }
+  return check_launch(c, "checkpoint_restore");
+}
+
+int gb2d_levelset_advection(gb2d_ctx* c, double dt) {
+  if (!c || !std::isfinite(dt)) return GB2D_ERR_ARG;
+  int dst = spare(c, c->phi_cur);
+  levelset_advection_into(c, c->phi_cur, dst, dt);
+  c->phi_cur = dst;
+  return check_launch(c, "levelset_advection");
+}
+
+int gb2d_reinitialization(gb2d_ctx* c) {
+  if (!c) return GB2D_ERR_ARG;
+  int a = spare(c, c->phi_cur), b = spare(c, c->phi_cur, a);
+  c->phi_cur = reinit_run(c, c->phi_cur, a, b);
+  return check_launch(c, "reinitialization");
+}
+
+int gb2d_levelset_rk3(gb2d_ctx* c, double dt) {
+  if (!c || !std::isfinite(dt)) return GB2D_ERR_ARG;
+  cudaStream_t s = c->stream;
+  int A = c->phi_cur, B = spare(c, A), C = spare(c, A, B), D = spare(c, A, B, C);
+  // Level-set TVD-RK3 (EULERIAN_FLUID_SOLVER_2D.h:1694-1717); A keeps phi^0.
+  levelset_advection_into(c, A, B, dt);
+  levelset_advection_into(c, B, C, dt);
+  launch_blend(s, c, c->phi_buf[A], c->phi_buf[C], 0.75, 0.25);
+  levelset_advection_into(c, C, B, dt);
+  launch_blend(s, c, c->phi_buf[A], c->phi_buf[B], 1 / 3.0, 2 / 3.0);
+  // Reinitialisation TVD-RK3 (:1719-1741); B keeps the stage-0 level set.
+  int R1 = reinit_run(c, B, C, D);
+  int o1 = R1 == C ? D : C;
+  int R2 = reinit_run(c, R1, o1, A);
+  launch_blend(s, c, c->phi_buf[B], c->phi_buf[R2], 0.75, 0.25);
+  int o2 = spare(c, B, R2);
+  int o3 = spare(c, B, R2, o2);
+  int R3 = reinit_run(c, R2, o2, o3);
+  launch_blend(s, c, c->phi_buf[B], c->phi_buf[R3], 1 / 3.0, 2 / 3.0);
+  c->phi_cur = R3;
+  return check_launch(c, "levelset_rk3");
+}
+
+int gb2d_velocity_advection(gb2d_ctx* c, double dt) {
+  if (!c || !std::isfinite(dt)) return GB2D_ERR_ARG;
+  int ni = c->grid.ni, nj = c->grid.nj;
+  launch_fill_ghost_copy(c->stream, c->ua, 3, c->u, 2, ni + 1, nj, 3);
+  launch_fill_ghost_copy(c->stream, c->va, 3, c->v, 2, ni, nj + 1, 3);
+  launch_eno3(c->stream, c, dt);
+  return check_launch(c, "velocity_advection");
+}
+
+static int curvature_impl(gb2d_ctx* c) {
+  double* phi = c->phi_buf[c->phi_cur];
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->flag, 0, sizeof(int), c->stream));
+  launch_extrapolate_ghosts(c->stream, phi, 2, c->grid.ni, c->grid.nj);
+  launch_curvature(c->stream, c, phi, c->kappa, &c->sc->flag);
+  return check_launch(c, "curvature");
+}
+
+static int read_flag(gb2d_ctx* c) {
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->host_stage, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+  int rc = sync_check(c, "read flags");
+  if (rc) return rc;
+  const Scalars* h = (const Scalars*)c->host_stage;
+  if (h->flag & 2) {
+    snprintf(c->err, sizeof(c->err), "curvature: |grad phi| is zero at a node (the reference exits here)");
+    return GB2D_ERR_ZERO_GRADIENT;
+  }
+  return GB2D_OK;
+}
+
+int gb2d_curvature(gb2d_ctx* c) {
+  if (!c) return GB2D_ERR_ARG;
+  int rc = curvature_impl(c);
+  if (rc) return rc;
+  return read_flag(c);
+}
+
+int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
+  if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
+  double* phi = c->phi_buf[c->phi_cur];
+  int rc = curvature_impl(c);
+  if (rc) return rc;
+  launch_assemble(c->stream, c, phi, dt);
+  if ((rc = check_launch(c, "assemble"))) return rc;
+  gb2d_solve_stats local;
+  memset(&local, 0, sizeof local);
+  int src = solver_solve(c, c->rhs, c->p, o, &local);
+  if (src != GB2D_OK && src != GB2D_ERR_MAX_ITERS) return src;
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->maxu_bits, 0, 2 * sizeof(unsigned long long), c->stream));
+  launch_velocity_update(c->stream, c, phi, dt, c->sc);
+  if ((rc = read_flag(c))) return rc;
+  const Scalars* h = (const Scalars*)c->host_stage;
+  double mu, mv;
+  memcpy(&mu, &h->maxu_bits, sizeof mu);
+  memcpy(&mv, &h->maxv_bits, sizeof mv);
+  local.max_velocity_x = mu;
+  local.max_velocity_y = mv;
+  if (st) *st = local;
+  return src;
+}
+
+int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {
+  if (!c || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
+  int rc = curvature_impl(c);
+  if (rc) return rc;
+  launch_assemble(c->stream, c, c->phi_buf[c->phi_cur], dt);
+  if ((rc = check_launch(c, "assemble"))) return rc;
+  size_t ni = c->grid.ni, nj = c->grid.nj;
+  if (bx) GB2D_CUDA_TRY(c, cudaMemcpyAsync(bx, c->bx, (ni + 1) * nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (by) GB2D_CUDA_TRY(c, cudaMemcpyAsync(by, c->by, ni * (nj + 1) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (diag) GB2D_CUDA_TRY(c, cudaMemcpyAsync(diag, c->diag, ni * nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (rhs) GB2D_CUDA_TRY(c, cudaMemcpyAsync(rhs, c->rhs, ni * nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = sync_check(c, "poisson_assemble"))) return rc;
+  return read_flag(c);
+}
+
+int gb2d_poisson_apply(gb2d_ctx* c, const double* x, double* y) {
+  if (!c || !x || !y) return GB2D_ERR_ARG;
+  size_t n = (size_t)c->grid.ni * c->grid.nj;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->tmp_a, x, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_poisson_apply_exact(c->stream, c, c->tmp_a, c->tmp_b);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(y, c->tmp_b, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return sync_check(c, "poisson_apply");
+}
+
+int gb2d_poisson_solve(gb2d_ctx* c, const double* rhs, double* x, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
+  if (!c || !rhs || !x || !o) return GB2D_ERR_ARG;
+  int ni = c->grid.ni, nj = c->grid.nj;
+  size_t n = (size_t)ni * nj;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->rhs, rhs, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->tmp_a, x, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_copy_interior(c->stream, c->tmp_a, 0, c->xw, 1, ni, nj);
+  gb2d_solve_stats local;
+  memset(&local, 0, sizeof local);
+  int src = solver_solve(c, c->rhs, c->xw, o, &local);
+  if (src != GB2D_OK && src != GB2D_ERR_MAX_ITERS) return src;
+  launch_copy_interior(c->stream, c->xw, 1, c->tmp_a, 0, ni, nj);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(x, c->tmp_a, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  int rc = sync_check(c, "poisson_solve");
+  if (rc) return rc;
+  if (st) *st = local;
+  return src;
+}
+
+}  // extern "C"

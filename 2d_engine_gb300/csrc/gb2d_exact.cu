@@ -1,0 +1,554 @@
+// FP64 kernels that reproduce the reference's own FP64 CPU arithmetic: ghost
+// fills, WENO5 advection and reinitialisation sweeps, ENO3 velocity advection,
+// curvature, ghost-fluid Poisson assembly and the GFM velocity update.
+// Built with --fmad=false: every multiply and add rounds separately, in the
+// reference's association order, so results match it bit for bit (the sine of
+// the smeared Heaviside is the only libm call and may differ in the last ulp).
+// The "mixed" advection variants (FP32 flux evaluation, FP64 state) live here
+// too so that they share the loaders.
+#include <cstdio>
+
+#include "gb2d_internal.cuh"
+#include "gb2d_schemes.cuh"
+
+namespace gb2d {
+
+namespace {
+
+inline unsigned blocks_for(size_t n, int threads = kThreads) { return (unsigned)((n + threads - 1) / threads); }
+
+// FillGhostCellsFrom (FIELD_STRUCTURE_2D.h:374-449): interior copied, each ghost
+// layer copies the second interior line, corners untouched.
+__global__ void k_fill_ghost_copy(double* dst_a, int gd, const double* __restrict__ src_a, int gs, int nI, int nJ, int g) {
+  DField d = dfield(dst_a, gd, nI, nJ);
+  DField s = dfield((double*)src_a, gs, nI, nJ);
+  int W = nI + 2 * g, H = nJ + 2 * g;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)W * H; t += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % W) - g, j = (int)(t / W) - g;
+    bool in_i = i >= 0 && i < nI, in_j = j >= 0 && j < nJ;
+    if (in_i && in_j)
+      GB_AT(d, i, j) = GB_AT(s, i, j);
+    else if (in_j)
+      GB_AT(d, i, j) = GB_AT(s, i < 0 ? 1 : nI - 2, j);
+    else if (in_i)
+      GB_AT(d, i, j) = GB_AT(s, i, j < 0 ? 1 : nJ - 2);
+  }
+}
+
+// FillGhostCellsContinuousDerivativesFrom(phi, true, tid) on the field itself
+// (FIELD_STRUCTURE_2D.h:641-716).  One thread per boundary line keeps the
+// reference's layer order: left/bottom outermost first (the outer layer reads
+// the previous inner value), right/top innermost first.
+__global__ void k_extrapolate(double* a, int g, int nI, int nJ) {
+  DField f = dfield(a, g, nI, nJ);
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nJ) {
+    int j = t;
+    for (int i = -g; i <= -1; ++i) GB_AT(f, i, j) = 2.0 * GB_AT(f, i + 1, j) - GB_AT(f, i + 2, j);
+    for (int i = nI; i <= nI - 1 + g; ++i) GB_AT(f, i, j) = 2.0 * GB_AT(f, i - 1, j) - GB_AT(f, i - 2, j);
+  }
+  if (t < nI) {
+    int i = t;
+    for (int j = nJ; j <= nJ - 1 + g; ++j) GB_AT(f, i, j) = 2.0 * GB_AT(f, i, j - 1) - GB_AT(f, i, j - 2);
+    for (int j = -g; j <= -1; ++j) GB_AT(f, i, j) = 2.0 * GB_AT(f, i, j + 1) - GB_AT(f, i, j + 2);
+  }
+}
+
+// Reads of the WENO scratch copy (scalar_field_ghost, ghost 3) synthesised from
+// phi's interior: ghost layers hold the second interior line.
+__device__ __forceinline__ void gather_x(const DField& s, int i, int j, double q[7]) {
+  const int nI = s.nI;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    int ii = i - 3 + k;
+    ii = ii < 0 ? 1 : (ii >= nI ? nI - 2 : ii);
+    q[k] = __ldg(&GB_AT(s, ii, j));
+  }
+}
+__device__ __forceinline__ void gather_y(const DField& s, int i, int j, double q[7]) {
+  const int nJ = s.nJ;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) {
+    int jj = j - 3 + k;
+    jj = jj < 0 ? 1 : (jj >= nJ ? nJ - 2 : jj);
+    q[k] = __ldg(&GB_AT(s, i, jj));
+  }
+}
+
+struct LSArgs {
+  int ni, nj;
+  double odx, ody, eps;
+};
+
+// WENO5th (ADVECTION_METHOD_2D.h:508-663) for the node-grid level set: writes
+// dst's interior from src, copies src's ghost ring (the sweep leaves phi's own
+// ghosts to the caller's extrapolation).
+template <bool MIXED>
+__global__ void k_weno5_advect(const double* __restrict__ src_a, double* __restrict__ dst_a, const double* __restrict__ ua_a,
+                               const double* __restrict__ va_a, LSArgs a, double dt) {
+  int ni = a.ni, nj = a.nj;
+  int W = ni + 4, H = nj + 4;
+  int ix = blockIdx.x * blockDim.x + threadIdx.x, jy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= W || jy >= H) return;
+  int i = ix - 2, j = jy - 2;
+  DField src = dfield((double*)src_a, 2, ni, nj), dst = dfield(dst_a, 2, ni, nj);
+  if (i < 0 || j < 0 || i >= ni || j >= nj) {
+    GB_AT(dst, i, j) = GB_AT(src, i, j);
+    return;
+  }
+  DField ua = dfield((double*)ua_a, 3, ni + 1, nj), va = dfield((double*)va_a, 3, ni, nj + 1);
+  double q[7];
+  double u = (__ldg(&GB_AT(ua, i + 1, j)) + __ldg(&GB_AT(ua, i, j))) * 0.5;
+  double v = (__ldg(&GB_AT(va, i, j + 1)) + __ldg(&GB_AT(va, i, j))) * 0.5;
+  double fx, fy;
+  if (MIXED) {
+    float m, p;
+    gather_x(src, i, j, q);
+    weno5_pair_f32(q, (float)a.odx, (float)a.eps, m, p);
+    fx = u > 0 ? (double)m : (double)p;
+    gather_y(src, i, j, q);
+    weno5_pair_f32(q, (float)a.ody, (float)a.eps, m, p);
+    fy = v > 0 ? (double)m : (double)p;
+  } else {
+    double m, p;
+    gather_x(src, i, j, q);
+    weno5_pair(q, a.odx, a.eps, m, p);
+    fx = u > 0 ? m : p;
+    gather_y(src, i, j, q);
+    weno5_pair(q, a.ody, a.eps, m, p);
+    fy = v > 0 ? m : p;
+  }
+  GB_AT(dst, i, j) = GB_AT(src, i, j) - dt * (u * fx + v * fy);
+}
+
+// Sign function of Reinitialization (EULERIAN_FLUID_SOLVER_2D.h:2431-2435).
+__global__ void k_reinit_sign(const double* __restrict__ phi_a, double* __restrict__ S, int ni, int nj, double dx) {
+  DField phi = dfield((double*)phi_a, 2, ni, nj);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % ni), j = (int)(t / ni);
+    double p = GB_AT(phi, i, j);
+    S[t] = p / sqrt(p * p + dx * dx);
+  }
+}
+
+// WENO5thReinitialization (ADVECTION_METHOD_2D.h:1401-1658).
+template <bool MIXED>
+__global__ void k_reinit_sweep(const double* __restrict__ src_a, double* __restrict__ dst_a, const double* __restrict__ S, LSArgs a,
+                               double dtau) {
+  int ni = a.ni, nj = a.nj;
+  int W = ni + 4, H = nj + 4;
+  int ix = blockIdx.x * blockDim.x + threadIdx.x, jy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= W || jy >= H) return;
+  int i = ix - 2, j = jy - 2;
+  DField src = dfield((double*)src_a, 2, ni, nj), dst = dfield(dst_a, 2, ni, nj);
+  double old = GB_AT(src, i, j);
+  if (i < 0 || j < 0 || i >= ni || j >= nj) {
+    GB_AT(dst, i, j) = old;
+    return;
+  }
+  double q[7];
+  double out = old;
+  if (MIXED) {
+    float mx, px, my, py, h;
+    gather_x(src, i, j, q);
+    weno5_pair_f32(q, (float)a.odx, (float)a.eps, mx, px);
+    gather_y(src, i, j, q);
+    weno5_pair_f32(q, (float)a.ody, (float)a.eps, my, py);
+    double s = __ldg(&S[i + (size_t)j * ni]);
+    if (godunov_h<float>((float)s, mx, px, my, py, h)) out = old - dtau * s * (double)h;
+  } else {
+    double mx, px, my, py, h;
+    gather_x(src, i, j, q);
+    weno5_pair(q, a.odx, a.eps, mx, px);
+    gather_y(src, i, j, q);
+    weno5_pair(q, a.ody, a.eps, my, py);
+    double s = __ldg(&S[i + (size_t)j * ni]);
+    if (godunov_h<double>(s, mx, px, my, py, h)) out = old - dtau * s * h;
+  }
+  GB_AT(dst, i, j) = out;
+}
+
+// Shu-Osher blend of the TVD-RK3 stages (EULERIAN_FLUID_SOLVER_2D.h:1706-1741): interior only.
+__global__ void k_blend(const double* __restrict__ keep_a, double* phi_a, int ni, int nj, double c0, double c1) {
+  DField keep = dfield((double*)keep_a, 2, ni, nj), phi = dfield(phi_a, 2, ni, nj);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % ni), j = (int)(t / ni);
+    GB_AT(phi, i, j) = c0 * GB_AT(keep, i, j) + c1 * GB_AT(phi, i, j);
+  }
+}
+
+struct EnoArgs {
+  int ni, nj;
+  Space xs, ys;
+};
+
+// ENO3rd on both MAC components (ADVECTION_METHOD_2D.h:2038-2231) as called by
+// Solve_Velocity (ADVECTION_2D.cpp:83-122): both read only the advecting copies
+// UA/VA (already refreshed from U/V), so one launch updates U and V.
+__global__ void k_eno3(double* __restrict__ u_a, double* __restrict__ v_a, const double* __restrict__ ua_a, const double* __restrict__ va_a,
+                       EnoArgs a, double dt) {
+  int ni = a.ni, nj = a.nj;
+  size_t nu = (size_t)(ni + 1) * nj, nv = (size_t)ni * (nj + 1);
+  DField ua = dfield((double*)ua_a, 3, ni + 1, nj), va = dfield((double*)va_a, 3, ni, nj + 1);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nu + nv; t += (size_t)gridDim.x * blockDim.x) {
+    bool xc = t < nu;
+    int nI = xc ? ni + 1 : ni;
+    size_t k = xc ? t : t - nu;
+    int i = (int)(k % nI), j = (int)(k / nI);
+    const DField& g = xc ? ua : va;
+    const Space& s = xc ? a.xs : a.ys;
+    double q[7];
+    for (int m = 0; m < 7; ++m) q[m] = __ldg(&GB_AT(g, i - 3 + m, j));
+    double mx, px, my, py;
+    eno3_pair(q, s.odx, s.o2dx, s.odx / 3, s.dx, mx, px);
+    for (int m = 0; m < 7; ++m) q[m] = __ldg(&GB_AT(g, i, j - 3 + m));
+    eno3_pair(q, s.ody, s.o2dy, s.ody / 3, s.dy, my, py);
+    double uu, vv;
+    if (xc) {
+      uu = GB_AT(ua, i, j);
+      vv = (GB_AT(va, i, j) + GB_AT(va, i, j + 1) + GB_AT(va, i - 1, j) + GB_AT(va, i - 1, j + 1)) * 0.25;
+    } else {
+      uu = (GB_AT(ua, i, j - 1) + GB_AT(ua, i + 1, j - 1) + GB_AT(ua, i, j) + GB_AT(ua, i + 1, j)) * 0.25;
+      vv = GB_AT(va, i, j);
+    }
+    double fx = uu > 0 ? mx : px, fy = vv > 0 ? my : py;
+    DField out = xc ? dfield(u_a, 2, ni + 1, nj) : dfield(v_a, 2, ni, nj + 1);
+    GB_AT(out, i, j) = GB_AT(out, i, j) - dt * (uu * fx + vv * fy);
+  }
+}
+
+// ComputeCurvaturesThread with curvature_by_levelset (LEVELSET_2D.h:898-990);
+// phi's ghosts must already be extrapolated.
+__global__ void k_curvature(const double* __restrict__ phi_a, double* __restrict__ kappa, int ni, int nj, Space s, int* flag) {
+  DField phi = dfield((double*)phi_a, 2, ni, nj);
+  double tol = 1.0 / (s.dx < s.dy ? s.dx : s.dy);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % ni), j = (int)(t / ni);
+    double c = GB_AT(phi, i, j);
+    double l = GB_AT(phi, i - 1, j), r = GB_AT(phi, i + 1, j), b = GB_AT(phi, i, j - 1), tp = GB_AT(phi, i, j + 1);
+    double px = (r - l) * s.o2dx;
+    double py = (tp - b) * s.o2dy;
+    double pxx = (r - 2 * c + l) * s.odx2;
+    double pyy = (tp - 2 * c + b) * s.ody2;
+    double pxy = (GB_AT(phi, i + 1, j + 1) - GB_AT(phi, i + 1, j - 1) - GB_AT(phi, i - 1, j + 1) + GB_AT(phi, i - 1, j - 1)) * s.o2dx * s.o2dy;
+    double mag = sqrt(px * px + py * py);
+    double deno = mag * mag * mag;
+    double curv;
+    if (deno != 0) {
+      double od = 1.0 / deno;
+      curv = -(px * px * pyy - 2.0 * px * py * pxy + py * py * pxx) * od;
+    } else {
+      px = (r - c) * s.odx;
+      py = (tp - c) * s.ody;
+      mag = sqrt(px * px + py * py);
+      deno = mag * mag * mag;
+      if (deno == 0) {
+        atomicOr(flag, 2);
+        continue;
+      }
+      double od = 1.0 / deno;
+      curv = -(px * px * pyy - 2.0 * px * py * pxy + py * py * pxx) * od;
+    }
+    if (fabs(curv) <= tol)
+      kappa[t] = curv;
+    else if (curv > tol)
+      kappa[t] = tol;
+    else if (curv < -tol)
+      kappa[t] = -tol;
+  }
+}
+
+struct AsmArgs {
+  int ni, nj;
+  Space s;
+  double water, air, sigma, one_over_dt, inv_dxdx, inv_dydy;
+};
+
+__device__ __forceinline__ double inv_density(double phi, const AsmArgs& a) {
+  double r = 1.0;
+  if (phi <= 0)
+    r = a.air;
+  else if (phi > 0)
+    r = a.water;
+  return 1.0 / r;
+}
+
+// 1/rho at a node or at its copied ghost (POISSON_SOLVER.cpp:131-138: the ghost
+// layer copies the second interior line).
+__device__ __forceinline__ double vnode(const DField& phi, int i, int j, const AsmArgs& a) {
+  i = i < 0 ? 1 : (i >= a.ni ? a.ni - 2 : i);
+  j = j < 0 ? 1 : (j >= a.nj ? a.nj - 2 : j);
+  return inv_density(GB_AT(phi, i, j), a);
+}
+
+__device__ __forceinline__ double face_beta(double vc, double vn, double pc, double pn) {
+  return vc * vn * (fabs(pn) + fabs(pc)) / (vc * fabs(pn) + vn * fabs(pc));
+}
+
+// Face weights of BuildLinearSystemNodeJumpConditionVaribleCoefficient
+// (POISSON_SOLVER.cpp:743-746): one value per face, symmetric in IEEE arithmetic.
+__global__ void k_faces(const double* __restrict__ phi_a, double* __restrict__ bx, double* __restrict__ by, AsmArgs a) {
+  int ni = a.ni, nj = a.nj;
+  DField phi = dfield((double*)phi_a, 2, ni, nj);
+  size_t nx = (size_t)(ni + 1) * nj, ny = (size_t)ni * (nj + 1);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nx + ny; t += (size_t)gridDim.x * blockDim.x) {
+    if (t < nx) {
+      int i = (int)(t % (ni + 1)), j = (int)(t / (ni + 1));
+      bx[t] = face_beta(vnode(phi, i, j, a), vnode(phi, i - 1, j, a), GB_AT(phi, i, j), GB_AT(phi, i - 1, j));
+    } else {
+      size_t k = t - nx;
+      int i = (int)(k % ni), j = (int)(k / ni);
+      by[k] = face_beta(vnode(phi, i, j, a), vnode(phi, i, j - 1, a), GB_AT(phi, i, j), GB_AT(phi, i, j - 1));
+    }
+  }
+}
+
+__device__ __forceinline__ double jc_at(const double* kappa, int i, int j, const AsmArgs& a) {
+  if (i < 0 || j < 0 || i >= a.ni || j >= a.nj) return 0.0;  // jc_on_solution ghosts stay zero
+  return a.sigma * kappa[i + (size_t)j * a.ni];
+}
+
+// Jump flux of one arm (POISSON_SOLVER.cpp:881-948) without the derivative-jump
+// part, which vanishes because jc_on_derivative is zeroed (PROJECTION_2D.h:501-504).
+__device__ __forceinline__ double arm_flux(double pc, double pn, double jcc, double jcn, double beta, double o2, bool lower) {
+  if ((pc <= 0 && pn <= 0) || (pc > 0 && pn > 0)) return 0.0;
+  double ac = fabs(pc), an = fabs(pn);
+  double av = (jcc * an + jcn * ac) / (ac + an);
+  // left/bottom arms: +o2*a*beta when phi_c <= 0 < phi_n; right/top arms have the same sign rule
+  (void)lower;
+  if (pc <= 0 && pn > 0) return o2 * av * beta;
+  if (pc > 0 && pn <= 0) return -o2 * av * beta;
+  return 0.0;
+}
+
+// Diagonal (dx^2 only, POISSON_SOLVER.cpp:872) and right-hand side -div - F_X - F_Y.
+__global__ void k_rhs_diag(const double* __restrict__ phi_a, const double* __restrict__ kappa, const double* __restrict__ u_a,
+                           const double* __restrict__ v_a, const double* __restrict__ bx, const double* __restrict__ by, double* __restrict__ diag,
+                           double* __restrict__ rhs, AsmArgs a) {
+  int ni = a.ni, nj = a.nj;
+  DField phi = dfield((double*)phi_a, 2, ni, nj);
+  DField u = dfield((double*)u_a, 2, ni + 1, nj), v = dfield((double*)v_a, 2, ni, nj + 1);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % ni), j = (int)(t / ni);
+    double bl = bx[i + (size_t)j * (ni + 1)], br = bx[i + 1 + (size_t)j * (ni + 1)];
+    double bb = by[i + (size_t)j * ni], bt = by[i + (size_t)(j + 1) * ni];
+    double coef = 0;
+    if (i > 0) coef += bl;
+    if (i < ni - 1) coef += br;
+    if (j > 0) coef += bb;
+    if (j < nj - 1) coef += bt;
+    if (i == 0 && j == 0) {  // Neumann arms of the first cell (POISSON_SOLVER.cpp:789-806)
+      if (i - 1 < 0) coef += bl;
+      if (i + 1 > ni - 1) coef += br;
+      if (j - 1 < 0) coef += bb;
+      if (j + 1 > nj - 1) coef += bt;
+    }
+    if (coef == 0) coef = 1;
+    diag[t] = a.inv_dxdx * coef;
+
+    double pc = GB_AT(phi, i, j);
+    double jcc = jc_at(kappa, i, j, a);
+    double FL = arm_flux(pc, GB_AT(phi, i - 1, j), jcc, jc_at(kappa, i - 1, j, a), bl, a.s.odx2, true);
+    double FR = arm_flux(pc, GB_AT(phi, i + 1, j), jcc, jc_at(kappa, i + 1, j, a), br, a.s.odx2, false);
+    double FB = arm_flux(pc, GB_AT(phi, i, j - 1), jcc, jc_at(kappa, i, j - 1, a), bb, a.s.ody2, true);
+    double FT = arm_flux(pc, GB_AT(phi, i, j + 1), jcc, jc_at(kappa, i, j + 1, a), bt, a.s.ody2, false);
+    double div = a.s.odx * (GB_AT(u, i + 1, j) - GB_AT(u, i, j)) + a.s.ody * (GB_AT(v, i, j + 1) - GB_AT(v, i, j));
+    div *= a.one_over_dt;
+    double FX = FL + FR, FY = FB + FT;
+    rhs[t] = -div - FX - FY;
+  }
+}
+
+// CSR_MATRIX::Multiply in the builder's row order (left, right, bottom, top, diagonal).
+__global__ void k_apply_exact(const double* __restrict__ bx, const double* __restrict__ by, const double* __restrict__ diag,
+                              const double* __restrict__ x, double* __restrict__ y, int ni, int nj, double idx2, double idy2) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % ni), j = (int)(t / ni);
+    double acc = 0;
+    if (i > 0) acc += -bx[i + (size_t)j * (ni + 1)] * idx2 * x[t - 1];
+    if (i < ni - 1) acc += -bx[i + 1 + (size_t)j * (ni + 1)] * idx2 * x[t + 1];
+    if (j > 0) acc += -by[i + (size_t)j * ni] * idy2 * x[t - ni];
+    if (j < nj - 1) acc += -by[i + (size_t)(j + 1) * ni] * idy2 * x[t + ni];
+    acc += diag[t] * x[t];
+    y[t] = acc;
+  }
+}
+
+// HeavisideFunction (PROJECTION_2D.h:1441-1461) with the reference's PI = 3.141592.
+__device__ __forceinline__ double heaviside(double phi, double eps) {
+  const double PI_REF = 3.141592;
+  if (phi < -eps) return 0;
+  if (phi > eps) return 1;
+  double oe = 1.0 / eps, opi = 1.0 / PI_REF;
+  return 0.5 + phi * oe * 0.5 + 0.5 * opi * sin(PI_REF * phi * oe);
+}
+
+__device__ __forceinline__ void block_max_bits(double v, unsigned long long* out) {
+  unsigned long long b = __double_as_longlong(v);
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, b, o);
+    b = w > b ? w : b;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, b);
+}
+
+// UpdateVelocityByPressureGradientVariableDensity (PROJECTION_2D.h:1297-1416):
+// same-sign faces use the node density on the + side, interface faces the
+// smeared-Heaviside density of the face-averaged phi (eps = 1.5 dx) and the
+// |phi|-weighted jump.  Pressure ghosts are zero; wall faces (bc < 0) are skipped.
+__global__ void k_velocity_update(const double* __restrict__ phi_a, const double* __restrict__ p_a, const double* __restrict__ kappa,
+                                  double* __restrict__ u_a, double* __restrict__ v_a, AsmArgs a, double dt, Scalars* sc) {
+  int ni = a.ni, nj = a.nj;
+  DField phi = dfield((double*)phi_a, 2, ni, nj), p = dfield((double*)p_a, 1, ni, nj);
+  DField u = dfield(u_a, 2, ni + 1, nj), v = dfield(v_a, 2, ni, nj + 1);
+  double odx = 1.0 / a.s.dx, ody = 1.0 / a.s.dy;
+  double eh = 1.5 * a.s.dx, ev = 1.5 * a.s.dy;
+  size_t n = (size_t)ni * nj;
+  double mx = 0, my = 0;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < 2 * n; t += (size_t)gridDim.x * blockDim.x) {
+    bool xc = t < n;
+    size_t k = xc ? t : t - n;
+    int i = (int)(k % ni), j = (int)(k / ni);
+    int in = xc ? i - 1 : i, jn = xc ? j : j - 1;
+    double l0 = GB_AT(phi, i, j), ln = GB_AT(phi, in, jn);
+    double rho_ij = l0 <= 0 ? a.air : a.water;
+    double oor = 1 / rho_ij;
+    double jcc = jc_at(kappa, i, j, a), jcn = jc_at(kappa, in, jn, a);
+    double gam = (jcn * fabs(l0) + jcc * fabs(ln)) / (fabs(l0) + fabs(ln));
+    double dp = GB_AT(p, i, j) - GB_AT(p, in, jn);
+    double od = xc ? odx : ody;
+    double* w = xc ? &GB_AT(u, i, j) : &GB_AT(v, i, j);
+    if (l0 * ln >= 0) {
+      *w -= dt * dp * oor * od;
+    } else {
+      double dh = a.air + (a.water - a.air) * heaviside(0.5 * (l0 + ln), xc ? eh : ev);
+      double odh = 1 / dh;
+      if (l0 < 0)
+        *w -= dt * (dp + gam) * odh * od;
+      else if (l0 > 0)
+        *w -= dt * (dp - gam) * odh * od;
+    }
+    double aw = fabs(*w);
+    if (xc)
+      mx = aw > mx ? aw : mx;
+    else
+      my = aw > my ? aw : my;
+  }
+  block_max_bits(mx, &sc->maxu_bits);
+  block_max_bits(my, &sc->maxv_bits);
+}
+
+__global__ void k_copy_interior(const double* __restrict__ src_a, int gs, double* __restrict__ dst_a, int gd, int nI, int nJ) {
+  DField s = dfield((double*)src_a, gs, nI, nJ), d = dfield(dst_a, gd, nI, nJ);
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)nI * nJ; t += (size_t)gridDim.x * blockDim.x) {
+    int i = (int)(t % nI), j = (int)(t / nI);
+    GB_AT(d, i, j) = GB_AT(s, i, j);
+  }
+}
+
+inline unsigned grid_cap(size_t n) {
+  unsigned b = blocks_for(n);
+  return b < 152u * 16u ? (b ? b : 1u) : 152u * 16u;
+}
+
+inline dim3 grid2d(int W, int H, dim3 blk) { return dim3((W + blk.x - 1) / blk.x, (H + blk.y - 1) / blk.y); }
+
+LSArgs ls_args(const gb2d_ctx* c) { return LSArgs{c->grid.ni, c->grid.nj, c->base.odx, c->base.ody, c->prm.weno_epsilon}; }
+
+AsmArgs asm_args(const gb2d_ctx* c, double dt) {
+  AsmArgs a;
+  a.ni = c->grid.ni;
+  a.nj = c->grid.nj;
+  a.s = c->base;
+  a.water = c->prm.water_density;
+  a.air = c->prm.air_density;
+  a.sigma = c->prm.surface_tension;
+  a.one_over_dt = 1.0 / dt;
+  a.inv_dxdx = 1.0 / (c->base.dx * c->base.dx);
+  a.inv_dydy = 1.0 / (c->base.dy * c->base.dy);
+  return a;
+}
+
+}  // namespace
+
+void launch_fill_ghost_copy(cudaStream_t s, double* dst, int gd, const double* src, int gs, int nI, int nJ, int g) {
+  size_t n = (size_t)(nI + 2 * g) * (nJ + 2 * g);
+  k_fill_ghost_copy<<<grid_cap(n), kThreads, 0, s>>>(dst, gd, src, gs, nI, nJ, g);
+  GB_LAUNCHED(1);
+}
+
+void launch_extrapolate_ghosts(cudaStream_t s, double* f, int g, int nI, int nJ) {
+  int n = nI > nJ ? nI : nJ;
+  k_extrapolate<<<blocks_for(n, 128), 128, 0, s>>>(f, g, nI, nJ);
+  GB_LAUNCHED(1);
+}
+
+void launch_weno5_advect(cudaStream_t s, const gb2d_ctx* c, const double* src, double* dst, double dt, int mixed) {
+  dim3 blk(32, 8);
+  dim3 grd = grid2d(c->grid.ni + 4, c->grid.nj + 4, blk);
+  if (mixed)
+    k_weno5_advect<true><<<grd, blk, 0, s>>>(src, dst, c->ua, c->va, ls_args(c), dt);
+  else
+    k_weno5_advect<false><<<grd, blk, 0, s>>>(src, dst, c->ua, c->va, ls_args(c), dt);
+  GB_LAUNCHED(1);
+}
+
+void launch_reinit_sign(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* S) {
+  k_reinit_sign<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(phi, S, c->grid.ni, c->grid.nj, c->base.dx);
+  GB_LAUNCHED(1);
+}
+
+void launch_reinit_sweep(cudaStream_t s, const gb2d_ctx* c, const double* src, double* dst, const double* S, double dtau, int mixed) {
+  dim3 blk(32, 8);
+  dim3 grd = grid2d(c->grid.ni + 4, c->grid.nj + 4, blk);
+  if (mixed)
+    k_reinit_sweep<true><<<grd, blk, 0, s>>>(src, dst, S, ls_args(c), dtau);
+  else
+    k_reinit_sweep<false><<<grd, blk, 0, s>>>(src, dst, S, ls_args(c), dtau);
+  GB_LAUNCHED(1);
+}
+
+void launch_blend(cudaStream_t s, const gb2d_ctx* c, const double* keep, double* phi, double c0, double c1) {
+  k_blend<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(keep, phi, c->grid.ni, c->grid.nj, c0, c1);
+  GB_LAUNCHED(1);
+}
+
+void launch_eno3(cudaStream_t s, const gb2d_ctx* c, double dt) {
+  EnoArgs a{c->grid.ni, c->grid.nj, c->xs, c->ys};
+  size_t n = (size_t)(c->grid.ni + 1) * c->grid.nj + (size_t)c->grid.ni * (c->grid.nj + 1);
+  k_eno3<<<grid_cap(n), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, dt);
+  GB_LAUNCHED(1);
+}
+
+void launch_curvature(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* kappa, int* flag) {
+  k_curvature<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(phi, kappa, c->grid.ni, c->grid.nj, c->base, flag);
+  GB_LAUNCHED(1);
+}
+
+void launch_assemble(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt) {
+  AsmArgs a = asm_args(c, dt);
+  size_t nf = (size_t)(c->grid.ni + 1) * c->grid.nj + (size_t)c->grid.ni * (c->grid.nj + 1);
+  k_faces<<<grid_cap(nf), kThreads, 0, s>>>(phi, c->bx, c->by, a);
+  GB_LAUNCHED(1);
+  k_rhs_diag<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(phi, c->kappa, c->u, c->v, c->bx, c->by, c->diag, c->rhs, a);
+  GB_LAUNCHED(1);
+}
+
+void launch_poisson_apply_exact(cudaStream_t s, const gb2d_ctx* c, const double* x, double* y) {
+  double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
+  k_apply_exact<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, x, y, c->grid.ni, c->grid.nj, idx2, idy2);
+  GB_LAUNCHED(1);
+}
+
+void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt, Scalars* sc) {
+  AsmArgs a = asm_args(c, dt);
+  k_velocity_update<<<grid_cap(2 * (size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(phi, c->p, c->kappa, c->u, c->v, a, dt, sc);
+  GB_LAUNCHED(1);
+}
+
+void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst, int gd, int nI, int nJ) {
+  k_copy_interior<<<grid_cap((size_t)nI * nJ), kThreads, 0, s>>>(src, gs, dst, gd, nI, nJ);
+  GB_LAUNCHED(1);
+}
+
+}  // namespace gb2d

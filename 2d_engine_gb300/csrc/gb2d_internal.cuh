@@ -1,0 +1,123 @@
+// Internal declarations shared by the gb2d translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gb2d.h"
+
+namespace gb2d {
+
+constexpr int kThreads = 256;       // threads per block for grid-stride kernels
+constexpr int kMaxPartials = 1216;  // 152 SMs x 8: reduction partial sums per pass
+constexpr int kCoarseMax = 64;      // coarsest multigrid level is solved by a dense inverse
+constexpr int kMaxLevels = 16;
+
+// Grid spacing of one (sub)grid, computed as GRID_STRUCTURE_2D::Initialize does.
+struct Space {
+  double dx, dy, odx, ody, o2dx, o2dy, odx2, ody2;
+};
+Space make_space(int ires, int jres, double x_min, double y_min, double x_max, double y_max);
+
+// Ghost-inclusive field view on the device.
+struct DField {
+  double* a;
+  int g, nI, nJ, ld;
+};
+__host__ __device__ inline DField dfield(double* a, int g, int nI, int nJ) { return DField{a, g, nI, nJ, nI + 2 * g}; }
+#define GB_AT(f, i, j) ((f).a[((i) + (f).g) + (size_t)((j) + (f).g) * (f).ld])
+
+// One multigrid level (cell-centred view of the node grid), padded with a zero
+// ring: cell (i, j) at (i+1) + (j+1)*ld, ld = nI + 2.  cx at the same index is the
+// conductance of the face between (i-1, j) and (i, j) (i = 0..nI), cy the face
+// between (i, j-1) and (i, j).  Wall faces carry zero conductance.
+template <typename T>
+struct Level {
+  int nI, nJ, ld;
+  T *cx, *cy, *dg, *idg, *sh;  // sh = dg - sum of face conductances (pin / dx != dy terms)
+  T *x, *b;                    // correction and right-hand side
+};
+
+// Device-resident solver scalars (deterministic reductions land here).
+struct Scalars {
+  double rz[2];    // r.z of the two most recent iterations (parity-indexed)
+  double rr;       // ||r||^2 of the latest update
+  double rr0;      // ||r0||^2 at the start of a solve
+  double bb;       // ||b||^2
+  int flag;        // non-finite / zero-gradient detections
+  int pad;
+  unsigned long long maxu_bits, maxv_bits;  // max |u|, |v| of the velocity update
+};
+
+struct Solver;  // defined in gb2d_solver.cu
+
+// Kernels launched by this library (process-wide), reported by gb2d_kernel_launches.
+extern unsigned long long g_launches;
+#define GB_LAUNCHED(n) (::gb2d::g_launches += (n))
+
+// Event brackets around one kernel's launches (roofline measurement).
+struct Probe {
+  int on = 0, n = 0, cap = 0;
+  cudaEvent_t* ev = nullptr;  // 2 * cap events
+  double bytes = 0;           // algorithmic bytes of one probed launch
+};
+
+}  // namespace gb2d
+
+struct gb2d_ctx {
+  gb2d_grid grid;
+  gb2d_params prm;
+  gb2d::Space base, xs, ys;
+  cudaStream_t stream;
+  cudaStream_t own_stream;
+  gb2d::Probe probe;
+  // Level-set buffers (ghost 2): current index into phi_buf.
+  double* phi_buf[4];
+  int phi_cur;
+  double *u, *v, *ua, *va, *p, *kappa;
+  double* sign;  // reinit S (interior)
+  // Assembled pressure system (FP64): faces bx ((ni+1) x nj), by (ni x (nj+1)), diag/rhs (ni x nj).
+  double *bx, *by, *diag, *rhs;
+  double *tmp_a, *tmp_b;  // compact scratch for the standalone Poisson calls
+  double* xw;             // padded solution buffer for gb2d_poisson_solve
+  double* ckpt[6];        // checkpoint copies of phi, u, v, ua, va, p (allocated on first save)
+  int ckpt_phi_cur;
+  double* host_stage;  // pinned staging for small reads
+  gb2d::Scalars* sc;   // device scalars
+  gb2d::Solver* solver;
+  char err[512];
+};
+
+namespace gb2d {
+
+// ---- gb2d_exact.cu (FP64 kernels compiled without FMA contraction) ----
+void launch_fill_ghost_copy(cudaStream_t s, double* dst, int gd, const double* src, int gs, int nI, int nJ, int g);
+void launch_extrapolate_ghosts(cudaStream_t s, double* f, int g, int nI, int nJ);
+void launch_weno5_advect(cudaStream_t s, const gb2d_ctx* c, const double* src, double* dst, double dt, int mixed);
+void launch_reinit_sign(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* S);
+void launch_reinit_sweep(cudaStream_t s, const gb2d_ctx* c, const double* src, double* dst, const double* S, double dtau, int mixed);
+void launch_blend(cudaStream_t s, const gb2d_ctx* c, const double* keep, double* phi, double c0, double c1);
+void launch_eno3(cudaStream_t s, const gb2d_ctx* c, double dt);
+void launch_curvature(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* kappa, int* flag);
+void launch_assemble(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt);
+void launch_poisson_apply_exact(cudaStream_t s, const gb2d_ctx* c, const double* x, double* y);
+void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt, Scalars* sc);
+void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst, int gd, int nI, int nJ);
+
+// ---- gb2d_solver.cu ----
+Solver* solver_create(int ni, int nj, char* err, size_t errlen);
+void solver_destroy(Solver* s);
+// Solve A x = rhs (system held in ctx->bx/by/diag) with x (ni x nj, FP64, compact) as warm start.
+int solver_solve(gb2d_ctx* c, const double* rhs, double* x, const gb2d_solve_opts* o, gb2d_solve_stats* st);
+
+}  // namespace gb2d
+
+#define GB2D_CUDA_TRY(ctx, expr)                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (expr);                                                                      \
+    if (e_ != cudaSuccess) {                                                                      \
+      snprintf((ctx)->err, sizeof((ctx)->err), "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_),   \
+               __FILE__, __LINE__);                                                               \
+      return GB2D_ERR_CUDA;                                                                       \
+    }                                                                                             \
+  } while (0)

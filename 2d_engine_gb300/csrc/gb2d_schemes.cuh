@@ -1,0 +1,127 @@
+// Device forms of the reference's upwind schemes.  Expressions keep the
+// reference's association order; the translation unit that instantiates the
+// FP64 versions is compiled with --fmad=false so that they round exactly as the
+// reference's FP64 CPU code (ADVECTION_METHOD_2D.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace gb2d {
+
+// WENO5 one-sided derivative from five first differences (ADVECTION_METHOD_2D.h:545-619).
+template <typename R>
+__device__ __forceinline__ R weno5_side(R a1, R a2, R a3, R a4, R a5, R eps) {
+  const R c13 = R(13.0 / 12.0);
+  const R q = R(0.25);
+  R A1 = a1 - R(2) * a2 + a3, B1 = a1 - R(4) * a2 + R(3) * a3;
+  R A2 = a2 - R(2) * a3 + a4, B2 = a2 - a4;
+  R A3 = a3 - R(2) * a4 + a5, B3 = R(3) * a3 - R(4) * a4 + a5;
+  R s1 = c13 * A1 * A1 + q * B1 * B1;
+  R s2 = c13 * A2 * A2 + q * B2 * B2;
+  R s3 = c13 * A3 * A3 + q * B3 * B3;
+  R al1 = R(1.0 / 10.0) / ((eps + s1) * (eps + s1));
+  R al2 = R(6.0 / 10.0) / ((eps + s2) * (eps + s2));
+  R al3 = R(3.0 / 10.0) / ((eps + s3) * (eps + s3));
+  R sum = al1 + al2 + al3;
+  R w1 = al1 / sum, w2 = al2 / sum, w3 = al3 / sum;
+  const R cm16 = R((-1.0) / 6.0);
+  return w1 * (a1 / R(3) - a2 * R(7) / R(6) + a3 * R(11) / R(6)) + w2 * (a2 * cm16 + a3 * R(5) / R(6) + a4 / R(3)) +
+         w3 * (a3 / R(3) + a4 * R(5) / R(6) - a5 / R(6));
+}
+
+// Exact FP64 pair: q[0..6] are values at offsets -3..+3 (ADVECTION_METHOD_2D.h:521-543).
+__device__ __forceinline__ void weno5_pair(const double q[7], double o, double eps, double& dm, double& dp) {
+  double d[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d[k] = o * (q[k + 1] - q[k]);
+  dm = weno5_side<double>(d[0], d[1], d[2], d[3], d[4], eps);
+  dp = weno5_side<double>(d[5], d[4], d[3], d[2], d[1], eps);
+}
+
+// Mixed pair: differences of the FP64 state formed in FP64, everything after in FP32.
+__device__ __forceinline__ void weno5_pair_f32(const double q[7], float o, float eps, float& dm, float& dp) {
+  float d[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d[k] = (float)(q[k + 1] - q[k]) * o;
+  dm = weno5_side<float>(d[0], d[1], d[2], d[3], d[4], eps);
+  dp = weno5_side<float>(d[5], d[4], d[3], d[2], d[1], eps);
+}
+
+// Godunov selection of WENO5thReinitialization (ADVECTION_METHOD_2D.h:1505-1655).
+// Returns false where the reference leaves phi unchanged (tie sss == 0 or NaN);
+// otherwise h = |grad phi| - 1 over the selected one-sided derivatives.
+template <typename R>
+__device__ __forceinline__ bool godunov_h(R s, R mx, R px, R my, R py, R& h) {
+  R smx = s * mx, spx = s * px, smy = s * my, spy = s * py;
+  int xs, ys;
+  if (spx >= 0 && smx >= 0)
+    xs = 0;
+  else if (spx <= 0 && smx <= 0)
+    xs = 1;
+  else if (spx > 0 && smx < 0)
+    xs = 2;
+  else if (spx < 0 && smx > 0) {
+    R sss = s * (fabs(px) - fabs(mx)) / (px - mx);
+    if (sss > 0)
+      xs = 0;
+    else if (sss < 0)
+      xs = 1;
+    else
+      return false;
+  } else
+    return false;
+  if (spy >= 0 && smy >= 0)
+    ys = 0;
+  else if (spy <= 0 && smy <= 0)
+    ys = 1;
+  else if (spy > 0 && smy < 0)
+    ys = 2;
+  else if (spy < 0 && smy > 0) {
+    R ss = s * (fabs(py) - fabs(my)) / (py - my);
+    ys = (ss > 0) ? 0 : 1;
+  } else
+    return false;
+  R gx = xs == 0 ? mx : px, gy = ys == 0 ? my : py;
+  if (xs != 2 && ys != 2)
+    h = sqrt(gx * gx + gy * gy) - R(1);
+  else if (xs != 2)
+    h = sqrt(gx * gx) - R(1);
+  else if (ys != 2)
+    h = sqrt(gy * gy) - R(1);
+  else
+    h = R(-1);
+  return true;
+}
+
+// ENO3 one-sided derivatives by divided-difference selection (ADVECTION_METHOD_2D.h:2054-2111).
+__device__ __forceinline__ void eno3_pair(const double q[7], double o, double o2, double o3, double h, double& dm, double& dp) {
+  double d1n3 = o * (q[1] - q[0]), d1n2 = o * (q[2] - q[1]), d1n1 = o * (q[3] - q[2]);
+  double d10 = o * (q[4] - q[3]), d1p1 = o * (q[5] - q[4]), d1p2 = o * (q[6] - q[5]);
+  double d2n2 = o2 * (d1n2 - d1n3), d2n1 = o2 * (d1n1 - d1n2), d20 = o2 * (d10 - d1n1);
+  double d2p1 = o2 * (d1p1 - d10), d2p2 = o2 * (d1p2 - d1p1);
+  double d3n2 = o3 * (d2n1 - d2n2), d3n1 = o3 * (d20 - d2n1), d30 = o3 * (d2p1 - d20), d3p1 = o3 * (d2p2 - d2p1);
+  if (fabs(d2n1) <= fabs(d20)) {
+    if (fabs(d3n2) <= fabs(d3n1))
+      dm = d1n1 + d2n1 * h + 2 * d3n2 * h * h;
+    else
+      dm = d1n1 + d2n1 * h + 2 * d3n1 * h * h;
+  } else {
+    if (fabs(d3n1) <= fabs(d30))
+      dm = d1n1 + d20 * h - d3n1 * h * h;
+    else
+      dm = d1n1 + d20 * h - d30 * h * h;
+  }
+  if (fabs(d20) <= fabs(d2p1)) {
+    if (fabs(d3n1) <= fabs(d30))
+      dp = d10 - d20 * h - d3n1 * h * h;
+    else
+      dp = d10 - d20 * h - d30 * h * h;
+  } else {
+    if (fabs(d30) <= fabs(d3p1))
+      dp = d10 - d2p1 * h + 2 * d30 * h * h;
+    else
+      dp = d10 - d2p1 * h + 2 * d3p1 * h * h;
+  }
+}
+
+}  // namespace gb2d

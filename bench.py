@@ -1,0 +1,347 @@
+"""Benchmark: ms per ghost-fluid pressure projection at 1024^2 to relative residual 1e-8.
+
+Workload (one "step" = one PROJECTION_2D::Solve): 1024 x 1024 pressure nodes on
+[0,1]^2, level set = signed distance to 8 seeded circles (rho 1 inside, 1000
+outside, sigma = 0.0728), MAC velocity U[-1,1] smoothed by 4 Jacobi passes,
+dt = 0.5 dx, zero initial pressure; solve to ||b - A p|| / ||b|| <= 1e-8.
+The timed path is the mixed-precision MG-PCG (FP64 refinement around FP32 CG +
+FP32 V-cycles); the plain FP64 MG-PCG path is timed beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU path (the oracle restatement of
+PCG-IC(0) on the same workload, the reference's solver is single-threaded) on a
+bounded sample per step, extrapolated to the iterations a full solve needs.
+Prints one JSON line on rank 0.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 1024
+TOL = 1e-8
+SEED = 0
+METRIC = "ms per projection at 1024^2 to rel. residual 1e-8 (mixed MG-PCG)"
+WORKLOAD = "standalone ghost-fluid projection, 1024x1024 nodes, 8 circles rho 1:1000, sigma 0.0728, rel. residual 1e-8"
+# Iterations the reference's PCG-IC(0) needs on this workload to reach ||r||/||b|| <= 1e-8
+# (measured with the oracle, which reproduces the reference's iterations exactly).
+REF_FULL_ITERATIONS = None  # filled from _ref_iterations() below
+REF_SAMPLE_ITERATIONS = 150
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """DRAM bytes per launch of the probed kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get("smooth_f32_level0_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def make_case():
+    from tests.golden.cases import bubbles_case
+    return bubbles_case(N, seed=SEED)
+
+
+def cpu_baseline(case, sample_iterations, full_iterations):
+    """Oracle (the reference's PCG-IC(0) restated, single-threaded like the reference's
+    solve) on the full workload: setup + `sample_iterations` PCG iterations timed,
+    extrapolated to the iterations a full solve needs."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle2d
+    oracle2d.build()
+    g = oracle2d.grid(N, N)
+    dt = 0.5 / (N - 1)
+    t0 = time.perf_counter()
+    phi = case["phi"].copy()
+    kappa = np.zeros((N, N))
+    oracle2d.curvature(g, phi, kappa)
+    bx, by, dg, rhs = oracle2d.poisson_assemble(g, oracle2d.params(), phi, case["u"], case["v"], kappa, dt)
+    t1 = time.perf_counter()
+    x = np.zeros((N, N))
+    st = oracle2d.pcg_ic0(g, oracle2d.params(pcg_tolerance=0.0, pcg_max_iterations=sample_iterations - 1), bx, by, dg, rhs, x)
+    t2 = time.perf_counter()
+    per_iter = (t2 - t1) / max(st.iterations, 1)
+    total_ms = ((t1 - t0) + per_iter * full_iterations) * 1e3
+    return total_ms, per_iter * 1e3, st.iterations
+
+
+def ref_full_iterations():
+    path = os.path.join(ROOT, "profiles", "cpu_reference_1024.json")
+    try:
+        with open(path) as f:
+            return int(json.load(f)["pcg_ic0_iterations_to_1e-8"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    full = ref_full_iterations()
+    if full is None:
+        print(json.dumps({"impl": "reference", "unavailable": "profiles/cpu_reference_1024.json (iterations of the full CPU solve) missing"}))
+        return
+    case = make_case()
+    times = []
+    for step in range(args.warmup + args.steps):
+        ms, per_iter, it = cpu_baseline(case, REF_SAMPLE_ITERATIONS, full)
+        if step >= args.warmup:
+            times.append(ms)
+    ms = statistics.mean(times)
+    sample = f"setup + {REF_SAMPLE_ITERATIONS} PCG-IC(0) iterations at 1024^2 per step, extrapolated to the {full} iterations of the full solve"
+    out = {"metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "impl": "reference",
+           "config": {"workload": WORKLOAD, "solver": "PCG-IC(0) (reference PCG_METHOD, CPU, 1 thread)"},
+           "cpu_baseline": {"value": ms, "unit": "ms", "cores": 1, "kind": "port", "sample": sample},
+           "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+    import importlib
+    gb = importlib.import_module("2d_engine_gb300")
+
+    ws, rank, local = dist_env()
+    dist = init_dist(ws)
+    torch.cuda.set_device(local)
+    case = make_case()
+    dt = 0.5 / (N - 1)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def setup(prec):
+        c = gb.Context(N, N)
+        c.set_stream(stream.cuda_stream)
+        for f, k in ((gb.FIELD_PHI, "phi"), (gb.FIELD_U, "u"), (gb.FIELD_V, "v"), (gb.FIELD_P, "p"), (gb.FIELD_UA, "ua"), (gb.FIELD_VA, "va")):
+            c.set(f, case[k])
+        c.checkpoint_save()
+        c.synchronize()
+        return c
+
+    def timed(c, opts, steps, warmup, probe=False):
+        ms, iters, stats = [], [], None
+        for step in range(warmup + steps):
+            c.checkpoint_restore()
+            with torch.cuda.stream(stream):
+                flush.zero_()  # > L2 (129 MB): every step starts cold
+                if probe and step == warmup:
+                    c.probe(True)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                st = c.projection(dt, opts)
+                e1.record(stream)
+            e1.synchronize()
+            if step >= warmup:
+                ms.append(e0.elapsed_time(e1))
+                iters.append(st.iterations)
+                stats = st
+        return ms, iters, stats
+
+    mixed = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=TOL)
+    fp64 = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=TOL)
+    cm = setup(gb.PRECISION_MIXED)
+    c64 = setup(gb.PRECISION_FP64)
+    timed(cm, mixed, 0, args.warmup)
+    timed(c64, fp64, 0, min(args.warmup, 2))
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(dist)
+    torch.cuda.synchronize()
+    launches0 = gb.kernel_launches()
+    t_wall0 = time.perf_counter()
+    ms_m, it_m, st_m = timed(cm, mixed, args.steps, 0, probe=True)
+    t_wall = time.perf_counter() - t_wall0
+    launches = gb.kernel_launches() - launches0
+    torch.cuda.synchronize()
+    barrier(dist)
+    nprobe, probe_ms, probe_bytes = cm.probe_read()
+    cm.probe(False)
+    ms_64, it_64, st_64 = timed(c64, fp64, max(1, min(args.steps, 3)), 0)
+    clk = clocks.stop()
+
+    p_mixed = cm.get(gb.FIELD_P)
+    p_64 = c64.get(gb.FIELD_P)
+    diff = float(np.linalg.norm(p_mixed - p_64) / np.linalg.norm(p_64))
+
+    # End to end through the C ABI with host buffers: H2D of the step's inputs, the
+    # projection, D2H of p, u, v, all inside the timed region.
+    pin = {k: torch.from_numpy(np.ascontiguousarray(case[k])).pin_memory().numpy() for k in ("phi", "u", "v", "p")}
+    out = {k: torch.empty(case[k].shape, dtype=torch.float64).pin_memory().numpy() for k in ("p", "u", "v")}
+    h2d = sum(pin[k].nbytes for k in pin)
+    d2h = sum(out[k].nbytes for k in out)
+    e2e = []
+    for step in range(args.warmup + args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            cm.set(gb.FIELD_PHI, pin["phi"]); cm.set(gb.FIELD_U, pin["u"]); cm.set(gb.FIELD_V, pin["v"]); cm.set(gb.FIELD_P, pin["p"])
+            cm.projection(dt, mixed)
+            cm.get(gb.FIELD_P, out["p"]); cm.get(gb.FIELD_U, out["u"]); cm.get(gb.FIELD_V, out["v"])
+            e1.record(stream)
+        e1.synchronize()
+        if step >= args.warmup:
+            e2e.append(e0.elapsed_time(e1))
+
+    ms_step = max_over_ranks(dist, statistics.mean(ms_m))
+    value = ms_step / ws
+    e2e_ms = max_over_ranks(dist, statistics.mean(e2e)) / ws
+    peak, peak_kind = measured_peaks()
+    achieved = (probe_bytes / (probe_ms / nprobe * 1e-3) / 1e9) if nprobe else None
+    traffic = ncu_traffic_per_launch()
+
+    if rank != 0:
+        return
+    full = ref_full_iterations()
+    cpu = None
+    if full is not None and not args.no_cpu:
+        cms, per_iter, it = cpu_baseline(case, REF_SAMPLE_ITERATIONS, full)
+        cpu = {"value": cms, "unit": "ms", "cores": 1, "kind": "port",
+               "sample": f"oracle PCG-IC(0) (the reference's solver, single-threaded as in the reference): setup + {it} iterations "
+                         f"at 1024^2 timed ({per_iter:.1f} ms/iteration), extrapolated to the {full} iterations of a full solve to 1e-8"}
+    res = {
+        "metric": METRIC, "value": value, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 inner / f64 refinement", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": f"{N}x{N}", "tolerance": TOL, "seed": SEED, "l2": "flushed (256 MB write) before every step",
+                   "solver": "FP64 iterative refinement around FP32 CG + FP32 V-cycles (2+2 red-black GS)",
+                   "iterations_mixed": statistics.mean(it_m), "outer_iterations_mixed": st_m.outer_iterations,
+                   "rel_residual_mixed": st_m.rel_residual,
+                   "fp64_mgpcg_ms": statistics.mean(ms_64), "iterations_fp64": statistics.mean(it_64), "rel_residual_fp64": st_64.rel_residual,
+                   "mixed_vs_fp64_rel_l2_p": diff, "replicas": ws},
+        "clocks": clk,
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_smooth<float> finest level (one red-black half sweep)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "peak_source": peak_kind, "traffic": traffic, "launches_timed": nprobe,
+                     "avg_launch_us": (probe_ms / nprobe * 1e3) if nprobe else None, "algorithmic_bytes_per_launch": probe_bytes},
+        "cpu_baseline": cpu,
+        "wall_s_timed": t_wall,
+    }
+    print(json.dumps(res))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

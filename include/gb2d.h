@@ -1,0 +1,155 @@
+/*
+ * gb2d.h — C ABI of the GB300 (sm_103a) level-set / ghost-fluid projection path.
+ *
+ * Drop-in target: the calls EULERIAN_FLUID_SOLVER_2D makes into its advection,
+ * reinitialisation and projection members (reference ByungJoonLee/2D_Engine):
+ *   Levelset_Advection(dt, tid)        EULERIAN_FLUID_SOLVER_2D.h:1896-2045
+ *   Reinitialization(dt, tid)          EULERIAN_FLUID_SOLVER_2D.h:2402-2445
+ *   Velocity_Advection(dt, tid)        EULERIAN_FLUID_SOLVER_2D.h:1886-1889
+ *   Projection(dt, tid)                EULERIAN_FLUID_SOLVER_2D.h:2359-2363
+ *   level-set/reinit TVD-RK3 blocks    EULERIAN_FLUID_SOLVER_2D.h:1694-1741
+ *   LEVELSET_2D::ComputeCurvaturesThread  LEVELSET_2D.h:898-990
+ *   POISSON_SOLVER::Solve + PCG_METHOD    POISSON_SOLVER.cpp:127-145, PCG_METHOD.cpp:176-264
+ * Plain pointers and sizes only.  Every call returns a status (GB2D_OK = 0,
+ * negative on error); gb2d_last_error() gives the message.  A context owns one
+ * CUDA stream and its device buffers; it is not re-entrant (one host thread
+ * at a time), matching how the reference runs these on its head thread.
+ *
+ * Host arrays use the reference's ghost-inclusive ARRAY_2D layout
+ * (ARRAY_2D.h:140-146): row-major, i fastest, element (i, j) of a field with
+ * ghost width g and interior width nI at [(i+g) + (j+g)*(nI+2g)], i.e. the
+ * FIELD_STRUCTURE_2D::array_for_this.values pointer can be passed as is.
+ */
+#ifndef GB2D_H
+#define GB2D_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB2D_OK 0
+#define GB2D_ERR_ARG (-1)          /* invalid argument or size */
+#define GB2D_ERR_CUDA (-2)         /* CUDA runtime error (message names it) */
+#define GB2D_ERR_NONFINITE (-3)    /* NaN/Inf met in a reduction */
+#define GB2D_ERR_MAX_ITERS (-4)    /* solver stopped at its iteration cap above tolerance */
+#define GB2D_ERR_ZERO_GRADIENT (-5)/* curvature denominator zero (reference exits: LEVELSET_2D.h:869-873) */
+#define GB2D_ERR_NO_DEVICE (-6)
+
+/* Field identifiers and their ghost widths (EULERIAN_FLUID_SOLVER_2D.h:350-384,
+ * PROJECTION_2D.h:207-213, LEVELSET_2D.h:64-79). */
+#define GB2D_FIELD_PHI 0   /* level set, nodes ni x nj, ghost 2 */
+#define GB2D_FIELD_U 1     /* x-face velocity (ni+1) x nj, ghost 2 */
+#define GB2D_FIELD_V 2     /* y-face velocity ni x (nj+1), ghost 2 */
+#define GB2D_FIELD_UA 3    /* advecting x-velocity copy (ghost 3): velocity_field_mac_ghost_x */
+#define GB2D_FIELD_VA 4    /* advecting y-velocity copy (ghost 3): velocity_field_mac_ghost_y */
+#define GB2D_FIELD_P 5     /* pressure, ghost 1 */
+#define GB2D_FIELD_KAPPA 6 /* curvature, no ghost */
+
+#define GB2D_PRECISION_FP64 0  /* FP64 everywhere: reproduces the reference's FP64 results */
+#define GB2D_PRECISION_MIXED 1 /* FP32 inner work inside FP64 refinement (see gb2d_solve_opts) */
+
+#define GB2D_SOLVER_MGPCG 0       /* multigrid-preconditioned CG */
+#define GB2D_SOLVER_PCG_JACOBI 1  /* diagonal-preconditioned CG (simple FP64 parity solver) */
+
+typedef struct gb2d_ctx gb2d_ctx;
+
+/* Node grid as GRID_STRUCTURE_2D (GRID_STRUCTURE_2D.h:88-123): dx = (x_max-x_min)/(ni-1). */
+typedef struct {
+  int ni, nj;
+  double x_min, y_min, x_max, y_max;
+} gb2d_grid;
+
+/* Physical and scheme constants read by the reference from its .sim script
+ * (EULERIAN_FLUID_SOLVER_2D.h:170-262, ADVECTION_2D.cpp:4-18). */
+typedef struct {
+  double water_density;    /* phi > 0 (air_bubble_rising) */
+  double air_density;      /* phi <= 0 */
+  double surface_tension;  /* jump jc = sigma * kappa */
+  double weno_epsilon;     /* WENO weight epsilon (1e-6) */
+  int reinit_iterations;   /* iteration_number_for_reinitialization */
+  int reinit_scaling;      /* scaling_number_for_reinitialization: dtau = dx/scaling */
+  int advection_precision; /* GB2D_PRECISION_FP64: exact FP64 WENO; MIXED: FP32 flux evaluation, FP64 state */
+} gb2d_params;
+
+/* Pressure-solve options (replace PROJECTION block's tolerance/max_iteration/
+ * poisson_solver_type, PROJECTION_2D.h:132-160). */
+typedef struct {
+  int solver;           /* GB2D_SOLVER_* */
+  int precision;        /* GB2D_PRECISION_*: MIXED = FP64 refinement around FP32 CG + FP32 V-cycles */
+  double tolerance;     /* stop at ||b - A p||_2 / ||b||_2 <= tolerance */
+  int max_iterations;   /* cap on Krylov iterations (all refinement steps together) */
+  int mg_smooth;        /* red-black Gauss-Seidel sweeps before and after each coarse correction (0 = 2) */
+  double inner_tolerance; /* MIXED: relative reduction of each FP32 inner solve (0 = 1e-4) */
+} gb2d_solve_opts;
+
+typedef struct {
+  int iterations;        /* Krylov iterations done */
+  int outer_iterations;  /* FP64 refinement steps (1 for FP64) */
+  double rel_residual;   /* final FP64 ||b - A p|| / ||b|| */
+  double max_velocity_x; /* max |u| after the update (PROJECTION_2D::max_velocity_x) */
+  double max_velocity_y;
+} gb2d_solve_stats;
+
+/* Context lifetime.  Allocates every device buffer up front (no allocation in later calls). */
+int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out);
+int gb2d_destroy(gb2d_ctx* ctx);
+const char* gb2d_last_error(const gb2d_ctx* ctx);
+/* Ghost-inclusive host extents of a field: *ires x *jres doubles. */
+int gb2d_field_extent(const gb2d_grid* grid, int field, int* ires, int* jres);
+
+/* Host <-> device state transfer of one ghost-inclusive field (blocking). */
+int gb2d_set_field(gb2d_ctx* ctx, int field, const double* host);
+int gb2d_get_field(gb2d_ctx* ctx, int field, double* host);
+/* Device-side copy of a whole field (for callers that keep their own device state). */
+int gb2d_field_device_ptr(gb2d_ctx* ctx, int field, double** dptr);
+int gb2d_synchronize(gb2d_ctx* ctx);
+/* Run the context's work on a caller-owned CUDA stream (a cudaStream_t passed as
+ * void*); NULL returns to the context's own stream. */
+int gb2d_set_stream(gb2d_ctx* ctx, void* stream);
+
+/* Kernel probe for roofline measurement: while enabled, the pressure solver
+ * brackets every launch of its finest-level smoother (one red-black half sweep)
+ * with CUDA events on the context stream.  gb2d_probe_read returns the launches
+ * seen, their summed event time and the algorithmic bytes of one launch
+ * (every array the half sweep must read or write, once). */
+int gb2d_probe_enable(gb2d_ctx* ctx, int enable);
+int gb2d_probe_read(gb2d_ctx* ctx, int* launches, double* total_ms, double* bytes_per_launch);
+/* Kernels this library has launched in this process so far (all contexts). */
+int gb2d_kernel_launches(unsigned long long* count);
+
+/* Device-resident checkpoint of the step state (PHI with its ghosts, U, V, UA,
+ * VA, P): save copies it to a second set of device buffers (allocated on the
+ * first save), restore copies it back.  Asynchronous on the context stream. */
+int gb2d_checkpoint_save(gb2d_ctx* ctx);
+int gb2d_checkpoint_restore(gb2d_ctx* ctx);
+
+/* One Levelset_Advection: WENO5 sweep with the advecting copies UA/VA, then phi's
+ * ghost extrapolation (a1, a5, a7). */
+int gb2d_levelset_advection(gb2d_ctx* ctx, double dt);
+/* One Reinitialization: S = phi/sqrt(phi^2+dx^2), reinit_iterations WENO5-Godunov sweeps (a2, a6). */
+int gb2d_reinitialization(gb2d_ctx* ctx);
+/* Level-set TVD-RK3 followed by reinit TVD-RK3, as one step of the reference (a4). */
+int gb2d_levelset_rk3(gb2d_ctx* ctx, double dt);
+/* One Velocity_Advection: refresh UA/VA from U/V, ENO3 on both MAC components (a3). */
+int gb2d_velocity_advection(gb2d_ctx* ctx, double dt);
+/* ComputeCurvaturesThread: extrapolate phi's ghosts, write KAPPA (a8). */
+int gb2d_curvature(gb2d_ctx* ctx);
+/* One PROJECTION_2D::Solve(dt): density, divergence, sigma*kappa jump, matrix-free
+ * ghost-fluid Poisson system, solve (P is the warm start), GFM velocity update (a9-a14). */
+int gb2d_projection(gb2d_ctx* ctx, double dt, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+
+/* Standalone pieces of the pressure system for parity checks and for
+ * POISSON_SOLVER_2D-style use (a10, a15).  gb2d_poisson_assemble runs the
+ * curvature step (which extrapolates phi's ghosts) and builds the system of the
+ * current state as PROJECTION_2D would, then copies out face weights bx
+ * ((ni+1) x nj), by (ni x (nj+1)), diag and rhs (ni x nj); any output may be NULL. */
+int gb2d_poisson_assemble(gb2d_ctx* ctx, double dt, double* bx, double* by, double* diag, double* rhs);
+/* y = A x with the assembled operator, summed in the reference CSR row order. */
+int gb2d_poisson_apply(gb2d_ctx* ctx, const double* x, double* y);
+/* Solve A x = rhs with the assembled operator; x is the warm start (ni x nj). */
+int gb2d_poisson_solve(gb2d_ctx* ctx, const double* rhs, double* x, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GB2D_H */

@@ -598,6 +598,12 @@ int or_pcg_ic0(const or_grid* gr, const or_params* pr, const double* bx, const d
   double res_new = 0;
   for (size_t k = 0; k < n; ++k) res_new += r[k] * p[k];
   double sqr_tol = pr->pcg_tolerance * pr->pcg_tolerance;
+  double rel_thr2 = 0;
+  if (pr->pcg_rel_residual > 0) {
+    double bb = 0;
+    for (size_t k = 0; k < n; ++k) bb += rhs[k] * rhs[k];
+    rel_thr2 = pr->pcg_rel_residual * pr->pcg_rel_residual * bb;
+  }
   int it = 0;
   while (1) {
     or_poisson_apply(gr, bx, by, diag, p, Ap);
@@ -620,6 +626,11 @@ int or_pcg_ic0(const or_grid* gr, const or_params* pr, const double* bx, const d
     it++;
     if (it > pr->pcg_max_iterations) break;
     if (res_new < sqr_tol) break;
+    if (rel_thr2 > 0) {
+      double rr = 0;
+      for (size_t k = 0; k < n; ++k) rr += r[k] * r[k];
+      if (rr <= rel_thr2) break;
+    }
   }
   if (st) {
     st->iterations = it;

