@@ -128,6 +128,7 @@ void free_ctx(gb2d_ctx* c) {
   if (c->probe.ev) {
     for (int k = 0; k < 2 * c->probe.cap; ++k) cudaEventDestroy(c->probe.ev[k]);
     delete[] c->probe.ev;
+    delete[] c->probe.bytes_each;
   }
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
@@ -256,7 +257,8 @@ int gb2d_probe_enable(gb2d_ctx* c, int enable) {
   if (enable && !c->probe.ev) {
     c->probe.cap = 4096;
     c->probe.ev = new (std::nothrow) cudaEvent_t[2 * c->probe.cap];
-    if (!c->probe.ev) return GB2D_ERR_ARG;
+    c->probe.bytes_each = new (std::nothrow) double[c->probe.cap];
+    if (!c->probe.ev || !c->probe.bytes_each) return GB2D_ERR_ARG;
     for (int k = 0; k < 2 * c->probe.cap; ++k) GB2D_CUDA_TRY(c, cudaEventCreate(&c->probe.ev[k]));
   }
   c->probe.on = enable ? 1 : 0;
@@ -295,18 +297,19 @@ int gb2d_probe_read(gb2d_ctx* c, int* launches, double* total_ms, double* bytes_
       srt[b] = srt[b - 1];
       srt[b - 1] = t;
     }
-  double med = n > 0 ? srt[n / 2] : 0.0, tot = 0;
+  double med = n > 0 ? srt[n / 2] : 0.0, tot = 0, bytes = 0;
   int used = 0;
   for (int k = 0; k < n; ++k)
     if (ms[k] >= 0.5 * med) {
       tot += ms[k];
+      bytes += c->probe.bytes_each[k];
       used++;
     }
   delete[] ms;
   delete[] srt;
   *launches = used;
   *total_ms = tot;
-  *bytes_per_launch = c->probe.bytes;
+  *bytes_per_launch = used ? bytes / used : 0.0;
   c->probe.n = 0;
   return GB2D_OK;
 }

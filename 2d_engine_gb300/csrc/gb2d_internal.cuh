@@ -42,7 +42,7 @@ struct Level {
 struct Scalars {
   double rz[2];    // r.z of the two most recent iterations (parity-indexed)
   double rr;       // ||r||^2 of the latest update
-  double rr0;      // ||r0||^2 at the start of a solve
+  double thr2;     // ||r||^2 at which the running solve stops
   double bb;       // ||b||^2
   int flag;        // non-finite / zero-gradient detections
   int pad;
@@ -58,8 +58,8 @@ extern unsigned long long g_launches;
 // Event brackets around one kernel's launches (roofline measurement).
 struct Probe {
   int on = 0, n = 0, cap = 0;
-  cudaEvent_t* ev = nullptr;  // 2 * cap events
-  double bytes = 0;           // algorithmic bytes of one probed launch
+  cudaEvent_t* ev = nullptr;     // 2 * cap events
+  double* bytes_each = nullptr;  // algorithmic bytes of each probed launch
 };
 
 }  // namespace gb2d
