@@ -23,7 +23,8 @@ PRECISION_FP64, PRECISION_MIXED = 0, 1
 SOLVER_MGPCG, SOLVER_PCG_JACOBI = 0, 1
 
 ERRORS = {-1: "invalid argument", -2: "CUDA error", -3: "non-finite value", -4: "iteration cap reached",
-          -5: "zero level-set gradient", -6: "no CUDA device"}
+          -5: "zero level-set gradient", -6: "no CUDA device", -7: "size above the fixed maximum"}
+NOALLOC_MAX_CELLS = 65536
 
 
 class GridT(ctypes.Structure):
@@ -89,6 +90,7 @@ def library():
         "gb2d_kernel_launches": [ctypes.POINTER(ctypes.c_ulonglong)],
         "gb2d_checkpoint_save": [vp],
         "gb2d_checkpoint_restore": [vp],
+        "gb2d_poisson_solve_noalloc": [i, i, d, d, vp, vp, vp, vp, vp, d, i, vp, ctypes.POINTER(i), ctypes.POINTER(d)],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -21,6 +21,7 @@ UNITS = {
     "gb2d_exact.cu": ["--fmad=false"],
     "gb2d_solver.cu": [],
     "gb2d_api.cu": [],
+    "gb2d_noalloc.cu": [],
 }
 
 

@@ -34,6 +34,7 @@ extern "C" {
 #define GB2D_ERR_MAX_ITERS (-4)    /* solver stopped at its iteration cap above tolerance */
 #define GB2D_ERR_ZERO_GRADIENT (-5)/* curvature denominator zero (reference exits: LEVELSET_2D.h:869-873) */
 #define GB2D_ERR_NO_DEVICE (-6)
+#define GB2D_ERR_TOO_LARGE (-7)    /* size above a fixed maximum (gb2d_poisson_solve_noalloc) */
 
 /* Field identifiers and their ghost widths (EULERIAN_FLUID_SOLVER_2D.h:350-384,
  * PROJECTION_2D.h:207-213, LEVELSET_2D.h:64-79). */
@@ -148,6 +149,27 @@ int gb2d_poisson_assemble(gb2d_ctx* ctx, double dt, double* bx, double* by, doub
 int gb2d_poisson_apply(gb2d_ctx* ctx, const double* x, double* y);
 /* Solve A x = rhs with the assembled operator; x is the warm start (ni x nj). */
 int gb2d_poisson_solve(gb2d_ctx* ctx, const double* rhs, double* x, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+
+/* Allocation-free solve for callers that cannot allocate device memory: hosts that
+ * reserve all GPU memory for their own pool and forbid cudaMalloc/cudaFree after
+ * start-up, or that must not allocate inside a frame because allocation can
+ * synchronise the device.  No counterpart in the reference (its PCG allocates
+ * its vectors on every call, PCG_METHOD.cpp:180-200).
+ * FP64 Jacobi-preconditioned CG on an assembled system given as DEVICE pointers
+ * in the layout gb2d_poisson_assemble returns (bx (ni+1) x nj, by ni x (nj+1),
+ * diag, rhs ni x nj); x is the device warm start and receives the solution.
+ * Stops at ||b - A x|| / ||b|| <= tolerance or after max_iterations.  stream is a
+ * cudaStream_t as void* (NULL = the default stream); the call returns after the
+ * solve has finished on that stream.  Scratch is one file-scope device array of
+ * about 2.1 MB that every GPU loading the library keeps until exit; at most
+ * GB2D_NOALLOC_MAX_CELLS unknowns, larger sizes return GB2D_ERR_TOO_LARGE.  The
+ * first call on a device looks up the array's address with that device current
+ * (make it before any stream capture).  All calls share the array and keep the
+ * last call's contents, so calls that overlap on the GPU race. */
+#define GB2D_NOALLOC_MAX_CELLS 65536
+int gb2d_poisson_solve_noalloc(int ni, int nj, double dx, double dy, const double* bx, const double* by, const double* diag,
+                               const double* rhs, double* x, double tolerance, int max_iterations, void* stream, int* iterations,
+                               double* rel_residual);
 
 #ifdef __cplusplus
 }
