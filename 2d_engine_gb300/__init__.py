@@ -88,6 +88,7 @@ def library():
         "gb2d_probe_enable": [vp, i],
         "gb2d_probe_read": [vp, ctypes.POINTER(i), ctypes.POINTER(d), ctypes.POINTER(d)],
         "gb2d_kernel_launches": [ctypes.POINTER(ctypes.c_ulonglong)],
+        "gb2d_solver_layout": [vp, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)],
         "gb2d_checkpoint_save": [vp],
         "gb2d_checkpoint_restore": [vp],
         "gb2d_poisson_solve_noalloc": [i, i, d, d, vp, vp, vp, vp, vp, d, i, vp, ctypes.POINTER(i), ctypes.POINTER(d)],
@@ -190,6 +191,12 @@ class Context:
     def probe(self, enable):
         self._check(self.L.gb2d_probe_enable(self.h, 1 if enable else 0))
 
+    def solver_layout(self, precision):
+        """(levels, first cluster-tail level or -1, cluster CTAs) of one precision's hierarchy."""
+        lv, top, ctas = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.gb2d_solver_layout(self.h, precision, ctypes.byref(lv), ctypes.byref(top), ctypes.byref(ctas)))
+        return lv.value, top.value, ctas.value
+
     def probe_read(self):
         n, ms, by = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
         self._check(self.L.gb2d_probe_read(self.h, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(by)))
@@ -233,10 +240,12 @@ class Context:
         self._check(self.L.gb2d_poisson_apply(self.h, _ptr(x), _ptr(y)))
         return y
 
-    def poisson_solve(self, rhs, x0=None, opts=None):
+    def poisson_solve(self, rhs, x0=None, opts=None, allow_max_iters=False):
         rhs = np.ascontiguousarray(rhs, dtype=np.float64)
         x = np.zeros_like(rhs) if x0 is None else np.ascontiguousarray(x0, dtype=np.float64).copy()
         opts = opts or solve_opts()
         st = SolveStatsT()
-        self._check(self.L.gb2d_poisson_solve(self.h, _ptr(rhs), _ptr(x), ctypes.byref(opts), ctypes.byref(st)))
+        rc = self.L.gb2d_poisson_solve(self.h, _ptr(rhs), _ptr(x), ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
         return x, st

@@ -314,6 +314,13 @@ int gb2d_probe_read(gb2d_ctx* c, int* launches, double* total_ms, double* bytes_
   return GB2D_OK;
 }
 
+int gb2d_solver_layout(gb2d_ctx* c, int precision, int* levels, int* cluster_top, int* cluster_ctas) {
+  if (!c || !levels || !cluster_top || !cluster_ctas) return GB2D_ERR_ARG;
+  if (precision != GB2D_PRECISION_FP64 && precision != GB2D_PRECISION_MIXED) return GB2D_ERR_ARG;
+  gb2d::solver_layout(c->solver, precision == GB2D_PRECISION_MIXED, levels, cluster_top, cluster_ctas);
+  return GB2D_OK;
+}
+
 int gb2d_kernel_launches(unsigned long long* count) {
   if (!count) return GB2D_ERR_ARG;
   *count = gb2d::g_launches;

@@ -262,15 +262,15 @@ struct AsmArgs {
   int ni, nj;
   Space s;
   double water, air, sigma, one_over_dt, inv_dxdx, inv_dydy;
+  double inv_water, inv_air;  // 1/water, 1/air: IEEE quotients taken once on the host
 };
 
+// 1/rho of a node.  The density takes two values, so the quotient is a select of
+// the host's correctly rounded reciprocals (FP64 divides are scarce on this part).
 __device__ __forceinline__ double inv_density(double phi, const AsmArgs& a) {
-  double r = 1.0;
-  if (phi <= 0)
-    r = a.air;
-  else if (phi > 0)
-    r = a.water;
-  return 1.0 / r;
+  if (phi <= 0) return a.inv_air;
+  if (phi > 0) return a.inv_water;
+  return 1.0;
 }
 
 // 1/rho at a node or at its copied ghost (POISSON_SOLVER.cpp:131-138: the ghost
@@ -310,14 +310,21 @@ __device__ __forceinline__ double jc_at(const double* kappa, int i, int j, const
 
 // Jump flux of one arm (POISSON_SOLVER.cpp:881-948) without the derivative-jump
 // part, which vanishes because jc_on_derivative is zeroed (PROJECTION_2D.h:501-504).
-__device__ __forceinline__ double arm_flux(double pc, double pn, double jcc, double jcn, double beta, double o2, bool lower) {
-  if ((pc <= 0 && pn <= 0) || (pc > 0 && pn > 0)) return 0.0;
-  double ac = fabs(pc), an = fabs(pn);
-  double av = (jcc * an + jcn * ac) / (ac + an);
-  // left/bottom arms: +o2*a*beta when phi_c <= 0 < phi_n; right/top arms have the same sign rule
-  (void)lower;
-  if (pc <= 0 && pn > 0) return o2 * av * beta;
-  if (pc > 0 && pn <= 0) return -o2 * av * beta;
+// Left/bottom and right/top arms follow the same sign rule.  The jump values are
+// read only on arms that cross the interface.
+__device__ __forceinline__ double arm_flux(double pc, double pn, double jcc, const double* kappa, int in, int jn, double beta, double o2,
+                                           const AsmArgs& a) {
+  const bool cneg = pc <= 0, nneg = pn <= 0;
+  if (cneg && !nneg && pn > 0) {
+    double ac = fabs(pc), an = fabs(pn);
+    double av = (jcc * an + jc_at(kappa, in, jn, a) * ac) / (ac + an);
+    return o2 * av * beta;
+  }
+  if (!cneg && pc > 0 && nneg) {
+    double ac = fabs(pc), an = fabs(pn);
+    double av = (jcc * an + jc_at(kappa, in, jn, a) * ac) / (ac + an);
+    return -o2 * av * beta;
+  }
   return 0.0;
 }
 
@@ -348,10 +355,10 @@ __global__ void k_rhs_diag(const double* __restrict__ phi_a, const double* __res
 
     double pc = GB_AT(phi, i, j);
     double jcc = jc_at(kappa, i, j, a);
-    double FL = arm_flux(pc, GB_AT(phi, i - 1, j), jcc, jc_at(kappa, i - 1, j, a), bl, a.s.odx2, true);
-    double FR = arm_flux(pc, GB_AT(phi, i + 1, j), jcc, jc_at(kappa, i + 1, j, a), br, a.s.odx2, false);
-    double FB = arm_flux(pc, GB_AT(phi, i, j - 1), jcc, jc_at(kappa, i, j - 1, a), bb, a.s.ody2, true);
-    double FT = arm_flux(pc, GB_AT(phi, i, j + 1), jcc, jc_at(kappa, i, j + 1, a), bt, a.s.ody2, false);
+    double FL = arm_flux(pc, GB_AT(phi, i - 1, j), jcc, kappa, i - 1, j, bl, a.s.odx2, a);
+    double FR = arm_flux(pc, GB_AT(phi, i + 1, j), jcc, kappa, i + 1, j, br, a.s.odx2, a);
+    double FB = arm_flux(pc, GB_AT(phi, i, j - 1), jcc, kappa, i, j - 1, bb, a.s.ody2, a);
+    double FT = arm_flux(pc, GB_AT(phi, i, j + 1), jcc, kappa, i, j + 1, bt, a.s.ody2, a);
     double div = a.s.odx * (GB_AT(u, i + 1, j) - GB_AT(u, i, j)) + a.s.ody * (GB_AT(v, i, j + 1) - GB_AT(v, i, j));
     div *= a.one_over_dt;
     double FX = FL + FR, FY = FB + FT;
@@ -411,16 +418,15 @@ __global__ void k_velocity_update(const double* __restrict__ phi_a, const double
     int i = (int)(k % ni), j = (int)(k / ni);
     int in = xc ? i - 1 : i, jn = xc ? j : j - 1;
     double l0 = GB_AT(phi, i, j), ln = GB_AT(phi, in, jn);
-    double rho_ij = l0 <= 0 ? a.air : a.water;
-    double oor = 1 / rho_ij;
-    double jcc = jc_at(kappa, i, j, a), jcn = jc_at(kappa, in, jn, a);
-    double gam = (jcn * fabs(l0) + jcc * fabs(ln)) / (fabs(l0) + fabs(ln));
+    double oor = l0 <= 0 ? a.inv_air : a.inv_water;  // 1 / rho_ij
     double dp = GB_AT(p, i, j) - GB_AT(p, in, jn);
     double od = xc ? odx : ody;
     double* w = xc ? &GB_AT(u, i, j) : &GB_AT(v, i, j);
     if (l0 * ln >= 0) {
       *w -= dt * dp * oor * od;
     } else {
+      double jcc = jc_at(kappa, i, j, a), jcn = jc_at(kappa, in, jn, a);
+      double gam = (jcn * fabs(l0) + jcc * fabs(ln)) / (fabs(l0) + fabs(ln));
       double dh = a.air + (a.water - a.air) * heaviside(0.5 * (l0 + ln), xc ? eh : ev);
       double odh = 1 / dh;
       if (l0 < 0)
@@ -466,6 +472,8 @@ AsmArgs asm_args(const gb2d_ctx* c, double dt) {
   a.one_over_dt = 1.0 / dt;
   a.inv_dxdx = 1.0 / (c->base.dx * c->base.dx);
   a.inv_dydy = 1.0 / (c->base.dy * c->base.dy);
+  a.inv_water = 1.0 / a.water;
+  a.inv_air = 1.0 / a.air;
   return a;
 }
 

@@ -10,7 +10,7 @@ namespace gb2d {
 
 constexpr int kThreads = 256;       // threads per block for grid-stride kernels
 constexpr int kMaxPartials = 1216;  // 152 SMs x 8: reduction partial sums per pass
-constexpr int kCoarseMax = 64;      // coarsest multigrid level is solved by a dense inverse
+constexpr int kCoarseMax = 64;      // coarsest multigrid level (<= 64 cells) is solved by a dense inverse
 constexpr int kMaxLevels = 16;
 
 // Grid spacing of one (sub)grid, computed as GRID_STRUCTURE_2D::Initialize does.
@@ -36,11 +36,15 @@ struct Level {
   int nI, nJ, ld;
   T *cx, *cy, *dg, *idg, *sh;  // sh = dg - sum of face conductances (pin / dx != dy terms)
   T *x, *b;                    // correction and right-hand side
+  T* xa;                       // second correction buffer: tiled sweeps read one and write the other
 };
 
 // Device-resident solver scalars (deterministic reductions land here).
 struct Scalars {
-  double rz[2];    // r.z of the two most recent iterations (parity-indexed)
+  double rz_new;   // r.z of the latest preconditioned residual
+  double rz_cur;   // r.z belonging to the current search direction
+  double alpha;    // step length for the current direction
+  double beta;     // rz_new / rz_cur
   double rr;       // ||r||^2 of the latest update
   double thr2;     // ||r||^2 at which the running solve stops
   double bb;       // ||b||^2
@@ -109,6 +113,7 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen);
 void solver_destroy(Solver* s);
 // Solve A x = rhs (system held in ctx->bx/by/diag) with x (ni x nj, FP64, compact) as warm start.
 int solver_solve(gb2d_ctx* c, const double* rhs, double* x, const gb2d_solve_opts* o, gb2d_solve_stats* st);
+void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, int* cluster_ctas);
 
 }  // namespace gb2d
 

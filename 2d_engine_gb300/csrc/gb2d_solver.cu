@@ -29,7 +29,10 @@
 //
 // All reductions are two-stage and deterministic: blocks write partial sums,
 // consumers re-reduce the partials in a fixed order.
+#include <cooperative_groups.h>
+
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 
@@ -39,7 +42,6 @@ namespace gb2d {
 
 namespace {
 
-constexpr int TX = 32, TY = 16;  // smoothing tile (even, so restriction stays inside a tile)
 constexpr int kTailCells = 64 * 64;
 constexpr int kTailThreads = 1024;
 
@@ -49,11 +51,15 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// Deterministic block sum (blockDim.x multiple of 32, <= 1024); result valid in every thread.
+__device__ __forceinline__ int linear_tid() { return threadIdx.x + threadIdx.y * blockDim.x; }
+__device__ __forceinline__ int block_threads() { return blockDim.x * blockDim.y; }
+
+// Deterministic block sum (block size a multiple of 32, <= 1024); result valid in every thread.
 __device__ double block_sum(double v) {
   __shared__ double sm[32];
   __shared__ double total;
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int tid = linear_tid();
+  int lane = tid & 31, w = tid >> 5, nw = block_threads() >> 5;
   v = warp_sum(v);
   __syncthreads();
   if (lane == 0) sm[w] = v;
@@ -70,7 +76,7 @@ __device__ double block_sum(double v) {
 // Partials written by other blocks: read through L2 (__ldcg), never a stale L1 line.
 __device__ double sum_partials(const double* part, int n) {
   double v = 0.0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) v += __ldcg(&part[k]);
+  for (int k = linear_tid(); k < n; k += block_threads()) v += __ldcg(&part[k]);
   return block_sum(v);
 }
 
@@ -151,33 +157,35 @@ __global__ void k_coarsen(Level<T> F, Level<T> C) {
 }
 
 // Dense inverse of the coarsest operator (n <= 64), in-place Gauss-Jordan
-// without pivoting (the operator is SPD).  One block of 1024 threads; each pivot
-// step scales the pivot row and updates all other entries in parallel.
+// without pivoting (the operator is SPD), computed in the hierarchy's precision
+// (one SM's FP64 rate would make the FP64 elimination ~100 us).  One block of
+// 1024 threads; each pivot step scales the pivot row and updates all other
+// entries in parallel.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_dense_inverse(Level<T> C, double* __restrict__ ainv) {
-  __shared__ double A[kCoarseMax][kCoarseMax + 1];
-  __shared__ double prow[kCoarseMax], fcol[kCoarseMax];
+  __shared__ T A[kCoarseMax][kCoarseMax + 1];
+  __shared__ T prow[kCoarseMax], fcol[kCoarseMax];
   const int n = C.nI * C.nJ;
   if (n > kCoarseMax) return;  // prevented on the host (alloc_hierarchy)
   for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
     int r = t / n, m = t % n;
     int i = r % C.nI, j = r / C.nI;
     size_t k = (size_t)(i + 1) + (size_t)(j + 1) * C.ld;
-    double v = 0.0;
-    if (m == r) v = (double)C.dg[k];
-    else if (i > 0 && m == r - 1) v = -(double)C.cx[k];
-    else if (i < C.nI - 1 && m == r + 1) v = -(double)C.cx[k + 1];
-    else if (j > 0 && m == r - C.nI) v = -(double)C.cy[k];
-    else if (j < C.nJ - 1 && m == r + C.nI) v = -(double)C.cy[k + C.ld];
+    T v = 0;
+    if (m == r) v = C.dg[k];
+    else if (i > 0 && m == r - 1) v = -C.cx[k];
+    else if (i < C.nI - 1 && m == r + 1) v = -C.cx[k + 1];
+    else if (j > 0 && m == r - C.nI) v = -C.cy[k];
+    else if (j < C.nJ - 1 && m == r + C.nI) v = -C.cy[k + C.ld];
     A[r][m] = v;
   }
   __syncthreads();
   for (int kk = 0; kk < n; ++kk) {
     if ((int)threadIdx.x < n) {
       int t = threadIdx.x;
-      double piv = A[kk][kk];
+      T inv = (T)1 / A[kk][kk];
       fcol[t] = A[t][kk];
-      prow[t] = (t == kk) ? 1.0 / piv : A[kk][t] / piv;
+      prow[t] = (t == kk) ? inv : A[kk][t] * inv;
     }
     __syncthreads();
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
@@ -191,142 +199,266 @@ __global__ void __launch_bounds__(1024) k_dense_inverse(Level<T> C, double* __re
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < n * n; t += blockDim.x) ainv[t] = A[t / n][t % n];
+  for (int t = threadIdx.x; t < n * n; t += blockDim.x) ainv[t] = (double)A[t / n][t % n];
 }
 
 // ---- tiled smoothing (levels above the tail) ----------------------------------
+//
+// A block of 32x8 threads owns a 64x16 tile; thread (tx, ty) owns the 2x2 quad of
+// cells (2tx..2tx+1, 2ty..2ty+1), which is also one coarse cell.  The block stages
+// x and the coefficients (b, 1/dg, cx, cy, and dg when it restricts) for the tile
+// plus a halo of H cells in shared memory with unrolled, compile-time-bounded
+// loops, runs both half sweeps from shared memory (halo cells of the first colour
+// are recomputed so that the tile's second colour is exact), and writes the tile.
+// Cells outside the domain are staged as zero, which is also the value of every
+// wall-face conductance.  A sweep reads x from L.x and writes xout (the level's
+// other buffer): blocks stage halo cells that neighbouring blocks of the same
+// launch update, so an in-place write would let a block read a neighbour's
+// already-smoothed (and, when prolonging, already-corrected) value.
 
-// Gauss-Seidel value of cell k from the staged neighbours c[-1], c[+1], c[-W], c[+W].
-template <typename T, int W>
-__device__ __forceinline__ T relax(const Level<T>& L, const T* c, size_t k) {
-  return (L.b[k] + L.cx[k] * c[-1] + L.cx[k + 1] * c[1] + L.cy[k] * c[-W] + L.cy[k + L.ld] * c[W]) * L.idg[k];
+constexpr int BXT = 32, BYT = 8;          // threads per block (x, y)
+constexpr int TXS = 2 * BXT, TYS = 2 * BYT;  // tile of one block
+
+template <typename T, int H>
+struct Win {
+  static constexpr int W = TXS + 2 * H, HH = TYS + 2 * H, N = W * HH;
+};
+
+template <typename T, int H, bool DG>
+constexpr size_t sweep_smem() {
+  return sizeof(T) * (size_t)Win<T, H>::N * (DG ? 6 : 5);
 }
 
-// Stage x over the tile plus a halo of width H (zero outside the domain).  With a
-// coarse level given, the piecewise-constant coarse correction is added first.
-template <typename T, int H>
-__device__ __forceinline__ void stage_x(const Level<T>& L, const Level<T>* C, T* xs, int i0, int j0, bool zero) {
-  constexpr int W = TX + 2 * H, HH = TY + 2 * H;
-  for (int idx = threadIdx.x; idx < W * HH; idx += blockDim.x) {
-    int ci = i0 - H + idx % W, cj = j0 - H + idx / W;
-    T v = 0;
-    if (!zero && ci >= 0 && ci < L.nI && cj >= 0 && cj < L.nJ) {
-      v = L.x[(size_t)(ci + 1) + (size_t)(cj + 1) * L.ld];
-      if (C) v += C->x[(size_t)(ci / 2 + 1) + (size_t)(cj / 2 + 1) * C->ld];
+// Stage the window.  LOAD_X: read x (else zero); PROLONG: add the coarse correction.
+template <typename T, int H, bool LOAD_X, bool PROLONG, bool DG>
+__device__ __forceinline__ void stage_window(const Level<T>& L, const Level<T>& C, T* sm, int i0, int j0) {
+  using Wn = Win<T, H>;
+  constexpr int W = Wn::W, HH = Wn::HH, N = Wn::N;
+  T *xs = sm, *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N, *ds = sm + 5 * N;
+  const int gi0 = i0 - H, gj0 = j0 - H;
+  const bool inner = gi0 >= 0 && gj0 >= 0 && gi0 + W <= L.nI && gj0 + HH <= L.nJ;
+  const size_t base = (size_t)(gi0 + 1) + (size_t)(gj0 + 1) * L.ld;
+#pragma unroll
+  for (int r0 = 0; r0 < HH; r0 += BYT) {
+    const int r = r0 + threadIdx.y;
+    if (r >= HH) continue;
+#pragma unroll
+    for (int c0 = 0; c0 < W; c0 += BXT) {
+      const int c = c0 + threadIdx.x;
+      if (c >= W) continue;
+      const int gi = gi0 + c, gj = gj0 + r;
+      T x = 0, b = 0, id = 0, cx = 0, cy = 0, dg = 0;
+      if (inner || (gi >= 0 && gi < L.nI && gj >= 0 && gj < L.nJ)) {
+        const size_t k = base + c + (size_t)r * L.ld;
+        if (LOAD_X) {
+          x = L.x[k];
+          if (PROLONG) x += C.x[(size_t)(gi / 2 + 1) + (size_t)(gj / 2 + 1) * C.ld];
+        }
+        b = L.b[k];
+        id = L.idg[k];
+        cx = L.cx[k];
+        cy = L.cy[k];
+        if (DG) dg = L.dg[k];
+      }
+      const int q = c + r * W;
+      xs[q] = x;
+      bs[q] = b;
+      is[q] = id;
+      cxs[q] = cx;
+      cys[q] = cy;
+      if (DG) ds[q] = dg;
     }
-    xs[idx] = v;
   }
 }
 
-// Half sweep of one colour over the staged region shrunk by `ring` cells per side.
-template <typename T, int H>
-__device__ __forceinline__ void half_sweep(const Level<T>& L, T* xs, int i0, int j0, int color, int ring) {
-  constexpr int W = TX + 2 * H, HH = TY + 2 * H;
-  const int RW = W - 2 * ring, RH = HH - 2 * ring;
-  for (int idx = threadIdx.x; idx < RW * RH; idx += blockDim.x) {
-    int si = ring + idx % RW, sj = ring + idx / RW;
-    int ci = i0 - H + si, cj = j0 - H + sj;
-    if (((ci + cj) & 1) != color || ci < 0 || ci >= L.nI || cj < 0 || cj >= L.nJ) continue;
-    size_t k = (size_t)(ci + 1) + (size_t)(cj + 1) * L.ld;
-    T* c = &xs[si + sj * W];
-    *c = relax<T, W>(L, c, k);
+// Half sweep of one colour over the window shrunk by R cells per side; each
+// thread takes rows ty, ty+8, ... and, in each, the colour's cells 2m+parity for
+// m = tx, tx+32, ...
+template <typename T, int H, int R>
+__device__ __forceinline__ void window_half(T* sm, int i0, int j0, int nI, int nJ, int color) {
+  using Wn = Win<T, H>;
+  constexpr int W = Wn::W, HH = Wn::HH, N = Wn::N;
+  constexpr int RW = W - 2 * R, RH = HH - 2 * R, HALF = RW / 2;
+  static_assert(RW % 2 == 0, "window rows must hold an even number of cells");
+  T* xs = sm;
+  const T *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N;
+  const int gi0 = i0 - H, gj0 = j0 - H;
+#pragma unroll
+  for (int q = 0; q < (RH + BYT - 1) / BYT; ++q) {
+    const int r = R + threadIdx.y + q * BYT;
+    if (r >= HH - R) continue;
+    const int gj = gj0 + r;
+    const int par = (color - (gi0 + R) - gj) & 1;
+#pragma unroll
+    for (int p = 0; p < (HALF + BXT - 1) / BXT; ++p) {
+      const int m = threadIdx.x + p * BXT;
+      if (m >= HALF) continue;
+      const int c = R + 2 * m + par;
+      const int gi = gi0 + c;
+      if (gi < 0 || gi >= nI || gj < 0 || gj >= nJ) continue;
+      const int s = c + r * W;
+      xs[s] = (bs[s] + cxs[s] * xs[s - 1] + cxs[s + 1] * xs[s + 1] + cys[s] * xs[s - W] + cys[s + W] * xs[s + W]) * is[s];
+    }
   }
 }
 
-// Pre-smoothing sweep (red, then black) on one tile; with restrict_to, the sweep
-// is followed by the residual b - A x on the tile and its average over 2x2
-// children written as the coarse right-hand side (halo 3 makes the black values
-// one cell outside the tile available for that residual).
-template <typename T, int H>
-__global__ void __launch_bounds__(256) k_pre_sweep(Level<T> L, Level<T> C, int zero_init, int restrict_to, const int* __restrict__ done) {
+// FP32-friendly accumulation of a few products per thread (Kahan-compensated in
+// the vector precision); the block and grid reductions are FP64.
+template <typename T>
+struct Acc {
+  T s = 0, c = 0;
+  __device__ __forceinline__ void add(T v) {
+    T y = v - c;
+    T t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <>
+struct Acc<double> {  // FP64 vectors: plain accumulation (FP64 issue slots are scarce)
+  double s = 0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+// Last-block finalisation of a reduction: every block stores its partial, the
+// block that arrives last sums them in a fixed order.  Returns true in that block
+// (every thread), with *total set.
+__device__ __forceinline__ bool last_block_sum(double acc, double* part, unsigned nblocks, unsigned* counter, double* total) {
+  __shared__ bool last;
+  acc = block_sum(acc);
+  unsigned bid = block_linear();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    part[bid] = acc;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == nblocks - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  *total = sum_partials(part, nblocks);
+  if (threadIdx.x == 0 && threadIdx.y == 0) *counter = 0u;
+  return true;
+}
+
+// r.z of a preconditioned residual is known: record it and beta = rz_new / rz_cur.
+__device__ __forceinline__ void publish_rz(Scalars* sc, double rz) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    sc->rz_new = rz;
+    sc->beta = rz / sc->rz_cur;
+  }
+}
+
+// Pre-smoothing sweep (red, then black).  ZERO: x was zero (not read).  With
+// RESTRICT (halo 3), each thread's quad residual b - A x is averaged into the
+// coarse right-hand side.
+template <typename T, bool ZERO, bool RESTRICT>
+__global__ void __launch_bounds__(BXT* BYT) k_pre_sweep(Level<T> L, Level<T> C, T* __restrict__ xout, const int* __restrict__ done) {
   if (*done) return;
-  constexpr int W = TX + 2 * H, HH = TY + 2 * H;
-  __shared__ T xs[W * HH];
-  __shared__ T rs[TX * TY];
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  stage_x<T, H>(L, nullptr, xs, i0, j0, zero_init != 0);
+  constexpr int H = RESTRICT ? 3 : 2;
+  using Wn = Win<T, H>;
+  constexpr int W = Wn::W, N = Wn::N;
+  extern __shared__ unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const int i0 = blockIdx.x * TXS, j0 = blockIdx.y * TYS;
+  stage_window<T, H, !ZERO, false, RESTRICT>(L, C, sm, i0, j0);
   __syncthreads();
-  half_sweep<T, H>(L, xs, i0, j0, 0, 1);
+  window_half<T, H, 1>(sm, i0, j0, L.nI, L.nJ, 0);
   __syncthreads();
-  half_sweep<T, H>(L, xs, i0, j0, 1, 2);
+  window_half<T, H, 2>(sm, i0, j0, L.nI, L.nJ, 1);
   __syncthreads();
-  for (int idx = threadIdx.x; idx < TX * TY; idx += blockDim.x) {
-    int ti = idx % TX, tj = idx / TX;
-    int ci = i0 + ti, cj = j0 + tj;
-    T r = 0;
-    if (ci < L.nI && cj < L.nJ) {
-      size_t k = (size_t)(ci + 1) + (size_t)(cj + 1) * L.ld;
-      const T* c = &xs[(ti + H) + (tj + H) * W];
-      L.x[k] = c[0];
-      if (restrict_to) {
-        T ax = L.dg[k] * c[0] - L.cx[k] * c[-1] - L.cx[k + 1] * c[1] - L.cy[k] * c[-W] - L.cy[k + L.ld] * c[W];
-        r = L.b[k] - ax;
+  const T *xs = sm, *bs = sm + N, *cxs = sm + 3 * N, *cys = sm + 4 * N, *ds = sm + 5 * N;
+  T acc = 0;
+#pragma unroll
+  for (int dr = 0; dr < 2; ++dr)
+#pragma unroll
+    for (int dc = 0; dc < 2; ++dc) {
+      const int ti = 2 * threadIdx.x + dc, tj = 2 * threadIdx.y + dr;
+      const int gi = i0 + ti, gj = j0 + tj;
+      if (gi >= L.nI || gj >= L.nJ) continue;
+      const int s = (ti + H) + (tj + H) * W;
+      xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
+      if (RESTRICT) {
+        T ax = ds[s] * xs[s] - cxs[s] * xs[s - 1] - cxs[s + 1] * xs[s + 1] - cys[s] * xs[s - W] - cys[s + W] * xs[s + W];
+        acc += bs[s] - ax;
       }
     }
-    rs[idx] = r;
-  }
-  if (!restrict_to) return;
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < (TX / 2) * (TY / 2); idx += blockDim.x) {
-    int a = idx % (TX / 2), b = idx / (TX / 2);
-    int I = i0 / 2 + a, J = j0 / 2 + b;
-    if (I >= C.nI || J >= C.nJ) continue;
-    const T* r = &rs[2 * a + 2 * b * TX];
-    T acc = r[0] + r[1] + r[TX] + r[TX + 1];
-    C.b[(size_t)(I + 1) + (size_t)(J + 1) * C.ld] = (T)0.25 * acc;
+  if (RESTRICT) {
+    const int I = i0 / 2 + threadIdx.x, J = j0 / 2 + threadIdx.y;
+    if (I < C.nI && J < C.nJ) C.b[(size_t)(I + 1) + (size_t)(J + 1) * C.ld] = (T)0.25 * acc;
   }
 }
 
-// Post-smoothing sweep (black, then red) on one tile; with prolong_from, the
-// coarse correction is added to x first.  With part_rz (finest level, last
-// sweep), the block's share of r.z (b = r, x = z on that level) is written.
-template <typename T>
-__global__ void __launch_bounds__(256) k_post_sweep(Level<T> L, Level<T> C, int prolong_from, double* __restrict__ part_rz,
-                                                   const int* __restrict__ done) {
+// Post-smoothing sweep (black, then red); PROLONG adds the coarse correction while
+// staging.  With part_rz (finest level, last sweep), r.z (b = r, x = z there) is
+// reduced and beta published.
+template <typename T, bool PROLONG>
+__global__ void __launch_bounds__(BXT* BYT) k_post_sweep(Level<T> L, Level<T> C, T* __restrict__ xout, double* __restrict__ part_rz, unsigned* __restrict__ counter,
+                                                        Scalars* sc, const int* __restrict__ done) {
   if (*done) return;
-  constexpr int H = 2, W = TX + 2 * H, HH = TY + 2 * H;
-  __shared__ T xs[W * HH];
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  stage_x<T, H>(L, prolong_from ? &C : nullptr, xs, i0, j0, false);
+  constexpr int H = 2;
+  using Wn = Win<T, H>;
+  constexpr int W = Wn::W, N = Wn::N;
+  extern __shared__ unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const int i0 = blockIdx.x * TXS, j0 = blockIdx.y * TYS;
+  stage_window<T, H, true, PROLONG, false>(L, C, sm, i0, j0);
   __syncthreads();
-  half_sweep<T, H>(L, xs, i0, j0, 1, 1);
+  window_half<T, H, 1>(sm, i0, j0, L.nI, L.nJ, 1);
   __syncthreads();
-  half_sweep<T, H>(L, xs, i0, j0, 0, 2);
+  window_half<T, H, 2>(sm, i0, j0, L.nI, L.nJ, 0);
   __syncthreads();
-  double acc = 0.0;
-  for (int idx = threadIdx.x; idx < TX * TY; idx += blockDim.x) {
-    int ci = i0 + idx % TX, cj = j0 + idx / TX;
-    if (ci >= L.nI || cj >= L.nJ) continue;
-    size_t k = (size_t)(ci + 1) + (size_t)(cj + 1) * L.ld;
-    T z = xs[(idx % TX + H) + (idx / TX + H) * W];
-    L.x[k] = z;
-    if (part_rz) acc += (double)L.b[k] * (double)z;
-  }
+  const T *xs = sm, *bs = sm + N;
+  Acc<T> acc;
+#pragma unroll
+  for (int dr = 0; dr < 2; ++dr)
+#pragma unroll
+    for (int dc = 0; dc < 2; ++dc) {
+      const int ti = 2 * threadIdx.x + dc, tj = 2 * threadIdx.y + dr;
+      const int gi = i0 + ti, gj = j0 + tj;
+      if (gi >= L.nI || gj >= L.nJ) continue;
+      const int s = (ti + H) + (tj + H) * W;
+      xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
+      acc.add(bs[s] * xs[s]);
+    }
   if (part_rz) {
-    acc = block_sum(acc);
-    if (threadIdx.x == 0) part_rz[block_linear()] = acc;
+    double rz;
+    if (last_block_sum(acc.value(), part_rz, gridDim.x * gridDim.y, counter, &rz)) publish_rz(sc, rz);
   }
 }
 
-// ---- single-CTA tail: every level from the first with <= 64^2 cells down -------
+// ---- single-CTA tail: the coarse levels, coefficients resident in shared memory ---
 
 template <typename T>
 struct TailArgs {
   int nlev;
   Level<T> L[kMaxLevels];
-  int off[kMaxLevels];  // shared-memory offset (elements) of level l's x; b follows it
-  double* part_rz;      // when the tail starts at the finest level: r.z partial (slot 0)
+  int off[kMaxLevels];  // shared-memory offset (elements) of level l's arrays
+  Scalars* sc;          // when the tail starts at the finest level: publish r.z / beta
+};
+
+// Per tail level, six padded arrays: x, b, cx, cy, 1/dg, dg.
+template <typename T>
+struct TailLevel {
+  T *x, *b, *cx, *cy, *idg, *dg;
 };
 
 template <typename T>
-__device__ __forceinline__ void tail_half(const Level<T>& L, T* x, const T* b, int color) {
+__device__ __forceinline__ TailLevel<T> tail_level(T* sm, int off, const Level<T>& L) {
+  int n = (L.nI + 2) * (L.nJ + 2);
+  T* p = sm + off;
+  return TailLevel<T>{p, p + n, p + 2 * n, p + 3 * n, p + 4 * n, p + 5 * n};
+}
+
+template <typename T>
+__device__ __forceinline__ void tail_half(const Level<T>& L, const TailLevel<T>& t, int color) {
   int hw = (L.nI + 1) / 2;
-  for (int t = threadIdx.x; t < hw * L.nJ; t += blockDim.x) {
-    int j = t / hw;
-    int i = 2 * (t % hw) + ((j + color) & 1);
+  for (int u = threadIdx.x; u < hw * L.nJ; u += blockDim.x) {
+    int j = u / hw;
+    int i = 2 * (u % hw) + ((j + color) & 1);
     if (i >= L.nI) continue;
     int k = (i + 1) + (j + 1) * L.ld;
-    x[k] = (b[k] + L.cx[k] * x[k - 1] + L.cx[k + 1] * x[k + 1] + L.cy[k] * x[k - L.ld] + L.cy[k + L.ld] * x[k + L.ld]) * L.idg[k];
+    t.x[k] = (t.b[k] + t.cx[k] * t.x[k - 1] + t.cx[k + 1] * t.x[k + 1] + t.cy[k] * t.x[k - L.ld] + t.cy[k + L.ld] * t.x[k + L.ld]) * t.idg[k];
   }
 }
 
@@ -336,91 +468,93 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(TailArgs<T> a, const doub
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int nl = a.nlev;
-  int total = a.off[nl - 1] + 2 * (a.L[nl - 1].nI + 2) * (a.L[nl - 1].nJ + 2);
-  for (int t = threadIdx.x; t < total; t += blockDim.x) sm[t] = (T)0;
-  __syncthreads();
-  {
-    const Level<T>& L = a.L[0];
-    T* b = sm + a.off[0] + (L.nI + 2) * (L.nJ + 2);
-    for (int t = threadIdx.x; t < L.nI * L.nJ; t += blockDim.x) {
-      int k = (t % L.nI + 1) + (t / L.nI + 1) * L.ld;
-      b[k] = L.b[k];
+  // Stage every level's coefficients (padded arrays, so the zero ring comes along),
+  // the top level's right-hand side, and zero x / b below.
+  for (int l = 0; l < nl; ++l) {
+    const Level<T>& L = a.L[l];
+    TailLevel<T> t = tail_level(sm, a.off[l], L);
+    int n = (L.nI + 2) * (L.nJ + 2);
+    for (int u = threadIdx.x; u < n; u += blockDim.x) {
+      t.x[u] = (T)0;
+      t.b[u] = l == 0 ? L.b[u] : (T)0;
+      t.cx[u] = L.cx[u];
+      t.cy[u] = L.cy[u];
+      t.idg[u] = L.idg[u];
+      t.dg[u] = L.dg[u];
     }
   }
   __syncthreads();
   for (int l = 0; l < nl - 1; ++l) {
     const Level<T>& L = a.L[l];
-    T* x = sm + a.off[l];
-    T* b = x + (L.nI + 2) * (L.nJ + 2);
+    TailLevel<T> t = tail_level(sm, a.off[l], L);
     for (int s = 0; s < nu; ++s) {
-      tail_half(L, x, b, 0);
+      tail_half(L, t, 0);
       __syncthreads();
-      tail_half(L, x, b, 1);
+      tail_half(L, t, 1);
       __syncthreads();
     }
     const Level<T>& C = a.L[l + 1];
-    T* cb = sm + a.off[l + 1] + (C.nI + 2) * (C.nJ + 2);
-    for (int t = threadIdx.x; t < C.nI * C.nJ; t += blockDim.x) {
-      int I = t % C.nI, J = t / C.nI;
+    TailLevel<T> tc = tail_level(sm, a.off[l + 1], C);
+    for (int u = threadIdx.x; u < C.nI * C.nJ; u += blockDim.x) {
+      int I = u % C.nI, J = u / C.nI;
       T acc = 0;
       for (int bb = 0; bb < 2; ++bb)
         for (int aa = 0; aa < 2; ++aa) {
           int i = 2 * I + aa, j = 2 * J + bb;
           if (i >= L.nI || j >= L.nJ) continue;
           int k = (i + 1) + (j + 1) * L.ld;
-          T ax = L.dg[k] * x[k] - L.cx[k] * x[k - 1] - L.cx[k + 1] * x[k + 1] - L.cy[k] * x[k - L.ld] - L.cy[k + L.ld] * x[k + L.ld];
-          acc += b[k] - ax;
+          T ax = t.dg[k] * t.x[k] - t.cx[k] * t.x[k - 1] - t.cx[k + 1] * t.x[k + 1] - t.cy[k] * t.x[k - L.ld] - t.cy[k + L.ld] * t.x[k + L.ld];
+          acc += t.b[k] - ax;
         }
-      cb[(I + 1) + (J + 1) * C.ld] = (T)0.25 * acc;
+      tc.b[(I + 1) + (J + 1) * C.ld] = (T)0.25 * acc;
     }
     __syncthreads();
   }
   {
     const Level<T>& C = a.L[nl - 1];
-    T* x = sm + a.off[nl - 1];
-    T* b = x + (C.nI + 2) * (C.nJ + 2);
+    TailLevel<T> t = tail_level(sm, a.off[nl - 1], C);
     int n = C.nI * C.nJ;
     if ((int)threadIdx.x < n) {
       double acc = 0.0;
-      for (int m = 0; m < n; ++m) acc += ainv[(size_t)threadIdx.x * n + m] * (double)b[(m % C.nI + 1) + (m / C.nI + 1) * C.ld];
-      x[(threadIdx.x % C.nI + 1) + (threadIdx.x / C.nI + 1) * C.ld] = (T)acc;
+      for (int m = 0; m < n; ++m) acc += ainv[(size_t)threadIdx.x * n + m] * (double)t.b[(m % C.nI + 1) + (m / C.nI + 1) * C.ld];
+      t.x[(threadIdx.x % C.nI + 1) + (threadIdx.x / C.nI + 1) * C.ld] = (T)acc;
     }
     __syncthreads();
   }
   for (int l = nl - 2; l >= 0; --l) {
     const Level<T>& L = a.L[l];
     const Level<T>& C = a.L[l + 1];
-    T* x = sm + a.off[l];
-    T* b = x + (L.nI + 2) * (L.nJ + 2);
-    const T* cx = sm + a.off[l + 1];
-    for (int t = threadIdx.x; t < L.nI * L.nJ; t += blockDim.x) {
-      int i = t % L.nI, j = t / L.nI;
-      x[(i + 1) + (j + 1) * L.ld] += cx[(i / 2 + 1) + (j / 2 + 1) * C.ld];
+    TailLevel<T> t = tail_level(sm, a.off[l], L);
+    const T* xc = tail_level(sm, a.off[l + 1], C).x;
+    for (int u = threadIdx.x; u < L.nI * L.nJ; u += blockDim.x) {
+      int i = u % L.nI, j = u / L.nI;
+      t.x[(i + 1) + (j + 1) * L.ld] += xc[(i / 2 + 1) + (j / 2 + 1) * C.ld];
     }
     __syncthreads();
     for (int s = 0; s < nu; ++s) {
-      tail_half(L, x, b, 1);
+      tail_half(L, t, 1);
       __syncthreads();
-      tail_half(L, x, b, 0);
+      tail_half(L, t, 0);
       __syncthreads();
     }
   }
   {
     const Level<T>& L = a.L[0];
-    const T* x = sm + a.off[0];
-    const T* b = x + (L.nI + 2) * (L.nJ + 2);
+    TailLevel<T> t = tail_level(sm, a.off[0], L);
     double acc = 0.0;
-    for (int t = threadIdx.x; t < L.nI * L.nJ; t += blockDim.x) {
-      int k = (t % L.nI + 1) + (t / L.nI + 1) * L.ld;
-      L.x[k] = x[k];
-      acc += (double)b[k] * (double)x[k];
+    for (int u = threadIdx.x; u < L.nI * L.nJ; u += blockDim.x) {
+      int k = (u % L.nI + 1) + (u / L.nI + 1) * L.ld;
+      L.x[k] = t.x[k];
+      acc += (double)t.b[k] * (double)t.x[k];
     }
-    if (a.part_rz) {
+    if (a.sc) {
       acc = block_sum(acc);
-      if (threadIdx.x == 0) a.part_rz[0] = acc;
+      publish_rz(a.sc, acc);
     }
   }
 }
+
+#include "gb2d_ctail.cuh"
 
 // ---- CG kernels ------------------------------------------------------------------
 
@@ -456,26 +590,25 @@ __global__ void k_reduce_two(const double* __restrict__ pa, const double* __rest
   }
 }
 
-// Search direction and operator: beta = rz_new / rz_old, p_new = z + beta p_old
-// (p_new = z when first), Ap = A p_new in flux form, partial p_new.Ap.  The
-// neighbours' p_new are formed on the fly from z and p_old.  Block 0 records
-// rz_new in rz[par ^ 1] (rz[par] is the value of the previous direction).
+// Search direction and operator: p_new = z + beta p_old (p_new = z when first,
+// which also clears the correction e), Ap = A p_new in flux form; the last block
+// forms p.Ap and publishes alpha = rz_new / p.Ap and rz_cur = rz_new.  The
+// neighbours' p_new are formed on the fly from z and p_old.
 template <typename T>
 __global__ void k_direction_apply(Level<T> L, const T* __restrict__ z, const T* __restrict__ pold, T* __restrict__ pnew, T* __restrict__ ap,
-                                  const double* __restrict__ part_rz, int nrz, Scalars* sc, int par, int first, double* __restrict__ part_pap,
-                                  const int* __restrict__ done) {
+                                  T* __restrict__ e, T* __restrict__ elo, Scalars* sc, int first, double* __restrict__ part_pap,
+                                  unsigned* __restrict__ counter, const int* __restrict__ done) {
   if (*done) return;
-  double rz = sum_partials(part_rz, nrz);
-  double beta = first ? 0.0 : rz / sc->rz[par];
-  if (blockIdx.x == 0 && threadIdx.x == 0) sc->rz[par ^ 1] = rz;
-  const T bt = (T)beta;
-  double acc = 0.0;
+  const T bt = first ? (T)0 : (T)sc->beta;
+  Acc<T> acc;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
     int i, j;
     size_t k = cell_index(L, t, i, j);
     T pc, pl, pr, pb, pt;
     if (first) {
       pc = z[k], pl = z[k - 1], pr = z[k + 1], pb = z[k - L.ld], pt = z[k + L.ld];
+      e[k] = (T)0;
+      if (elo) elo[k] = (T)0;
     } else {
       pc = z[k] + bt * pold[k];
       pl = z[k - 1] + bt * pold[k - 1];
@@ -486,72 +619,95 @@ __global__ void k_direction_apply(Level<T> L, const T* __restrict__ z, const T* 
     T y = L.sh[k] * pc + L.cx[k] * (pc - pl) + L.cx[k + 1] * (pc - pr) + L.cy[k] * (pc - pb) + L.cy[k + L.ld] * (pc - pt);
     pnew[k] = pc;
     ap[k] = y;
-    acc += (double)pc * (double)y;
+    acc.add(pc * y);
   }
-  acc = block_sum(acc);
-  if (threadIdx.x == 0) part_pap[blockIdx.x] = acc;
+  double pap;
+  if (last_block_sum(acc.value(), part_pap, gridDim.x, counter, &pap) && threadIdx.x == 0) {
+    double rz = sc->rz_new;
+    sc->rz_cur = rz;
+    sc->alpha = rz / pap;
+  }
 }
 
-// alpha = r.z / p.Ap;  x (FP64) += alpha p;  r -= alpha Ap;  ||r||^2.  The last
-// block to finish sums the partials, stores ||r||^2 for the host and raises the
-// done flag at the threshold (or on a non-finite value).
+// e += alpha p;  r -= alpha Ap;  ||r||^2.  The last block stores ||r||^2 for the
+// host and raises the done flag at the threshold (or on a non-finite value).
+// With elo (FP32 vectors), e is kept as the unevaluated sum e + elo (Knuth's
+// TwoSum per update): a plain FP32 correction would carry a rounding error of
+// 2^-24 |e| whose high-frequency residual A de stalls the refinement near 1e-8.
+__device__ __forceinline__ void two_sum_into(float& hi, float& lo, float v) {
+  float s = __fadd_rn(hi, v);
+  float bv = __fsub_rn(s, hi);
+  float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(v, bv));
+  hi = s;
+  lo = __fadd_rn(lo, err);
+}
+
 template <typename T>
-__global__ void k_cg_update(Level<T> L, double* __restrict__ x, T* __restrict__ r, const T* __restrict__ p, const T* __restrict__ ap,
-                            const double* __restrict__ part_pap, int nparts, Scalars* sc, int par, double* __restrict__ part_rr,
-                            unsigned* __restrict__ counter, int* __restrict__ done, double* __restrict__ host_rr) {
+__global__ void k_cg_update(Level<T> L, T* __restrict__ e, T* __restrict__ elo, T* __restrict__ r, const T* __restrict__ p,
+                            const T* __restrict__ ap, Scalars* sc, double* __restrict__ part_rr, unsigned* __restrict__ counter,
+                            int* __restrict__ done, double* __restrict__ host_rr) {
   if (*done) return;
-  double pap = sum_partials(part_pap, nparts);
-  double alpha = sc->rz[par] / pap;
-  const T at = (T)alpha;
-  double acc = 0.0;
+  const T at = (T)sc->alpha;
+  Acc<T> acc;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
     int i, j;
     size_t k = cell_index(L, t, i, j);
-    x[k] += alpha * (double)p[k];
+    if constexpr (sizeof(T) == 4) {
+      float hi = e[k], lo = elo[k];
+      two_sum_into(hi, lo, __fmul_rn(at, p[k]));
+      e[k] = hi;
+      elo[k] = lo;
+    } else {
+      e[k] += at * p[k];
+    }
     T rn = r[k] - at * ap[k];
     r[k] = rn;
-    acc += (double)rn * (double)rn;
+    acc.add(rn * rn);
   }
-  acc = block_sum(acc);
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
-    part_rr[blockIdx.x] = acc;
-    __threadfence();
-    last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  double rr = sum_partials(part_rr, gridDim.x);
-  if (threadIdx.x == 0) {
+  double rr;
+  if (last_block_sum(acc.value(), part_rr, gridDim.x, counter, &rr) && threadIdx.x == 0) {
     sc->rr = rr;
     if (!(rr > sc->thr2)) {
       *done = 1;
       if (!isfinite(rr)) sc->flag |= 1;
     }
     *host_rr = rr;
-    *counter = 0u;
   }
 }
 
-// Jacobi preconditioner z = r / dg with partial r.z.
+// Jacobi preconditioner z = r / dg; the last block publishes r.z and beta.
 template <typename T>
-__global__ void k_jacobi(Level<T> L, const T* __restrict__ r, T* __restrict__ z, double* __restrict__ part_rz, const int* __restrict__ done) {
+__global__ void k_jacobi(Level<T> L, const T* __restrict__ r, T* __restrict__ z, Scalars* sc, double* __restrict__ part_rz,
+                         unsigned* __restrict__ counter, const int* __restrict__ done) {
   if (*done) return;
-  double acc = 0.0;
+  Acc<T> acc;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
     int i, j;
     size_t k = cell_index(L, t, i, j);
     T zv = r[k] * L.idg[k];
     z[k] = zv;
-    acc += (double)r[k] * (double)zv;
+    acc.add(r[k] * zv);
   }
-  acc = block_sum(acc);
-  if (threadIdx.x == 0) part_rz[blockIdx.x] = acc;
+  double rz;
+  if (last_block_sum(acc.value(), part_rz, gridDim.x, counter, &rz)) publish_rz(sc, rz);
+}
+
+// x (FP64) += e (+ elo): the inner solve's correction joins the FP64 solution.
+template <typename T>
+__global__ void k_add_correction(Level<T> L, double* __restrict__ x, const T* __restrict__ e, const T* __restrict__ elo) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
+    int i, j;
+    size_t k = cell_index(L, t, i, j);
+    double d = (double)e[k];
+    if (elo) d += (double)elo[k];
+    x[k] += d;
+  }
 }
 
 __global__ void k_begin_inner(Scalars* sc, int* done, double thr2) {
   *done = 0;
   sc->thr2 = thr2;
+  sc->rz_cur = 1.0;
 }
 
 }  // namespace
@@ -562,8 +718,14 @@ template <typename T>
 struct Hierarchy {
   int nlev = 0, tail = 0;  // levels [tail, nlev) run in the single-CTA tail kernel
   size_t tail_smem = 0;
+  int ctail = -1;          // levels [ctail, nlev) run in the cluster tail (-1: not used)
+  int ct_P = 0;            // CTAs in that cluster
+  size_t ct_smem = 0;
+  CtArgs<T> ct;
   Level<T> L[kMaxLevels];
   T *p[2] = {nullptr, nullptr}, *ap = nullptr, *r = nullptr;  // CG vectors (padded fine layout); z = L[0].x
+  T* e = nullptr;    // correction accumulated by the inner solve
+  T* elo = nullptr;  // its low part (FP32 hierarchy only)
 };
 
 struct GraphSet {
@@ -579,9 +741,9 @@ struct Solver {
   double* ainv64 = nullptr;
   double* ainv32 = nullptr;
   double* b64 = nullptr;   // right-hand side, padded
-  double* part = nullptr;  // 4 slots x nparts_cap
+  double* part = nullptr;  // 4 slots x nparts_cap: p.Ap, r.r, r.z, b.b
   int nparts_cap = 0;
-  unsigned* counter = nullptr;
+  unsigned* counter = nullptr;  // 4 last-block counters: p.Ap, r.r, r.z (jacobi), r.z (sweep)
   double* host = nullptr;  // pinned: [0..1] per-parity r.r, [4..5] residual / rhs norms
   int* done = nullptr;
   Scalars* sc = nullptr;
@@ -600,7 +762,7 @@ cudaError_t alloc_level(Level<T>& L, int nI, int nJ, bool own_b) {
   L.nJ = nJ;
   L.ld = nI + 2;
   size_t n = (size_t)(nI + 2) * (nJ + 2);
-  T** arrs[7] = {&L.cx, &L.cy, &L.dg, &L.idg, &L.sh, &L.x, &L.b};
+  T** arrs[8] = {&L.cx, &L.cy, &L.dg, &L.idg, &L.sh, &L.x, &L.xa, &L.b};
   for (auto a : arrs) {
     if (a == &L.b && !own_b) continue;
     cudaError_t e = cudaMalloc(a, n * sizeof(T));
@@ -613,7 +775,7 @@ cudaError_t alloc_level(Level<T>& L, int nI, int nJ, bool own_b) {
 
 template <typename T>
 void free_level(Level<T>& L, bool own_b) {
-  T* arrs[7] = {L.cx, L.cy, L.dg, L.idg, L.sh, L.x, own_b ? L.b : nullptr};
+  T* arrs[8] = {L.cx, L.cy, L.dg, L.idg, L.sh, L.x, L.xa, own_b ? L.b : nullptr};
   for (auto a : arrs)
     if (a) cudaFree(a);
 }
@@ -621,8 +783,9 @@ void free_level(Level<T>& L, bool own_b) {
 template <typename T>
 cudaError_t alloc_hierarchy(Hierarchy<T>& H, int ni, int nj) {
   size_t n = (size_t)(ni + 2) * (nj + 2);
-  T** v[4] = {&H.p[0], &H.p[1], &H.ap, &H.r};
+  T** v[6] = {&H.p[0], &H.p[1], &H.ap, &H.r, &H.e, &H.elo};
   for (auto a : v) {
+    if (a == &H.elo && sizeof(T) != 4) continue;
     cudaError_t e = cudaMalloc(a, n * sizeof(T));
     if (e != cudaSuccess) return e;
     e = cudaMemset(*a, 0, n * sizeof(T));
@@ -643,12 +806,12 @@ cudaError_t alloc_hierarchy(Hierarchy<T>& H, int ni, int nj) {
     nI = (nI + 1) / 2;
     nJ = (nJ + 1) / 2;
   }
-  // Shared memory of the tail: x and b of every tail level; start one level lower
-  // while it does not fit.
+  // Shared memory of the tail: six padded arrays per tail level; start one level
+  // lower while it does not fit.
   const size_t kSmemCap = 200 * 1024;
   while (true) {
     size_t elems = 0;
-    for (int l = H.tail; l < H.nlev; ++l) elems += 2 * (size_t)(H.L[l].nI + 2) * (H.L[l].nJ + 2);
+    for (int l = H.tail; l < H.nlev; ++l) elems += 6 * (size_t)(H.L[l].nI + 2) * (H.L[l].nJ + 2);
     H.tail_smem = elems * sizeof(T);
     if (H.tail_smem <= kSmemCap || H.tail == H.nlev - 1) break;
     H.tail++;
@@ -657,10 +820,148 @@ cudaError_t alloc_hierarchy(Hierarchy<T>& H, int ni, int nj) {
   return cudaSuccess;
 }
 
+inline int ceil_log2(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return l;
+}
+
+// Lay out the cluster tail: the finest top level whose levels fit in one CTA's
+// shared memory.  Distributed levels have at least P * kCtMinRows rows; the
+// coarsest level is always local.  Returns false (single-CTA tail instead) when
+// no top level qualifies.
+template <typename T>
+bool plan_ctail(Hierarchy<T>& H, int P) {
+  H.ctail = -1;
+  if (P < 2 || P > kClusterMax) return false;
+  const int nl = H.nlev;
+  for (int top = 0; top < nl - 1; ++top) {
+    if (nl - top > kCtMaxLevels) continue;
+    int lb = top - 1;
+    while (lb + 1 < nl - 1 && H.L[lb + 1].nJ >= P * kCtMinRows) ++lb;
+    if (lb < top || H.L[lb].nJ > kCtOwnerRows) continue;
+    CtArgs<T> a;
+    memset(&a, 0, sizeof a);
+    a.nlev = nl - top;
+    a.ndist = lb - top + 1;
+    for (int c = 0; c <= P; ++c) a.J0[a.ndist - 1][c] = (short)((long)c * H.L[lb].nJ / P);
+    for (int l = a.ndist - 2; l >= 0; --l) {
+      for (int c = 0; c < P; ++c) a.J0[l][c] = (short)(2 * a.J0[l + 1][c]);
+      a.J0[l][P] = (short)H.L[top + l].nJ;
+    }
+    size_t off = 0;
+    bool ok = true;
+    for (int l = 0; l < a.nlev; ++l) {
+      const Level<T>& L = H.L[top + l];
+      CtLevel<T>& C = a.L[l];
+      C.nI = L.nI;
+      C.nJ = L.nJ;
+      C.ld = L.ld;
+      int rc = L.nJ;
+      if (l < a.ndist) {
+        rc = 0;
+        for (int c = 0; c < P; ++c) {
+          int r = a.J0[l][c + 1] - a.J0[l][c];
+          if (r < 1) ok = false;
+          rc = r > rc ? r : rc;
+        }
+      }
+      C.rows_cap = rc;
+      C.off = (int)off;
+      off += 6 * (size_t)(rc + 2) * L.ld;
+      int hw = (L.nI + 1) / 2;
+      C.half_log2 = ceil_log2(hw < kCtThreads ? hw : kCtThreads);
+      C.full_log2 = ceil_log2(L.nI < kCtThreads ? L.nI : kCtThreads);
+      C.cx = L.cx;
+      C.cy = L.cy;
+      C.idg = L.idg;
+      C.dg = L.dg;
+      C.b = L.b;
+      C.x = L.x;
+    }
+    if (!ok) continue;
+    a.res_off = (int)off;
+    off += (size_t)(a.L[a.ndist - 1].rows_cap + 2) * a.L[a.ndist - 1].ld;
+    a.ainv_off = (int)off;
+    const int nc = H.L[nl - 1].nI * H.L[nl - 1].nJ;
+    off += (size_t)nc * nc;
+    const size_t bytes = off * sizeof(T);
+    if (bytes > kCtSmemCap) continue;
+    H.ctail = top;
+    H.ct = a;
+    H.ct_P = P;
+    H.ct_smem = bytes;
+    return true;
+  }
+  return false;
+}
+
+// Cluster size the part can co-schedule for the cluster tail (16, else 8), or 0.
+// GB2D_CLUSTER_TAIL=0 in the environment selects the single-CTA tail instead.
+int ctail_cluster_size() {
+  const char* env = getenv("GB2D_CLUSTER_TAIL");
+  if (env && env[0] == '0') return 0;
+  static int cached = -1;
+  if (cached >= 0) return cached;
+  cached = 0;
+  bool attr_ok = cudaFuncSetAttribute(k_ctail<float>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+                 cudaFuncSetAttribute(k_ctail<double>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess &&
+                 cudaFuncSetAttribute(k_ctail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCtSmemCap) == cudaSuccess &&
+                 cudaFuncSetAttribute(k_ctail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCtSmemCap) == cudaSuccess;
+  if (!attr_ok) {
+    cudaGetLastError();
+    return cached;
+  }
+  for (int P : {16, 8}) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = P;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(P);
+    cfg.blockDim = dim3(kCtThreads);
+    cfg.dynamicSmemBytes = kCtSmemCap;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int n32 = 0, n64 = 0;
+    bool ok = cudaOccupancyMaxActiveClusters(&n32, k_ctail<float>, &cfg) == cudaSuccess &&
+              cudaOccupancyMaxActiveClusters(&n64, k_ctail<double>, &cfg) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      continue;
+    }
+    if (n32 >= 1 && n64 >= 1) {
+      cached = P;
+      break;
+    }
+  }
+  return cached;
+}
+
+template <typename T>
+void launch_ctail(cudaStream_t s, const Hierarchy<T>& H, const double* ainv, int nu, const int* done, Scalars* sc) {
+  CtArgs<T> a = H.ct;
+  a.sc = H.ctail == 0 ? sc : nullptr;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = H.ct_P;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(H.ct_P);
+  cfg.blockDim = dim3(kCtThreads);
+  cfg.dynamicSmemBytes = H.ct_smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_ctail<T>, a, ainv, nu, done);
+}
+
 template <typename T>
 void free_hierarchy(Hierarchy<T>& H) {
   for (int l = 0; l < H.nlev; ++l) free_level(H.L[l], l > 0);
-  T* v[4] = {H.p[0], H.p[1], H.ap, H.r};
+  T* v[6] = {H.p[0], H.p[1], H.ap, H.r, H.e, H.elo};
   for (auto a : v)
     if (a) cudaFree(a);
 }
@@ -671,7 +972,7 @@ inline unsigned nblocks(size_t n, unsigned cap) {
   return (unsigned)(b < cap ? b : cap);
 }
 
-inline dim3 tiles(int nI, int nJ) { return dim3((nI + TX - 1) / TX, (nJ + TY - 1) / TY); }
+inline dim3 tiles(int nI, int nJ) { return dim3((nI + TXS - 1) / TXS, (nJ + TYS - 1) / TYS); }
 
 template <typename T>
 void build_hierarchy(cudaStream_t s, Hierarchy<T>& H, const gb2d_ctx* c, double* b64, double* ainv) {
@@ -717,70 +1018,90 @@ inline void probe_end(Probe* pr, cudaStream_t s, bool on, double bytes) {
   pr->n++;
 }
 
-// z = M r: the fine level's x/b are z/r.  part_rz receives r.z partials (one per
-// finest-level tile, or one from the tail when it starts at the finest level).
+// z = M r: the fine level's x/b are z/r.  The last finest-level post-sweep (or the
+// tail, when it starts at the finest level) publishes r.z and beta.
 template <typename T>
-void vcycle(cudaStream_t s, Hierarchy<T>& H, const double* ainv, int nu, const int* done, double* part_rz, Probe* pr) {
-  const int tail = H.tail;
+void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int nu, Probe* pr) {
+  const bool cluster = H.ctail >= 0;
+  const int tail = cluster ? H.ctail : H.tail;
+  const int* done = S->done;
+  double* P_rz = S->part + 2 * (size_t)S->nparts_cap;
+  const dim3 blk(BXT, BYT);
+  // Sweep k of a level's 2*nu writes L.xa or L.x so that the last one writes L.x
+  // (the buffer the next finer level prolongs from, and z on the finest level).
+  auto out = [nu](const Level<T>& L, int k) { return ((2 * nu - 1 - k) & 1) ? L.xa : L.x; };
+  auto reading = [](Level<T> L, T* x) {
+    L.x = x;
+    return L;
+  };
   for (int l = 0; l < tail; ++l) {
     Level<T>& L = H.L[l];
+    const dim3 grd = tiles(L.nI, L.nJ);
     for (int sweep = 0; sweep < nu; ++sweep) {
-      bool last = sweep == nu - 1;
+      bool last = sweep == nu - 1, zero = sweep == 0;
       bool on = l == 0 && probe_begin(pr, s);
-      if (last)
-        k_pre_sweep<T, 3><<<tiles(L.nI, L.nJ), 256, 0, s>>>(L, H.L[l + 1], sweep == 0, 1, done);
+      Level<T> Lin = reading(L, zero ? nullptr : out(L, sweep - 1));
+      T* xo = out(L, sweep);
+      if (zero && last)
+        k_pre_sweep<T, true, true><<<grd, blk, sweep_smem<T, 3, true>(), s>>>(Lin, H.L[l + 1], xo, done);
+      else if (zero)
+        k_pre_sweep<T, true, false><<<grd, blk, sweep_smem<T, 2, false>(), s>>>(Lin, H.L[l + 1], xo, done);
+      else if (last)
+        k_pre_sweep<T, false, true><<<grd, blk, sweep_smem<T, 3, true>(), s>>>(Lin, H.L[l + 1], xo, done);
       else
-        k_pre_sweep<T, 2><<<tiles(L.nI, L.nJ), 256, 0, s>>>(L, H.L[l + 1], sweep == 0, 0, done);
+        k_pre_sweep<T, false, false><<<grd, blk, sweep_smem<T, 2, false>(), s>>>(Lin, H.L[l + 1], xo, done);
       GB_LAUNCHED(1);
-      probe_end(pr, s, on, sweep_bytes(L, sweep == 0, last, false));
+      probe_end(pr, s, on, sweep_bytes(L, zero, last, false));
     }
   }
-  TailArgs<T> ta;
-  memset(&ta, 0, sizeof ta);
-  ta.nlev = H.nlev - tail;
-  int off = 0;
-  for (int l = 0; l < ta.nlev; ++l) {
-    ta.L[l] = H.L[tail + l];
-    ta.off[l] = off;
-    off += 2 * (ta.L[l].nI + 2) * (ta.L[l].nJ + 2);
+  if (cluster) {
+    launch_ctail<T>(s, H, ainv, nu, done, S->sc);
+  } else {
+    TailArgs<T> ta;
+    memset(&ta, 0, sizeof ta);
+    ta.nlev = H.nlev - tail;
+    int off = 0;
+    for (int l = 0; l < ta.nlev; ++l) {
+      ta.L[l] = H.L[tail + l];
+      ta.off[l] = off;
+      off += 6 * (ta.L[l].nI + 2) * (ta.L[l].nJ + 2);
+    }
+    ta.sc = tail == 0 ? S->sc : nullptr;
+    k_tail<T><<<1, kTailThreads, H.tail_smem, s>>>(ta, ainv, nu, done);
   }
-  ta.part_rz = tail == 0 ? part_rz : nullptr;
-  k_tail<T><<<1, kTailThreads, H.tail_smem, s>>>(ta, ainv, nu, done);
   GB_LAUNCHED(1);
   for (int l = tail - 1; l >= 0; --l) {
     Level<T>& L = H.L[l];
+    const dim3 grd = tiles(L.nI, L.nJ);
     for (int sweep = 0; sweep < nu; ++sweep) {
       bool first = sweep == 0;
-      double* prz = (l == 0 && sweep == nu - 1) ? part_rz : nullptr;
+      double* prz = (l == 0 && sweep == nu - 1) ? P_rz : nullptr;
       bool on = l == 0 && probe_begin(pr, s);
-      k_post_sweep<T><<<tiles(L.nI, L.nJ), 256, 0, s>>>(L, H.L[l + 1], first, prz, done);
+      Level<T> Lin = reading(L, out(L, nu + sweep - 1));
+      T* xo = out(L, nu + sweep);
+      if (first)
+        k_post_sweep<T, true><<<grd, blk, sweep_smem<T, 2, false>(), s>>>(Lin, H.L[l + 1], xo, prz, S->counter + 3, S->sc, done);
+      else
+        k_post_sweep<T, false><<<grd, blk, sweep_smem<T, 2, false>(), s>>>(Lin, H.L[l + 1], xo, prz, S->counter + 3, S->sc, done);
       GB_LAUNCHED(1);
       probe_end(pr, s, on, sweep_bytes(L, false, false, first));
     }
   }
 }
 
-template <typename T>
-int n_rz_parts(const Hierarchy<T>& H, bool use_mg, unsigned G) {
-  if (!use_mg) return (int)G;
-  if (H.tail == 0) return 1;
-  dim3 t = tiles(H.L[0].nI, H.L[0].nJ);
-  return (int)(t.x * t.y);
-}
-
-// Preconditioner + first direction: z = M r, p[0] = z, Ap, rz[0].
+// Preconditioner + first direction: z = M r, p[0] = z, Ap, alpha.
 template <typename T>
 void enqueue_init(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int use_mg, int nu, Probe* pr) {
   Level<T>& L = H.L[0];
   double* P_pap = S->part;
   double* P_rz = S->part + 2 * (size_t)S->nparts_cap;
   if (use_mg) {
-    vcycle<T>(s, H, ainv, nu, S->done, P_rz, pr);
+    vcycle<T>(s, S, H, ainv, nu, pr);
   } else {
-    k_jacobi<T><<<S->G, kThreads, 0, s>>>(L, H.r, L.x, P_rz, S->done);
+    k_jacobi<T><<<S->G, kThreads, 0, s>>>(L, H.r, L.x, S->sc, P_rz, S->counter + 2, S->done);
     GB_LAUNCHED(1);
   }
-  k_direction_apply<T><<<S->G, kThreads, 0, s>>>(L, L.x, H.p[1], H.p[0], H.ap, P_rz, n_rz_parts(H, use_mg, S->G), S->sc, 1, 1, P_pap, S->done);
+  k_direction_apply<T><<<S->G, kThreads, 0, s>>>(L, L.x, H.p[1], H.p[0], H.ap, H.e, H.elo, S->sc, 1, P_pap, S->counter, S->done);
   GB_LAUNCHED(1);
 }
 
@@ -791,16 +1112,15 @@ void enqueue_iter(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv
   double* P_pap = S->part;
   double* P_rr = S->part + (size_t)S->nparts_cap;
   double* P_rz = S->part + 2 * (size_t)S->nparts_cap;
-  k_cg_update<T><<<S->G, kThreads, 0, s>>>(L, x64, H.r, H.p[par], H.ap, P_pap, S->G, S->sc, par, P_rr, S->counter, S->done, S->host + par);
+  k_cg_update<T><<<S->G, kThreads, 0, s>>>(L, H.e, H.elo, H.r, H.p[par], H.ap, S->sc, P_rr, S->counter + 1, S->done, S->host + par);
   GB_LAUNCHED(1);
   if (use_mg) {
-    vcycle<T>(s, H, ainv, nu, S->done, P_rz, pr);
+    vcycle<T>(s, S, H, ainv, nu, pr);
   } else {
-    k_jacobi<T><<<S->G, kThreads, 0, s>>>(L, H.r, L.x, P_rz, S->done);
+    k_jacobi<T><<<S->G, kThreads, 0, s>>>(L, H.r, L.x, S->sc, P_rz, S->counter + 2, S->done);
     GB_LAUNCHED(1);
   }
-  k_direction_apply<T><<<S->G, kThreads, 0, s>>>(L, L.x, H.p[par], H.p[par ^ 1], H.ap, P_rz, n_rz_parts(H, use_mg, S->G), S->sc, par, 0, P_pap,
-                                                 S->done);
+  k_direction_apply<T><<<S->G, kThreads, 0, s>>>(L, L.x, H.p[par], H.p[par ^ 1], H.ap, H.e, H.elo, S->sc, 0, P_pap, S->counter, S->done);
   GB_LAUNCHED(1);
 }
 
@@ -888,6 +1208,8 @@ int inner_pcg(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, doubl
     }
     k++;
   }
+  k_add_correction<T><<<S->G, kThreads, 0, s>>>(H.L[0], x64, H.e, H.elo);
+  GB_LAUNCHED(1);
   cudaStreamSynchronize(s);
   if (iters < 0) {
     iters = k;
@@ -909,14 +1231,19 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
   size_t np = (size_t)(ni + 2) * (nj + 2);
   cudaError_t e = alloc_hierarchy(S->h64, ni, nj);
   if (e == cudaSuccess) e = alloc_hierarchy(S->h32, ni, nj);
+  if (e == cudaSuccess) {
+    int P = ctail_cluster_size();
+    plan_ctail(S->h64, P);
+    plan_ctail(S->h32, P);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&S->ainv64, sizeof(double) * kCoarseMax * kCoarseMax);
   if (e == cudaSuccess) e = cudaMalloc(&S->ainv32, sizeof(double) * kCoarseMax * kCoarseMax);
   if (e == cudaSuccess) e = cudaMalloc(&S->b64, np * sizeof(double));
   if (e == cudaSuccess) e = cudaMemset(S->b64, 0, np * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&S->part, sizeof(double) * 4 * (size_t)S->nparts_cap);
   if (e == cudaSuccess) e = cudaMemset(S->part, 0, sizeof(double) * 4 * (size_t)S->nparts_cap);
-  if (e == cudaSuccess) e = cudaMalloc(&S->counter, sizeof(unsigned));
-  if (e == cudaSuccess) e = cudaMemset(S->counter, 0, sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&S->counter, 4 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMemset(S->counter, 0, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&S->done, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(S->done, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&S->sc, sizeof(Scalars));
@@ -924,8 +1251,22 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
   if (e == cudaSuccess) e = cudaMallocHost(&S->host, 8 * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->ev[0], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->ev[1], cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->h64.tail_smem);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->h32.tail_smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_sweep<double, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 3, true>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_sweep<double, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 3, true>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_sweep<double, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 2, false>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_sweep<double, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 2, false>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_sweep<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 2, false>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_sweep<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 2, false>());
+  // The attribute is per kernel for the whole process: only ever raise it.
+  static size_t tail_smem_set[2] = {0, 0};
+  if (e == cudaSuccess && S->h64.tail_smem > tail_smem_set[0]) {
+    e = cudaFuncSetAttribute(k_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->h64.tail_smem);
+    if (e == cudaSuccess) tail_smem_set[0] = S->h64.tail_smem;
+  }
+  if (e == cudaSuccess && S->h32.tail_smem > tail_smem_set[1]) {
+    e = cudaFuncSetAttribute(k_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S->h32.tail_smem);
+    if (e == cudaSuccess) tail_smem_set[1] = S->h32.tail_smem;
+  }
   if (e != cudaSuccess) {
     snprintf(err, errlen, "solver allocation failed: %s", cudaGetErrorString(e));
     solver_destroy(S);
@@ -955,6 +1296,18 @@ void solver_destroy(Solver* S) {
   for (auto e : S->ev)
     if (e) cudaEventDestroy(e);
   delete S;
+}
+
+void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, int* cluster_ctas) {
+  if (mixed) {
+    *levels = S->h32.nlev;
+    *cluster_top = S->h32.ctail;
+    *cluster_ctas = S->h32.ctail >= 0 ? S->h32.ct_P : 0;
+  } else {
+    *levels = S->h64.nlev;
+    *cluster_top = S->h64.ctail;
+    *cluster_ctas = S->h64.ctail >= 0 ? S->h64.ct_P : 0;
+  }
 }
 
 // x: padded FP64 solution (warm start in, result out); the system is ctx->bx/by/diag/rhs.

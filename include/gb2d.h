@@ -118,6 +118,13 @@ int gb2d_probe_read(gb2d_ctx* ctx, int* launches, double* total_ms, double* byte
 /* Kernels this library has launched in this process so far (all contexts). */
 int gb2d_kernel_launches(unsigned long long* count);
 
+/* Multigrid layout of the pressure solver for one precision (GB2D_PRECISION_FP64
+ * or GB2D_PRECISION_MIXED, whose V-cycles run in FP32): the number of levels, the
+ * first level handled by the thread-block-cluster tail kernel (-1 when the
+ * single-CTA tail is used instead) and that cluster's CTA count.  No counterpart
+ * in the reference (diagnostics). */
+int gb2d_solver_layout(gb2d_ctx* ctx, int precision, int* levels, int* cluster_top, int* cluster_ctas);
+
 /* Device-resident checkpoint of the step state (PHI with its ghosts, U, V, UA,
  * VA, P): save copies it to a second set of device buffers (allocated on the
  * first save), restore copies it back.  Asynchronous on the context stream. */

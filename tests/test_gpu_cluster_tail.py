@@ -1,0 +1,104 @@
+"""The coarse end of the V-cycle has two implementations: one thread-block cluster
+(levels split into row stripes across 8-16 CTAs, neighbour rows read from
+distributed shared memory) and one single CTA.  Both apply the same V-cycle
+(same smoother order, restriction and prolongation; only the dense coarse
+solve's summation order differs), so on the same system:
+
+  * the first PCG step (x1 = alpha0 z0, z0 = M r0) agrees to rounding,
+  * full solves take the same number of iterations (+-1) and agree to the
+    solve tolerance.
+
+GB2D_CLUSTER_TAIL=0 at context creation selects the single-CTA tail."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.golden.cases import bubbles_case
+
+pytestmark = pytest.mark.gpu
+
+# (ni, nj): square, rectangular both ways, small enough for the cluster to hold the finest level
+SHAPES = [(1024, 1024), (256, 256), (300, 140), (120, 330), (129, 129)]
+
+
+def case_for(ni, nj, seed):
+    # dx == dy: the reference's diagonal carries 1/dx^2 only, so dy < dx would make
+    # the assembled system indefinite
+    return bubbles_case(ni, nj, seed=seed, x_max=1.0, y_max=(nj - 1) / (ni - 1))
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def make(gb, case, cluster):
+    old = os.environ.get("GB2D_CLUSTER_TAIL")
+    os.environ["GB2D_CLUSTER_TAIL"] = "1" if cluster else "0"
+    try:
+        c = gb.Context(case["ni"], case["nj"], x_max=case["x_max"], y_max=case["y_max"])
+    finally:
+        if old is None:
+            del os.environ["GB2D_CLUSTER_TAIL"]
+        else:
+            os.environ["GB2D_CLUSTER_TAIL"] = old
+    for f, k in ((gb.FIELD_PHI, "phi"), (gb.FIELD_U, "u"), (gb.FIELD_V, "v"), (gb.FIELD_P, "p"), (gb.FIELD_UA, "ua"),
+                 (gb.FIELD_VA, "va")):
+        c.set(f, case[k])
+    return c
+
+
+def system(gb, c, dt):
+    bx, by, dg, rhs = c.poisson_assemble(dt)
+    return rhs
+
+
+@pytest.mark.parametrize("ni,nj", SHAPES)
+def test_cluster_layout(gb, ni, nj):
+    case = case_for(ni, nj, 5)
+    c = make(gb, case, True)
+    s = make(gb, case, False)
+    for prec in (gb.PRECISION_FP64, gb.PRECISION_MIXED):
+        lv, top, ctas = c.solver_layout(prec)
+        assert lv >= 2
+        assert s.solver_layout(prec)[1] == -1
+        if prec == gb.PRECISION_MIXED:
+            # FP32 levels up to 2^16 cells fit in the cluster's shared memory
+            assert top >= 0 and ctas in (8, 16), (lv, top, ctas)
+
+
+@pytest.mark.parametrize("ni,nj", SHAPES)
+@pytest.mark.parametrize("prec_name", ["FP64", "MIXED"])
+def test_first_step_matches_single_cta_tail(gb, ni, nj, prec_name):
+    prec = getattr(gb, "PRECISION_" + prec_name)
+    case = case_for(ni, nj, 5)
+    dt = 0.5 / (max(ni, nj) - 1)
+    out = {}
+    for cluster in (True, False):
+        c = make(gb, case, cluster)
+        rhs = system(gb, c, dt)
+        x, st = c.poisson_solve(rhs, opts=gb.solve_opts(precision=prec, tolerance=1e-14, max_iterations=1), allow_max_iters=True)
+        assert st.iterations == 1
+        out[cluster] = x
+        c.close()
+    tol = 1e-11 if prec_name == "FP64" else 2e-5
+    assert np.linalg.norm(out[True]) > 0
+    assert rel_l2(out[True], out[False]) <= tol
+
+
+@pytest.mark.parametrize("ni,nj", SHAPES)
+@pytest.mark.parametrize("prec_name", ["FP64", "MIXED"])
+def test_full_solve_matches_single_cta_tail(gb, ni, nj, prec_name):
+    prec = getattr(gb, "PRECISION_" + prec_name)
+    case = case_for(ni, nj, 6)
+    dt = 0.5 / (max(ni, nj) - 1)
+    out = {}
+    for cluster in (True, False):
+        c = make(gb, case, cluster)
+        rhs = system(gb, c, dt)
+        x, st = c.poisson_solve(rhs, opts=gb.solve_opts(precision=prec, tolerance=1e-9))
+        assert st.rel_residual <= 1e-9
+        out[cluster] = (x, st.iterations)
+        c.close()
+    assert abs(out[True][1] - out[False][1]) <= 1, (out[True][1], out[False][1])
+    assert rel_l2(out[True][0], out[False][0]) <= 1e-7
