@@ -336,7 +336,7 @@ __global__ void __launch_bounds__(kCtThreads, 1) k_ctail(CtArgs<T> a, const doub
       const int lr = u / L.nI + 1, i = u - (lr - 1) * L.nI;
       const size_t q = (size_t)lr * L.ld + i + 1;
       L.x[(size_t)(J0 + lr) * L.ld + i + 1] = v.x[q];
-      acc += (double)v.b[q] * (double)v.x[q];
+      if (a.sc) acc += (double)v.b[q] * (double)v.x[q];
     }
     if (a.sc) {
       acc = block_sum(acc);

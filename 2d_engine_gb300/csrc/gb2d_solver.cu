@@ -114,6 +114,7 @@ __global__ void k_build_level0(const double* __restrict__ bx, const double* __re
     double pin = (i == 0 && j == 0) ? (bl + bb) : 0.0;
     L.sh[k] = (T)(pin * idx2 + ybeta * (idx2 - idy2));
     if (b64) b64[k] = rhs[t];
+
   }
 }
 
@@ -341,13 +342,17 @@ __device__ __forceinline__ bool last_block_sum(double acc, double* part, unsigne
   return true;
 }
 
-// r.z of a preconditioned residual is known: record it and beta = rz_new / rz_cur.
+// z = M r is complete: record r.z and beta = rz_new / rz_cur (Fletcher-Reeves).
+// With the FP32 preconditioner, a flexible (Polak-Ribiere) beta and a deflation of
+// the pinned operator's near-null constant mode were tried: neither lowered the
+// iteration count, and both cost extra traffic per iteration.
 __device__ __forceinline__ void publish_rz(Scalars* sc, double rz) {
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     sc->rz_new = rz;
     sc->beta = rz / sc->rz_cur;
   }
 }
+
 
 // Pre-smoothing sweep (red, then black).  ZERO: x was zero (not read).  With
 // RESTRICT (halo 3), each thread's quad residual b - A x is averaged into the
@@ -393,8 +398,8 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_sweep(Level<T> L, Level<T> C, 
 // staging.  With part_rz (finest level, last sweep), r.z (b = r, x = z there) is
 // reduced and beta published.
 template <typename T, bool PROLONG>
-__global__ void __launch_bounds__(BXT* BYT) k_post_sweep(Level<T> L, Level<T> C, T* __restrict__ xout, double* __restrict__ part_rz, unsigned* __restrict__ counter,
-                                                        Scalars* sc, const int* __restrict__ done) {
+__global__ void __launch_bounds__(BXT* BYT) k_post_sweep(Level<T> L, Level<T> C, T* __restrict__ xout, double* __restrict__ part_rz,
+                                                        unsigned* __restrict__ counter, Scalars* sc, const int* __restrict__ done) {
   if (*done) return;
   constexpr int H = 2;
   using Wn = Win<T, H>;
@@ -419,7 +424,7 @@ __global__ void __launch_bounds__(BXT* BYT) k_post_sweep(Level<T> L, Level<T> C,
       if (gi >= L.nI || gj >= L.nJ) continue;
       const int s = (ti + H) + (tj + H) * W;
       xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
-      acc.add(bs[s] * xs[s]);
+      if (part_rz) acc.add(bs[s] * xs[s]);
     }
   if (part_rz) {
     double rz;
@@ -545,7 +550,7 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(TailArgs<T> a, const doub
     for (int u = threadIdx.x; u < L.nI * L.nJ; u += blockDim.x) {
       int k = (u % L.nI + 1) + (u / L.nI + 1) * L.ld;
       L.x[k] = t.x[k];
-      acc += (double)t.b[k] * (double)t.x[k];
+      if (a.sc) acc += (double)t.b[k] * (double)t.x[k];
     }
     if (a.sc) {
       acc = block_sum(acc);
@@ -557,19 +562,64 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(TailArgs<T> a, const doub
 #include "gb2d_ctail.cuh"
 
 // ---- CG kernels ------------------------------------------------------------------
+//
+// The CG itself is FP64 for both precisions: x, r, p and Ap are FP64 and A is
+// applied with the reference's matrix entries (standard 5-point form).  Only
+// the preconditioner's precision differs: an FP64 or an FP32 V-cycle (or Jacobi)
+// maps r to z.  An FP32 preconditioner is only an approximate inverse anyway;
+// keeping the Krylov recurrences in FP64 keeps the FP64 iteration count, where
+// refinement around an FP32 CG stalls at the FP32 operator's accuracy.
+// FP64 issue slots are scarce on this part (about 2 FP64 operations per clock
+// per SM), so each kernel does at most a handful per cell; FP32 <-> FP64 moves
+// are bit manipulations on the integer pipes.
 
-// FP64 residual of the refinement loop with the reference's matrix entries:
-// r64 = b - A x, its copy in the inner precision; partial ||r||^2 and ||b||^2.
+// Exact FP32 -> FP64 (every FP32 value is an FP64 value); FP32 subnormals, below
+// 1.2e-38, become signed zero.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  unsigned long long bits = (unsigned long long)(u >> 31) << 63;
+  if (e != 0u) {
+    const unsigned long long E = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
+    bits |= (E << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+  }
+  return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double widen(double d) { return d; }
+
+// FP64 -> FP32 by truncation of the significand (the preconditioner's input
+// only); magnitudes below the FP32 normal range become signed zero, above it
+// infinity.
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned s = (unsigned)(b >> 63) << 31;
+  const int E = (int)((b >> 52) & 0x7ffull);
+  const int e = E - 896;
+  unsigned bits;
+  if (E == 0x7ff)
+    bits = s | 0x7f800000u | (unsigned)((b >> 29) & 0x7fffffull) | ((b & 0xfffffffffffffull) ? 0x400000u : 0u);
+  else if (e <= 0)
+    bits = s;
+  else if (e >= 255)
+    bits = s | 0x7f800000u;
+  else
+    bits = s | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffull);
+  return __uint_as_float(bits);
+}
+
+// r = b - A x with the reference's matrix entries, in FP64; its copy for the
+// preconditioner (rT, FP32 or the FP64 r itself); partial ||r||^2 and ||b||^2.
 template <typename T>
-__global__ void k_residual64(Level<double> L, const double* __restrict__ x, const double* __restrict__ b, T* __restrict__ rT,
-                             double* __restrict__ part_rr, double* __restrict__ part_bb) {
+__global__ void k_residual64(Level<double> L, const double* __restrict__ x, const double* __restrict__ b, double* __restrict__ r64,
+                             T* __restrict__ rT, double* __restrict__ part_rr, double* __restrict__ part_bb) {
   double rr = 0.0, bb = 0.0;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
     int i, j;
     size_t k = cell_index(L, t, i, j);
     double ax = L.dg[k] * x[k] - L.cx[k] * x[k - 1] - L.cx[k + 1] * x[k + 1] - L.cy[k] * x[k - L.ld] - L.cy[k + L.ld] * x[k + L.ld];
     double r = b[k] - ax;
-    rT[k] = (T)r;
+    r64[k] = r;
+    if constexpr (sizeof(T) == 4) rT[k] = narrow(r);
     rr += r * r;
     bb += b[k] * b[k];
   }
@@ -590,82 +640,69 @@ __global__ void k_reduce_two(const double* __restrict__ pa, const double* __rest
   }
 }
 
-// Search direction and operator: p_new = z + beta p_old (p_new = z when first,
-// which also clears the correction e), Ap = A p_new in flux form; the last block
-// forms p.Ap and publishes alpha = rz_new / p.Ap and rz_cur = rz_new.  The
-// neighbours' p_new are formed on the fly from z and p_old.
-template <typename T>
-__global__ void k_direction_apply(Level<T> L, const T* __restrict__ z, const T* __restrict__ pold, T* __restrict__ pnew, T* __restrict__ ap,
-                                  T* __restrict__ e, T* __restrict__ elo, Scalars* sc, int first, double* __restrict__ part_pap,
-                                  unsigned* __restrict__ counter, const int* __restrict__ done) {
+// p = z + beta p (p = z when first).  z is the preconditioner's output in its
+// precision; one FP64 operation per cell.
+template <typename TZ>
+__global__ void k_direction(Level<double> L, const TZ* __restrict__ z, double* __restrict__ p, const Scalars* sc, int first,
+                            const int* __restrict__ done) {
   if (*done) return;
-  const T bt = first ? (T)0 : (T)sc->beta;
-  Acc<T> acc;
+  const double bt = first ? 0.0 : sc->beta;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
     int i, j;
     size_t k = cell_index(L, t, i, j);
-    T pc, pl, pr, pb, pt;
-    if (first) {
-      pc = z[k], pl = z[k - 1], pr = z[k + 1], pb = z[k - L.ld], pt = z[k + L.ld];
-      e[k] = (T)0;
-      if (elo) elo[k] = (T)0;
-    } else {
-      pc = z[k] + bt * pold[k];
-      pl = z[k - 1] + bt * pold[k - 1];
-      pr = z[k + 1] + bt * pold[k + 1];
-      pb = z[k - L.ld] + bt * pold[k - L.ld];
-      pt = z[k + L.ld] + bt * pold[k + L.ld];
-    }
-    T y = L.sh[k] * pc + L.cx[k] * (pc - pl) + L.cx[k + 1] * (pc - pr) + L.cy[k] * (pc - pb) + L.cy[k + L.ld] * (pc - pt);
-    pnew[k] = pc;
+    p[k] = first ? widen(z[k]) : widen(z[k]) + bt * p[k];
+  }
+}
+
+// Ap = A p (reference entries) and p.Ap; the last block publishes
+// alpha = rz_new / p.Ap and rz_cur = rz_new.
+__global__ void k_apply_pap(Level<double> L, const double* __restrict__ p, double* __restrict__ ap, Scalars* sc, double* __restrict__ part,
+                            unsigned* __restrict__ counter, const int* __restrict__ done) {
+  if (*done) return;
+  double acc = 0.0;
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
+    int i, j;
+    size_t k = cell_index(L, t, i, j);
+    const double pc = p[k];
+    double y = L.dg[k] * pc - L.cx[k] * p[k - 1] - L.cx[k + 1] * p[k + 1] - L.cy[k] * p[k - L.ld] - L.cy[k + L.ld] * p[k + L.ld];
     ap[k] = y;
-    acc.add(pc * y);
+    acc += pc * y;
   }
   double pap;
-  if (last_block_sum(acc.value(), part_pap, gridDim.x, counter, &pap) && threadIdx.x == 0) {
+  if (last_block_sum(acc, part, gridDim.x, counter, &pap) && threadIdx.x == 0) {
     double rz = sc->rz_new;
     sc->rz_cur = rz;
     sc->alpha = rz / pap;
   }
 }
 
-// e += alpha p;  r -= alpha Ap;  ||r||^2.  The last block stores ||r||^2 for the
-// host and raises the done flag at the threshold (or on a non-finite value).
-// With elo (FP32 vectors), e is kept as the unevaluated sum e + elo (Knuth's
-// TwoSum per update): a plain FP32 correction would carry a rounding error of
-// 2^-24 |e| whose high-frequency residual A de stalls the refinement near 1e-8.
-__device__ __forceinline__ void two_sum_into(float& hi, float& lo, float v) {
-  float s = __fadd_rn(hi, v);
-  float bv = __fsub_rn(s, hi);
-  float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(v, bv));
-  hi = s;
-  lo = __fadd_rn(lo, err);
-}
-
+// x += alpha p;  r -= alpha Ap;  the preconditioner's copy of r (FP32: rT; FP64:
+// r is read in place);  ||r||^2 (from the FP32 copy when there is one).  The
+// last block stores ||r||^2 for the host and raises the done flag at the
+// threshold (or on a non-finite value).
 template <typename T>
-__global__ void k_cg_update(Level<T> L, T* __restrict__ e, T* __restrict__ elo, T* __restrict__ r, const T* __restrict__ p,
-                            const T* __restrict__ ap, Scalars* sc, double* __restrict__ part_rr, unsigned* __restrict__ counter,
-                            int* __restrict__ done, double* __restrict__ host_rr) {
+__global__ void k_update(Level<double> L, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                         const double* __restrict__ ap, T* __restrict__ rT, Scalars* sc, double* __restrict__ part,
+                         unsigned* __restrict__ counter, int* __restrict__ done, double* __restrict__ host_rr) {
   if (*done) return;
-  const T at = (T)sc->alpha;
+  const double al = sc->alpha;
   Acc<T> acc;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
     int i, j;
     size_t k = cell_index(L, t, i, j);
-    if constexpr (sizeof(T) == 4) {
-      float hi = e[k], lo = elo[k];
-      two_sum_into(hi, lo, __fmul_rn(at, p[k]));
-      e[k] = hi;
-      elo[k] = lo;
-    } else {
-      e[k] += at * p[k];
-    }
-    T rn = r[k] - at * ap[k];
+    x[k] += al * p[k];
+    const double rn = r[k] - al * ap[k];
     r[k] = rn;
-    acc.add(rn * rn);
+    if constexpr (sizeof(T) == 4) {
+      const float rf = narrow(rn);
+      rT[k] = rf;
+      acc.add(rf * rf);
+    } else {
+      acc.add(rn * rn);
+    }
   }
   double rr;
-  if (last_block_sum(acc.value(), part_rr, gridDim.x, counter, &rr) && threadIdx.x == 0) {
+  if (last_block_sum(acc.value(), part, gridDim.x, counter, &rr) && threadIdx.x == 0) {
     sc->rr = rr;
     if (!(rr > sc->thr2)) {
       *done = 1;
@@ -692,18 +729,6 @@ __global__ void k_jacobi(Level<T> L, const T* __restrict__ r, T* __restrict__ z,
   if (last_block_sum(acc.value(), part_rz, gridDim.x, counter, &rz)) publish_rz(sc, rz);
 }
 
-// x (FP64) += e (+ elo): the inner solve's correction joins the FP64 solution.
-template <typename T>
-__global__ void k_add_correction(Level<T> L, double* __restrict__ x, const T* __restrict__ e, const T* __restrict__ elo) {
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
-    int i, j;
-    size_t k = cell_index(L, t, i, j);
-    double d = (double)e[k];
-    if (elo) d += (double)elo[k];
-    x[k] += d;
-  }
-}
-
 __global__ void k_begin_inner(Scalars* sc, int* done, double thr2) {
   *done = 0;
   sc->thr2 = thr2;
@@ -723,9 +748,7 @@ struct Hierarchy {
   size_t ct_smem = 0;
   CtArgs<T> ct;
   Level<T> L[kMaxLevels];
-  T *p[2] = {nullptr, nullptr}, *ap = nullptr, *r = nullptr;  // CG vectors (padded fine layout); z = L[0].x
-  T* e = nullptr;    // correction accumulated by the inner solve
-  T* elo = nullptr;  // its low part (FP32 hierarchy only)
+  T* r = nullptr;  // the preconditioner's input (padded fine layout, = L[0].b); z = L[0].x
 };
 
 struct GraphSet {
@@ -741,7 +764,8 @@ struct Solver {
   double* ainv64 = nullptr;
   double* ainv32 = nullptr;
   double* b64 = nullptr;   // right-hand side, padded
-  double* part = nullptr;  // 4 slots x nparts_cap: p.Ap, r.r, r.z, b.b
+  double *p = nullptr, *ap = nullptr;  // FP64 CG direction and A p (padded); r = h64.r
+  double* part = nullptr;  // kSlots x nparts_cap block partials (see slot())
   int nparts_cap = 0;
   unsigned* counter = nullptr;  // 4 last-block counters: p.Ap, r.r, r.z (jacobi), r.z (sweep)
   double* host = nullptr;  // pinned: [0..1] per-parity r.r, [4..5] residual / rhs norms
@@ -753,6 +777,10 @@ struct Solver {
   GraphSet graphs[2][2][3];
   double* graph_x[2][2][3] = {};
 };
+
+// Block-partial slots (nparts_cap doubles each).
+constexpr int kSlotPap = 0, kSlotRr = 1, kSlotRz = 2, kSlotBb = 3, kSlots = 4;
+inline double* slot(Solver* S, int k) { return S->part + (size_t)k * S->nparts_cap; }
 
 namespace {
 
@@ -783,12 +811,10 @@ void free_level(Level<T>& L, bool own_b) {
 template <typename T>
 cudaError_t alloc_hierarchy(Hierarchy<T>& H, int ni, int nj) {
   size_t n = (size_t)(ni + 2) * (nj + 2);
-  T** v[6] = {&H.p[0], &H.p[1], &H.ap, &H.r, &H.e, &H.elo};
-  for (auto a : v) {
-    if (a == &H.elo && sizeof(T) != 4) continue;
-    cudaError_t e = cudaMalloc(a, n * sizeof(T));
+  {
+    cudaError_t e = cudaMalloc(&H.r, n * sizeof(T));
     if (e != cudaSuccess) return e;
-    e = cudaMemset(*a, 0, n * sizeof(T));
+    e = cudaMemset(H.r, 0, n * sizeof(T));
     if (e != cudaSuccess) return e;
   }
   int nI = ni, nJ = nj;
@@ -961,9 +987,7 @@ void launch_ctail(cudaStream_t s, const Hierarchy<T>& H, const double* ainv, int
 template <typename T>
 void free_hierarchy(Hierarchy<T>& H) {
   for (int l = 0; l < H.nlev; ++l) free_level(H.L[l], l > 0);
-  T* v[6] = {H.p[0], H.p[1], H.ap, H.r, H.e, H.elo};
-  for (auto a : v)
-    if (a) cudaFree(a);
+  if (H.r) cudaFree(H.r);
 }
 
 inline unsigned nblocks(size_t n, unsigned cap) {
@@ -1025,7 +1049,7 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
   const bool cluster = H.ctail >= 0;
   const int tail = cluster ? H.ctail : H.tail;
   const int* done = S->done;
-  double* P_rz = S->part + 2 * (size_t)S->nparts_cap;
+  double* P_rz = slot(S, kSlotRz);
   const dim3 blk(BXT, BYT);
   // Sweep k of a level's 2*nu writes L.xa or L.x so that the last one writes L.x
   // (the buffer the next finer level prolongs from, and z on the finest level).
@@ -1089,39 +1113,39 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
   }
 }
 
-// Preconditioner + first direction: z = M r, p[0] = z, Ap, alpha.
+// z = M r with the preconditioner hierarchy H (FP64 or FP32): V-cycle or Jacobi.
 template <typename T>
-void enqueue_init(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int use_mg, int nu, Probe* pr) {
-  Level<T>& L = H.L[0];
-  double* P_pap = S->part;
-  double* P_rz = S->part + 2 * (size_t)S->nparts_cap;
+void precondition(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int use_mg, int nu, Probe* pr) {
   if (use_mg) {
     vcycle<T>(s, S, H, ainv, nu, pr);
   } else {
-    k_jacobi<T><<<S->G, kThreads, 0, s>>>(L, H.r, L.x, S->sc, P_rz, S->counter + 2, S->done);
+    k_jacobi<T><<<S->G, kThreads, 0, s>>>(H.L[0], H.r, H.L[0].x, S->sc, slot(S, kSlotRz), S->counter + 2, S->done);
     GB_LAUNCHED(1);
   }
-  k_direction_apply<T><<<S->G, kThreads, 0, s>>>(L, L.x, H.p[1], H.p[0], H.ap, H.e, H.elo, S->sc, 1, P_pap, S->counter, S->done);
-  GB_LAUNCHED(1);
 }
 
-// One CG iteration with direction p[par]: update x and r, precondition, next direction p[par^1].
+// First direction: z = M r, p = z, Ap, alpha.
+template <typename T>
+void enqueue_init(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int use_mg, int nu, Probe* pr) {
+  const Level<double>& L = S->h64.L[0];
+  precondition<T>(s, S, H, ainv, use_mg, nu, pr);
+  k_direction<T><<<S->G, kThreads, 0, s>>>(L, H.L[0].x, S->p, S->sc, 1, S->done);
+  k_apply_pap<<<S->G, kThreads, 0, s>>>(L, S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter, S->done);
+  GB_LAUNCHED(2);
+}
+
+// One CG iteration: x += alpha p, r -= alpha Ap (||r||^2 to host slot par),
+// z = M r, p = z + beta p, Ap, alpha.
 template <typename T>
 void enqueue_iter(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, double* x64, int use_mg, int nu, int par, Probe* pr) {
-  Level<T>& L = H.L[0];
-  double* P_pap = S->part;
-  double* P_rr = S->part + (size_t)S->nparts_cap;
-  double* P_rz = S->part + 2 * (size_t)S->nparts_cap;
-  k_cg_update<T><<<S->G, kThreads, 0, s>>>(L, H.e, H.elo, H.r, H.p[par], H.ap, S->sc, P_rr, S->counter + 1, S->done, S->host + par);
+  const Level<double>& L = S->h64.L[0];
+  T* rT = sizeof(T) == 4 ? H.r : nullptr;
+  k_update<T><<<S->G, kThreads, 0, s>>>(L, x64, S->h64.r, S->p, S->ap, rT, S->sc, slot(S, kSlotRr), S->counter + 1, S->done, S->host + par);
   GB_LAUNCHED(1);
-  if (use_mg) {
-    vcycle<T>(s, S, H, ainv, nu, pr);
-  } else {
-    k_jacobi<T><<<S->G, kThreads, 0, s>>>(L, H.r, L.x, S->sc, P_rz, S->counter + 2, S->done);
-    GB_LAUNCHED(1);
-  }
-  k_direction_apply<T><<<S->G, kThreads, 0, s>>>(L, L.x, H.p[par], H.p[par ^ 1], H.ap, H.e, H.elo, S->sc, 0, P_pap, S->counter, S->done);
-  GB_LAUNCHED(1);
+  precondition<T>(s, S, H, ainv, use_mg, nu, pr);
+  k_direction<T><<<S->G, kThreads, 0, s>>>(L, H.L[0].x, S->p, S->sc, 0, S->done);
+  k_apply_pap<<<S->G, kThreads, 0, s>>>(L, S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter, S->done);
+  GB_LAUNCHED(2);
 }
 
 // Capture fn's launches on the context's own stream into an executable graph.
@@ -1169,10 +1193,11 @@ GraphSet* graphs_for(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv
   return ok ? &gs : nullptr;
 }
 
-// Preconditioned CG on A e = r (r in H.r, the fine level's b), accumulating e into
-// the FP64 x.  Stops when ||r||^2 <= thr2 or after max_it iterations; returns the
-// iterations done and the last ||r||^2.  The host checks iteration k-1's residual
-// while iteration k is queued; work queued after convergence returns at entry.
+// FP64 preconditioned CG from x64 with r = b - A x64 in h64.r (and its FP32 copy
+// in H.r for an FP32 preconditioner), preconditioned by hierarchy H.  Stops when
+// ||r||^2 <= thr2 or after max_it iterations; returns the iterations done and the
+// last ||r||^2.  The host checks iteration k-1's residual while iteration k is
+// queued; work queued after convergence returns at entry.
 template <typename T>
 int inner_pcg(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, double* x64, double thr2, int max_it, int prec, int use_mg, int nu,
               double* last_rr) {
@@ -1208,8 +1233,6 @@ int inner_pcg(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, doubl
     }
     k++;
   }
-  k_add_correction<T><<<S->G, kThreads, 0, s>>>(H.L[0], x64, H.e, H.elo);
-  GB_LAUNCHED(1);
   cudaStreamSynchronize(s);
   if (iters < 0) {
     iters = k;
@@ -1238,10 +1261,12 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
   }
   if (e == cudaSuccess) e = cudaMalloc(&S->ainv64, sizeof(double) * kCoarseMax * kCoarseMax);
   if (e == cudaSuccess) e = cudaMalloc(&S->ainv32, sizeof(double) * kCoarseMax * kCoarseMax);
-  if (e == cudaSuccess) e = cudaMalloc(&S->b64, np * sizeof(double));
-  if (e == cudaSuccess) e = cudaMemset(S->b64, 0, np * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&S->part, sizeof(double) * 4 * (size_t)S->nparts_cap);
-  if (e == cudaSuccess) e = cudaMemset(S->part, 0, sizeof(double) * 4 * (size_t)S->nparts_cap);
+  for (double** v : {&S->b64, &S->p, &S->ap}) {
+    if (e == cudaSuccess) e = cudaMalloc(v, np * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(*v, 0, np * sizeof(double));
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&S->part, sizeof(double) * kSlots * (size_t)S->nparts_cap);
+  if (e == cudaSuccess) e = cudaMemset(S->part, 0, sizeof(double) * kSlots * (size_t)S->nparts_cap);
   if (e == cudaSuccess) e = cudaMalloc(&S->counter, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMemset(S->counter, 0, 4 * sizeof(unsigned));
   if (e == cudaSuccess) e = cudaMalloc(&S->done, sizeof(int));
@@ -1286,7 +1311,7 @@ void solver_destroy(Solver* S) {
       }
   free_hierarchy(S->h64);
   free_hierarchy(S->h32);
-  double* d[] = {S->ainv64, S->ainv32, S->b64, S->part};
+  double* d[] = {S->ainv64, S->ainv32, S->b64, S->p, S->ap, S->part};
   for (auto p : d)
     if (p) cudaFree(p);
   if (S->counter) cudaFree(S->counter);
@@ -1311,6 +1336,10 @@ void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, in
 }
 
 // x: padded FP64 solution (warm start in, result out); the system is ctx->bx/by/diag/rhs.
+// FP64 CG throughout; the preconditioner runs in FP64 or, for
+// GB2D_PRECISION_MIXED, in FP32.  The loop around the CG recomputes the true
+// residual with the reference's entries and restarts only if the recursive
+// residual has drifted above the tolerance.
 int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
   Solver* S = c->solver;
   cudaStream_t s = c->stream;
@@ -1318,11 +1347,10 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
   int use_mg = o->solver == GB2D_SOLVER_MGPCG;
   int prec = o->precision == GB2D_PRECISION_MIXED ? 1 : 0;
   double tol = o->tolerance > 0 ? o->tolerance : 1e-8;
-  double tin = o->inner_tolerance > 0 ? o->inner_tolerance : 1e-4;
   int max_it = o->max_iterations > 0 ? o->max_iterations : 10000;
   unsigned G = (unsigned)S->G;
-  double* P_rr = S->part + (size_t)S->nparts_cap;
-  double* P_bb = S->part + 3 * (size_t)S->nparts_cap;
+  double* P_rr = slot(S, kSlotRr);
+  double* P_bb = slot(S, kSlotBb);
 
   if (prec || !use_mg)
     build_level0_f64(s, S->h64, c, S->b64);
@@ -1339,11 +1367,10 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
   double rr = 0, bb = 0;
   int status = GB2D_OK;
   while (true) {
-    // FP64 residual with the reference's entries, copied into the inner precision.
     if (prec)
-      k_residual64<float><<<G, kThreads, 0, s>>>(S->h64.L[0], x, S->b64, S->h32.r, P_rr, P_bb);
+      k_residual64<float><<<G, kThreads, 0, s>>>(S->h64.L[0], x, S->b64, S->h64.r, S->h32.r, P_rr, P_bb);
     else
-      k_residual64<double><<<G, kThreads, 0, s>>>(S->h64.L[0], x, S->b64, S->h64.r, P_rr, P_bb);
+      k_residual64<double><<<G, kThreads, 0, s>>>(S->h64.L[0], x, S->b64, S->h64.r, nullptr, P_rr, P_bb);
     GB_LAUNCHED(1);
     k_reduce_two<<<1, kThreads, 0, s>>>(P_rr, P_bb, G, S->host + 4);
     GB_LAUNCHED(1);
@@ -1361,18 +1388,16 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
     }
     double thr2 = tol * tol * bb;
     if (rr <= thr2 || bb == 0.0) break;
-    if (total >= max_it) {
+    if (total >= max_it || outer >= 64) {
       status = GB2D_ERR_MAX_ITERS;
       break;
     }
     double rr_in = rr;
     int it;
-    if (prec) {
-      double thr_in = tin * tin * rr;
-      it = inner_pcg<float>(c, S, S->h32, S->ainv32, x, thr_in > thr2 ? thr_in : thr2, max_it - total, prec, use_mg, nu, &rr_in);
-    } else {
+    if (prec)
+      it = inner_pcg<float>(c, S, S->h32, S->ainv32, x, thr2, max_it - total, prec, use_mg, nu, &rr_in);
+    else
       it = inner_pcg<double>(c, S, S->h64, S->ainv64, x, thr2, max_it - total, prec, use_mg, nu, &rr_in);
-    }
     e = cudaGetLastError();
     if (e != cudaSuccess) {
       snprintf(c->err, sizeof(c->err), "pressure solve: %s", cudaGetErrorString(e));
@@ -1383,10 +1408,6 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
     if (!std::isfinite(rr_in)) {
       snprintf(c->err, sizeof(c->err), "pressure solve: non-finite inner residual");
       status = GB2D_ERR_NONFINITE;
-      break;
-    }
-    if (outer > 64) {
-      status = GB2D_ERR_MAX_ITERS;
       break;
     }
   }

@@ -4,8 +4,9 @@ Workload (one "step" = one PROJECTION_2D::Solve): 1024 x 1024 pressure nodes on
 [0,1]^2, level set = signed distance to 8 seeded circles (rho 1 inside, 1000
 outside, sigma = 0.0728), MAC velocity U[-1,1] smoothed by 4 Jacobi passes,
 dt = 0.5 dx, zero initial pressure; solve to ||b - A p|| / ||b|| <= 1e-8.
-The timed path is the mixed-precision MG-PCG (FP64 refinement around FP32 CG +
-FP32 V-cycles); the plain FP64 MG-PCG path is timed beside it.
+The timed path is the mixed-precision MG-PCG (FP64 CG with the reference's matrix
+entries, preconditioned by FP32 multigrid V-cycles); the all-FP64 MG-PCG path is
+timed beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -310,9 +311,9 @@ def run_gb300(args):
     res = {
         "metric": METRIC, "value": value, "unit": "ms", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 inner / f64 refinement", "data": "synthetic",
+        "dtype": "f64 CG / f32 preconditioner", "data": "synthetic",
         "config": {"workload": WORKLOAD, "grid": f"{N}x{N}", "tolerance": TOL, "seed": SEED, "l2": "flushed (256 MB write) before every step",
-                   "solver": "FP64 iterative refinement around FP32 CG + FP32 V-cycles (2+2 red-black GS)",
+                   "solver": "FP64 CG (reference matrix entries) preconditioned by FP32 V-cycles (2+2 red-black GS)",
                    "iterations_mixed": statistics.mean(it_m), "outer_iterations_mixed": st_m.outer_iterations,
                    "rel_residual_mixed": st_m.rel_residual,
                    "fp64_mgpcg_ms": statistics.mean(ms_64), "iterations_fp64": statistics.mean(it_64), "rel_residual_fp64": st_64.rel_residual,

@@ -47,7 +47,7 @@ extern "C" {
 #define GB2D_FIELD_KAPPA 6 /* curvature, no ghost */
 
 #define GB2D_PRECISION_FP64 0  /* FP64 everywhere: reproduces the reference's FP64 results */
-#define GB2D_PRECISION_MIXED 1 /* FP32 inner work inside FP64 refinement (see gb2d_solve_opts) */
+#define GB2D_PRECISION_MIXED 1 /* FP32 where it only affects speed, FP64 where it sets the result (see gb2d_solve_opts) */
 
 #define GB2D_SOLVER_MGPCG 0       /* multigrid-preconditioned CG */
 #define GB2D_SOLVER_PCG_JACOBI 1  /* diagonal-preconditioned CG (simple FP64 parity solver) */
@@ -76,16 +76,17 @@ typedef struct {
  * poisson_solver_type, PROJECTION_2D.h:132-160). */
 typedef struct {
   int solver;           /* GB2D_SOLVER_* */
-  int precision;        /* GB2D_PRECISION_*: MIXED = FP64 refinement around FP32 CG + FP32 V-cycles */
+  int precision;        /* GB2D_PRECISION_*: the CG (x, r, p, A p) is FP64 either way; MIXED runs the
+                           preconditioner (V-cycle or Jacobi) in FP32 */
   double tolerance;     /* stop at ||b - A p||_2 / ||b||_2 <= tolerance */
-  int max_iterations;   /* cap on Krylov iterations (all refinement steps together) */
+  int max_iterations;   /* cap on Krylov iterations (all restarts together) */
   int mg_smooth;        /* red-black Gauss-Seidel sweeps before and after each coarse correction (0 = 2) */
-  double inner_tolerance; /* MIXED: relative reduction of each FP32 inner solve (0 = 1e-4) */
+  double inner_tolerance; /* reserved (no inner solve in the current scheme); ignored */
 } gb2d_solve_opts;
 
 typedef struct {
   int iterations;        /* Krylov iterations done */
-  int outer_iterations;  /* FP64 refinement steps (1 for FP64) */
+  int outer_iterations;  /* CG starts: 1, or more if the true residual had drifted above the tolerance */
   double rel_residual;   /* final FP64 ||b - A p|| / ||b|| */
   double max_velocity_x; /* max |u| after the update (PROJECTION_2D::max_velocity_x) */
   double max_velocity_y;

@@ -5,8 +5,8 @@ distributed shared memory) and one single CTA.  Both apply the same V-cycle
 solve's summation order differs), so on the same system:
 
   * the first PCG step (x1 = alpha0 z0, z0 = M r0) agrees to rounding,
-  * full solves take the same number of iterations (+-1) and agree to the
-    solve tolerance.
+  * full solves take the same number of iterations (+-1 in FP64, +-2 with the
+    FP32 preconditioner) and agree to the solve tolerance.
 
 GB2D_CLUSTER_TAIL=0 at context creation selects the single-CTA tail."""
 import os
@@ -93,12 +93,17 @@ def test_full_solve_matches_single_cta_tail(gb, ni, nj, prec_name):
     case = case_for(ni, nj, 6)
     dt = 0.5 / (max(ni, nj) - 1)
     out = {}
+    # The FP32 preconditioner reaches the FP64 iteration count to about 1e-8; below
+    # that its rounding slows CG's final superlinear phase, and the iteration count
+    # becomes sensitive to rounding differences (such as the dense coarse solve's
+    # summation order), so the mixed path is compared at 1e-8.
+    tol = 1e-9 if prec_name == "FP64" else 1e-8
     for cluster in (True, False):
         c = make(gb, case, cluster)
         rhs = system(gb, c, dt)
-        x, st = c.poisson_solve(rhs, opts=gb.solve_opts(precision=prec, tolerance=1e-9))
-        assert st.rel_residual <= 1e-9
+        x, st = c.poisson_solve(rhs, opts=gb.solve_opts(precision=prec, tolerance=tol))
+        assert st.rel_residual <= tol
         out[cluster] = (x, st.iterations)
         c.close()
-    assert abs(out[True][1] - out[False][1]) <= 1, (out[True][1], out[False][1])
-    assert rel_l2(out[True][0], out[False][0]) <= 1e-7
+    assert abs(out[True][1] - out[False][1]) <= (1 if prec_name == "FP64" else 2), (out[True][1], out[False][1])
+    assert rel_l2(out[True][0], out[False][0]) <= 100 * tol
