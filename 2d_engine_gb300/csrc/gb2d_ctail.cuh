@@ -50,10 +50,23 @@ struct CtArgs {
   int ndist;  // levels [0, ndist) are distributed, the rest local
   int res_off;   // residual of the bottom distributed level (elements of T)
   int ainv_off;  // dense inverse of the coarsest level (elements of T)
+  int bc_off;    // the coarsest level's right-hand side in cell order (elements of T)
   CtLevel<T> L[kCtMaxLevels];
   short J0[kCtMaxLevels][kClusterMax + 1];  // CTA c owns rows [J0[l][c], J0[l][c+1])
   Scalars* sc;  // set when the top level is the finest: publish r.z and beta
 };
+
+// Asynchronous global -> shared copy of one element (no register staging: every
+// copy of the staging loop is in flight at once).
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 template <typename T>
 struct CtView {
@@ -76,17 +89,21 @@ __device__ __forceinline__ void ct_half(const CtView<T>& v, int nI, int ld, int 
   const int tpr = 1 << lg, groups = kCtThreads >> lg;
   const int g = threadIdx.x >> lg, s = threadIdx.x & (tpr - 1);
   const int hw = (nI + 1) >> 1;
-  for (int lr = 1 + g; lr <= rows; lr += groups) {
-    const T* xm = lr == 1 ? xdn : v.x + (size_t)(lr - 1) * ld;
-    const T* xp = lr == rows ? xup : v.x + (size_t)(lr + 1) * ld;
+  auto row = [&](int lr, const T* xm, const T* xp) {
     const int par = (color + J0 + lr - 1) & 1;  // colour of cell (i, J) is (i + J) & 1
-    const size_t rb = (size_t)lr * ld;
+    const int rb = lr * ld;
     for (int m = s; m < hw; m += tpr) {
       const int k = 2 * m + par + 1;
       if (k > nI) continue;
-      const size_t q = rb + k;
+      const int q = rb + k;
       v.x[q] = (v.b[q] + v.cx[q] * v.x[q - 1] + v.cx[q + 1] * v.x[q + 1] + v.cy[q] * xm[k] + v.cy[q + ld] * xp[k]) * v.idg[q];
     }
+  };
+  for (int lr = 1 + g; lr <= rows; lr += groups) {
+    if (lr == 1 || lr == rows)  // a neighbour's row (distributed shared memory) or the wall
+      row(lr, lr == 1 ? xdn : v.x + (lr - 1) * ld, lr == rows ? xup : v.x + (lr + 1) * ld);
+    else  // both rows in this CTA's shared memory
+      row(lr, v.x + (lr - 1) * ld, v.x + (lr + 1) * ld);
   }
 }
 
@@ -102,6 +119,8 @@ __device__ __forceinline__ T ct_residual(const CtView<T>& v, int ld, int lr, int
 
 // Restriction between two levels whose rows [fJ0, fJ0+frows) and [cJ0, cJ0+crows)
 // are held by this CTA, with fJ0 = 2 cJ0: coarse b = average of the fine residuals.
+// The pre-smoothing ends with a black half sweep, after which the residual of
+// every black cell is zero: only the red cell of each fine row is evaluated.
 template <typename T>
 __device__ __forceinline__ void ct_restrict(const CtView<T>& f, const CtLevel<T>& F, int fJ0, int frows, const T* xdn, const T* xup,
                                             const CtView<T>& c, const CtLevel<T>& C, int cJ0, int crows) {
@@ -114,14 +133,9 @@ __device__ __forceinline__ void ct_restrict(const CtView<T>& f, const CtLevel<T>
 #pragma unroll
       for (int bb = 0; bb < 2; ++bb) {
         const int J = 2 * Jc + bb;
-        if (J >= F.nJ) continue;
-        const int lr = J - fJ0 + 1;
-#pragma unroll
-        for (int a = 0; a < 2; ++a) {
-          const int i = 2 * I + a;
-          if (i >= F.nI) continue;
-          acc += ct_residual(f, F.ld, lr, frows, i + 1, xdn, xup);
-        }
+        const int i = 2 * I + (J & 1);  // the red cell of this fine row within the coarse cell
+        if (J >= F.nJ || i >= F.nI) continue;
+        acc += ct_residual(f, F.ld, J - fJ0 + 1, frows, i + 1, xdn, xup);
       }
       c.b[(size_t)lrc * C.ld + I + 1] = (T)0.25 * acc;
     }
@@ -162,26 +176,29 @@ __global__ void __launch_bounds__(kCtThreads, 1) k_ctail(CtArgs<T> a, const doub
     const int J0 = dist ? a.J0[l][c] : 0;
     const int rows = dist ? a.J0[l][c + 1] - J0 : L.nJ;
     const int n = (L.rows_cap + 2) * L.ld;
+    // Local row lr is padded global row J0 + lr, so local element u is global
+    // element u + J0 ld: the stripe is one contiguous range of each array.
+    const T *gcx = L.cx + (size_t)J0 * L.ld, *gcy = L.cy + (size_t)J0 * L.ld, *gid = L.idg + (size_t)J0 * L.ld,
+            *gdg = L.dg + (size_t)J0 * L.ld, *gb = L.b + (size_t)J0 * L.ld;
+    const int own_lo = L.ld, own_hi = (rows + 1) * L.ld;                              // local rows 1..rows
+    const int cy_hi = (rows + 2 < L.nJ + 2 - J0 ? rows + 2 : L.nJ + 2 - J0) * L.ld;  // + the face above the stripe
     for (int u = threadIdx.x; u < n; u += kCtThreads) {
-      const int lr = u / L.ld, col = u - lr * L.ld;
-      const int gr = J0 + lr;  // padded global row of local row lr
-      T cx = 0, cy = 0, id = 0, dg = 0, b = 0;
-      if (lr <= rows + 1 && gr <= L.nJ + 1) {
-        const size_t k = (size_t)col + (size_t)gr * L.ld;
-        if (lr >= 1 && lr <= rows) {
-          cx = L.cx[k];
-          id = L.idg[k];
-          dg = L.dg[k];
-          if (l == 0) b = L.b[k];
-        }
-        if (lr >= 1) cy = L.cy[k];  // row rows+1 carries the face above the stripe
-      }
       v.x[u] = (T)0;
-      v.b[u] = b;
-      v.cx[u] = cx;
-      v.cy[u] = cy;
-      v.idg[u] = id;
-      v.dg[u] = dg;
+      if (u >= own_lo && u < own_hi) {
+        cp_async_elem(v.cx + u, gcx + u);
+        cp_async_elem(v.idg + u, gid + u);
+        cp_async_elem(v.dg + u, gdg + u);
+        if (l == 0)
+          cp_async_elem(v.b + u, gb + u);
+        else
+          v.b[u] = (T)0;
+      } else {
+        v.cx[u] = v.idg[u] = v.dg[u] = v.b[u] = (T)0;
+      }
+      if (u >= own_lo && u < cy_hi)
+        cp_async_elem(v.cy + u, gcy + u);
+      else
+        v.cy[u] = (T)0;
     }
   }
   {
@@ -198,6 +215,7 @@ __global__ void __launch_bounds__(kCtThreads, 1) k_ctail(CtArgs<T> a, const doub
       }
     }
   }
+  cp_async_wait_all();
   cl.sync();  // every CTA's shared memory is initialised before any remote read
 
   // Neighbour rows of a distributed level: the last row of CTA c-1 and the first
@@ -236,7 +254,8 @@ __global__ void __launch_bounds__(kCtThreads, 1) k_ctail(CtArgs<T> a, const doub
       const int lg = L.full_log2, tpr = 1 << lg, groups = kCtThreads >> lg;
       const int g = threadIdx.x >> lg, sl = threadIdx.x & (tpr - 1);
       for (int lr = 1 + g; lr <= rows; lr += groups)
-        for (int i = sl; i < L.nI; i += tpr) res[(size_t)lr * L.ld + i + 1] = ct_residual(v, L.ld, lr, rows, i + 1, xdn, xup);
+        for (int i = sl; i < L.nI; i += tpr)  // black residuals are zero after the black half sweep
+          res[(size_t)lr * L.ld + i + 1] = ((i + J0 + lr - 1) & 1) ? (T)0 : ct_residual(v, L.ld, lr, rows, i + 1, xdn, xup);
       cl.sync();
       const CtLevel<T>& C = a.L[l + 1];
       const CtView<T> cv = ct_view(sm, C);
@@ -276,18 +295,31 @@ __global__ void __launch_bounds__(kCtThreads, 1) k_ctail(CtArgs<T> a, const doub
     __syncthreads();
   }
   {
-    // Dense coarse solve: 16 threads per row, 4 terms each, fixed-order tree sum.
+    // Dense coarse solve: b gathered into cell order (bc), then 16 threads per
+    // row, 4 terms each, fixed-order tree sum.  (Not the residual buffer: other
+    // CTAs may still be reading it.)
     const CtLevel<T>& C = a.L[nl - 1];
     const CtView<T> v = ct_view(sm, C);
     const int n = C.nI * C.nJ;
     const T* ai = sm + a.ainv_off;
+    T* bc = sm + a.bc_off;
     const int r = threadIdx.x >> 4, part = threadIdx.x & 15;
+    int cr = 0, cc = 0;  // cell of row r
+    if (r < n) {
+      cr = r / C.nI;
+      cc = r - cr * C.nI;
+    }
+    if (threadIdx.x < (unsigned)n) {
+      const int jj = threadIdx.x / C.nI, ii = threadIdx.x - jj * C.nI;
+      bc[threadIdx.x] = v.b[(size_t)(jj + 1) * C.ld + ii + 1];
+    }
+    __syncthreads();
     T acc = 0;
     if (r < n)
-      for (int m = part; m < n; m += 16) acc += ai[(size_t)r * n + m] * v.b[(size_t)(m / C.nI + 1) * C.ld + m % C.nI + 1];
+      for (int m = part; m < n; m += 16) acc += ai[(size_t)r * n + m] * bc[m];
 #pragma unroll
     for (int o = 8; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (r < n && part == 0) v.x[(size_t)(r / C.nI + 1) * C.ld + r % C.nI + 1] = acc;
+    if (r < n && part == 0) v.x[(size_t)(cr + 1) * C.ld + cc + 1] = acc;
     __syncthreads();
   }
   for (int l = nl - 2; l >= nd; --l) {

@@ -157,50 +157,77 @@ __global__ void k_coarsen(Level<T> F, Level<T> C) {
   }
 }
 
-// Dense inverse of the coarsest operator (n <= 64), in-place Gauss-Jordan
-// without pivoting (the operator is SPD), computed in the hierarchy's precision
-// (one SM's FP64 rate would make the FP64 elimination ~100 us).  One block of
-// 1024 threads; each pivot step scales the pivot row and updates all other
-// entries in parallel.
+// Dense inverse of the coarsest operator (n <= 64), Gauss-Jordan without
+// pivoting (the operator is SPD), computed in the hierarchy's precision (one SM's
+// FP64 rate makes the FP64 elimination ~60 us; the FP32 one takes a few).  One
+// block of 1024 threads, thread t owning row t/16 and columns t%16 + 16q
+// (q = 0..3) in registers; each pivot step publishes the pivot row, the pivot
+// column and the pivot's reciprocal through shared memory.
 template <typename T>
 __global__ void __launch_bounds__(1024) k_dense_inverse(Level<T> C, double* __restrict__ ainv) {
-  __shared__ T A[kCoarseMax][kCoarseMax + 1];
+  static_assert(kCoarseMax == 64, "register blocking assumes 64 x 64");
   __shared__ T prow[kCoarseMax], fcol[kCoarseMax];
+  __shared__ T s_inv;
   const int n = C.nI * C.nJ;
   if (n > kCoarseMax) return;  // prevented on the host (alloc_hierarchy)
-  for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-    int r = t / n, m = t % n;
-    int i = r % C.nI, j = r / C.nI;
-    size_t k = (size_t)(i + 1) + (size_t)(j + 1) * C.ld;
-    T v = 0;
-    if (m == r) v = C.dg[k];
-    else if (i > 0 && m == r - 1) v = -C.cx[k];
-    else if (i < C.nI - 1 && m == r + 1) v = -C.cx[k + 1];
-    else if (j > 0 && m == r - C.nI) v = -C.cy[k];
-    else if (j < C.nJ - 1 && m == r + C.nI) v = -C.cy[k + C.ld];
-    A[r][m] = v;
+  const int r = threadIdx.x >> 4, m0 = threadIdx.x & 15;
+  const bool rok = r < n;
+  T a[4];
+  {
+    int ri = 0, rj = 0;
+    size_t k = 0;
+    if (rok) {
+      ri = r % C.nI;
+      rj = r / C.nI;
+      k = (size_t)(ri + 1) + (size_t)(rj + 1) * C.ld;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int m = m0 + 16 * q;
+      T v = 0;
+      if (rok && m < n) {
+        if (m == r) v = C.dg[k];
+        else if (ri > 0 && m == r - 1) v = -C.cx[k];
+        else if (ri < C.nI - 1 && m == r + 1) v = -C.cx[k + 1];
+        else if (rj > 0 && m == r - C.nI) v = -C.cy[k];
+        else if (rj < C.nJ - 1 && m == r + C.nI) v = -C.cy[k + C.ld];
+      }
+      a[q] = v;
+    }
   }
-  __syncthreads();
   for (int kk = 0; kk < n; ++kk) {
-    if ((int)threadIdx.x < n) {
-      int t = threadIdx.x;
-      T inv = (T)1 / A[kk][kk];
-      fcol[t] = A[t][kk];
-      prow[t] = (t == kk) ? inv : A[kk][t] * inv;
+    const int qk = kk >> 4;
+    const T own_col = qk == 0 ? a[0] : qk == 1 ? a[1] : qk == 2 ? a[2] : a[3];
+    if (r == kk) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) prow[m0 + 16 * q] = a[q];
+      if (m0 == (kk & 15)) s_inv = (T)1 / own_col;
     }
+    if (rok && m0 == (kk & 15)) fcol[r] = own_col;
     __syncthreads();
-    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
-      int r = t / n, m = t % n;
+    const T inv = s_inv;
+    const T fr = rok ? fcol[r] : (T)0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int m = m0 + 16 * q;
+      if (!rok || m >= n) continue;
+      const T pm = m == kk ? inv : prow[m] * inv;
       if (r == kk)
-        A[r][m] = prow[m];
+        a[q] = pm;
       else if (m == kk)
-        A[r][m] = -fcol[r] * prow[kk];
+        a[q] = -fr * inv;
       else
-        A[r][m] -= fcol[r] * prow[m];
+        a[q] -= fr * pm;
     }
     __syncthreads();
   }
-  for (int t = threadIdx.x; t < n * n; t += blockDim.x) ainv[t] = (double)A[t / n][t % n];
+  if (rok) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int m = m0 + 16 * q;
+      if (m < n) ainv[(size_t)r * n + m] = (double)a[q];
+    }
+  }
 }
 
 // ---- tiled smoothing (levels above the tail) ----------------------------------
@@ -383,7 +410,7 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_sweep(Level<T> L, Level<T> C, 
       if (gi >= L.nI || gj >= L.nJ) continue;
       const int s = (ti + H) + (tj + H) * W;
       xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
-      if (RESTRICT) {
+      if (RESTRICT && !((gi + gj) & 1)) {  // red cells: black residuals are zero after the black half sweep
         T ax = ds[s] * xs[s] - cxs[s] * xs[s - 1] - cxs[s + 1] * xs[s + 1] - cys[s] * xs[s - W] - cys[s + W] * xs[s + W];
         acc += bs[s] - ax;
       }
@@ -503,14 +530,13 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(TailArgs<T> a, const doub
     for (int u = threadIdx.x; u < C.nI * C.nJ; u += blockDim.x) {
       int I = u % C.nI, J = u / C.nI;
       T acc = 0;
-      for (int bb = 0; bb < 2; ++bb)
-        for (int aa = 0; aa < 2; ++aa) {
-          int i = 2 * I + aa, j = 2 * J + bb;
-          if (i >= L.nI || j >= L.nJ) continue;
-          int k = (i + 1) + (j + 1) * L.ld;
-          T ax = t.dg[k] * t.x[k] - t.cx[k] * t.x[k - 1] - t.cx[k + 1] * t.x[k + 1] - t.cy[k] * t.x[k - L.ld] - t.cy[k + L.ld] * t.x[k + L.ld];
-          acc += t.b[k] - ax;
-        }
+      for (int bb = 0; bb < 2; ++bb) {  // red cells only: black residuals are zero after the black half sweep
+        int j = 2 * J + bb, i = 2 * I + (j & 1);
+        if (i >= L.nI || j >= L.nJ) continue;
+        int k = (i + 1) + (j + 1) * L.ld;
+        T ax = t.dg[k] * t.x[k] - t.cx[k] * t.x[k - 1] - t.cx[k + 1] * t.x[k + 1] - t.cy[k] * t.x[k - L.ld] - t.cy[k + L.ld] * t.x[k + L.ld];
+        acc += t.b[k] - ax;
+      }
       tc.b[(I + 1) + (J + 1) * C.ld] = (T)0.25 * acc;
     }
     __syncthreads();
@@ -911,6 +937,8 @@ bool plan_ctail(Hierarchy<T>& H, int P) {
     a.ainv_off = (int)off;
     const int nc = H.L[nl - 1].nI * H.L[nl - 1].nJ;
     off += (size_t)nc * nc;
+    a.bc_off = (int)off;
+    off += (size_t)nc;
     const size_t bytes = off * sizeof(T);
     if (bytes > kCtSmemCap) continue;
     H.ctail = top;

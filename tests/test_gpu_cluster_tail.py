@@ -106,4 +106,9 @@ def test_full_solve_matches_single_cta_tail(gb, ni, nj, prec_name):
         out[cluster] = (x, st.iterations)
         c.close()
     assert abs(out[True][1] - out[False][1]) <= (1 if prec_name == "FP64" else 2), (out[True][1], out[False][1])
-    assert rel_l2(out[True][0], out[False][0]) <= 100 * tol
+    # The reference pins a Neumann problem at one corner, so A has a near-null
+    # constant mode: solutions with the same small residual may differ by an
+    # almost constant offset.  Only pressure differences enter the velocity update.
+    a, b = out[True][0], out[False][0]
+    assert rel_l2(a - a.mean(), b - b.mean()) <= 100 * tol
+    assert rel_l2(a, b) <= 1e4 * tol
