@@ -233,16 +233,18 @@ __global__ void __launch_bounds__(1024) k_dense_inverse(Level<T> C, double* __re
 // ---- tiled smoothing (levels above the tail) ----------------------------------
 //
 // A block of 32x8 threads owns a 64x16 tile; thread (tx, ty) owns the 2x2 quad of
-// cells (2tx..2tx+1, 2ty..2ty+1), which is also one coarse cell.  The block stages
+// cells (2tx..2tx+1, 2ty..2ty+1), which is also one coarse cell.  All NS
+// red-black sweeps of one side of the V-cycle run in ONE launch: the block stages
 // x and the coefficients (b, 1/dg, cx, cy, and dg when it restricts) for the tile
-// plus a halo of H cells in shared memory with unrolled, compile-time-bounded
-// loops, runs both half sweeps from shared memory (halo cells of the first colour
-// are recomputed so that the tile's second colour is exact), and writes the tile.
-// Cells outside the domain are staged as zero, which is also the value of every
-// wall-face conductance.  A sweep reads x from L.x and writes xout (the level's
-// other buffer): blocks stage halo cells that neighbouring blocks of the same
-// launch update, so an in-place write would let a block read a neighbour's
-// already-smoothed (and, when prolonging, already-corrected) value.
+// plus a halo of 2 NS (+1 to restrict) cells in shared memory with unrolled,
+// compile-time-bounded loops, runs the 2 NS half sweeps from shared memory over
+// windows shrinking by one cell per side each (the halo is recomputed so that the
+// tile's last colour is exact), and writes the tile.  Cells outside the domain
+// are staged as zero, which is also the value of every wall-face conductance.
+// A launch reads x from one buffer and writes the level's other buffer: blocks
+// stage halo cells that neighbouring blocks of the same launch update, so an
+// in-place write would let a block read a neighbour's already-smoothed (and,
+// when prolonging, already-corrected) value.
 
 constexpr int BXT = 32, BYT = 8;          // threads per block (x, y)
 constexpr int TXS = 2 * BXT, TYS = 2 * BYT;  // tile of one block
@@ -381,24 +383,41 @@ __device__ __forceinline__ void publish_rz(Scalars* sc, double rz) {
 }
 
 
-// Pre-smoothing sweep (red, then black).  ZERO: x was zero (not read).  With
-// RESTRICT (halo 3), each thread's quad residual b - A x is averaged into the
-// coarse right-hand side.
-template <typename T, bool ZERO, bool RESTRICT>
-__global__ void __launch_bounds__(BXT* BYT) k_pre_sweep(Level<T> L, Level<T> C, T* __restrict__ xout, const int* __restrict__ done) {
+// Half sweeps R = R0..R1 (window shrunk by R), colour of the first = C0,
+// alternating, with a block barrier after each.
+template <typename T, int H, int R, int R1, int C0>
+__device__ __forceinline__ void window_halves(T* sm, int i0, int j0, int nI, int nJ) {
+  if constexpr (R <= R1) {
+    window_half<T, H, R>(sm, i0, j0, nI, nJ, (C0 + R - 1) & 1);
+    __syncthreads();
+    window_halves<T, H, R + 1, R1, C0>(sm, i0, j0, nI, nJ);
+  }
+}
+
+template <typename T, int NS>
+constexpr size_t pre_smem() {
+  return sweep_smem<T, 2 * NS + 1, true>();
+}
+template <typename T, int NS>
+constexpr size_t post_smem() {
+  return sweep_smem<T, 2 * NS, false>();
+}
+
+// Pre-smoothing: NS red-black sweeps (red first) from x = 0, then the residual
+// of the red cells (the black ones are zero after the last black half sweep)
+// averaged into the coarse right-hand side.  x is written to xout.
+template <typename T, int NS>
+__global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C, T* __restrict__ xout, const int* __restrict__ done) {
   if (*done) return;
-  constexpr int H = RESTRICT ? 3 : 2;
+  constexpr int H = 2 * NS + 1;
   using Wn = Win<T, H>;
   constexpr int W = Wn::W, N = Wn::N;
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int i0 = blockIdx.x * TXS, j0 = blockIdx.y * TYS;
-  stage_window<T, H, !ZERO, false, RESTRICT>(L, C, sm, i0, j0);
+  stage_window<T, H, false, false, true>(L, C, sm, i0, j0);
   __syncthreads();
-  window_half<T, H, 1>(sm, i0, j0, L.nI, L.nJ, 0);
-  __syncthreads();
-  window_half<T, H, 2>(sm, i0, j0, L.nI, L.nJ, 1);
-  __syncthreads();
+  window_halves<T, H, 1, 2 * NS, 0>(sm, i0, j0, L.nI, L.nJ);
   const T *xs = sm, *bs = sm + N, *cxs = sm + 3 * N, *cys = sm + 4 * N, *ds = sm + 5 * N;
   T acc = 0;
 #pragma unroll
@@ -410,36 +429,31 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_sweep(Level<T> L, Level<T> C, 
       if (gi >= L.nI || gj >= L.nJ) continue;
       const int s = (ti + H) + (tj + H) * W;
       xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
-      if (RESTRICT && !((gi + gj) & 1)) {  // red cells: black residuals are zero after the black half sweep
+      if (!((gi + gj) & 1)) {  // red cells: black residuals are zero after the black half sweep
         T ax = ds[s] * xs[s] - cxs[s] * xs[s - 1] - cxs[s + 1] * xs[s + 1] - cys[s] * xs[s - W] - cys[s + W] * xs[s + W];
         acc += bs[s] - ax;
       }
     }
-  if (RESTRICT) {
-    const int I = i0 / 2 + threadIdx.x, J = j0 / 2 + threadIdx.y;
-    if (I < C.nI && J < C.nJ) C.b[(size_t)(I + 1) + (size_t)(J + 1) * C.ld] = (T)0.25 * acc;
-  }
+  const int I = i0 / 2 + threadIdx.x, J = j0 / 2 + threadIdx.y;
+  if (I < C.nI && J < C.nJ) C.b[(size_t)(I + 1) + (size_t)(J + 1) * C.ld] = (T)0.25 * acc;
 }
 
-// Post-smoothing sweep (black, then red); PROLONG adds the coarse correction while
-// staging.  With part_rz (finest level, last sweep), r.z (b = r, x = z there) is
-// reduced and beta published.
-template <typename T, bool PROLONG>
-__global__ void __launch_bounds__(BXT* BYT) k_post_sweep(Level<T> L, Level<T> C, T* __restrict__ xout, double* __restrict__ part_rz,
-                                                        unsigned* __restrict__ counter, Scalars* sc, const int* __restrict__ done) {
+// Post-smoothing: x (from L.x) plus the prolonged coarse correction, then NS
+// black-red sweeps (black first); x to xout.  With part_rz (finest level) r.z
+// (b = r, x = z there) is reduced and beta published.
+template <typename T, int NS>
+__global__ void __launch_bounds__(BXT* BYT) k_post_smooth(Level<T> L, Level<T> C, T* __restrict__ xout, double* __restrict__ part_rz,
+                                                         unsigned* __restrict__ counter, Scalars* sc, const int* __restrict__ done) {
   if (*done) return;
-  constexpr int H = 2;
+  constexpr int H = 2 * NS;
   using Wn = Win<T, H>;
   constexpr int W = Wn::W, N = Wn::N;
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int i0 = blockIdx.x * TXS, j0 = blockIdx.y * TYS;
-  stage_window<T, H, true, PROLONG, false>(L, C, sm, i0, j0);
+  stage_window<T, H, true, true, false>(L, C, sm, i0, j0);
   __syncthreads();
-  window_half<T, H, 1>(sm, i0, j0, L.nI, L.nJ, 1);
-  __syncthreads();
-  window_half<T, H, 2>(sm, i0, j0, L.nI, L.nJ, 0);
-  __syncthreads();
+  window_halves<T, H, 1, 2 * NS, 1>(sm, i0, j0, L.nI, L.nJ);
   const T *xs = sm, *bs = sm + N;
   Acc<T> acc;
 #pragma unroll
@@ -633,15 +647,21 @@ __device__ __forceinline__ float narrow(double d) {
   return __uint_as_float(bits);
 }
 
+// The CG kernels below run flat over the padded rows 1..nJ, ghost columns
+// included: every vector here is zero on the padding ring and so are the
+// padded coefficients (wall conductances are zero), so ghost entries stay zero
+// and no per-cell index arithmetic is needed.
+#define GB_FLAT_FOR(L, k)                                                                                      \
+  for (size_t k = (size_t)(L).ld + blockIdx.x * (size_t)blockDim.x + threadIdx.x, k##_end = (size_t)(L).ld * ((L).nJ + 1); \
+       k < k##_end; k += (size_t)gridDim.x * blockDim.x)
+
 // r = b - A x with the reference's matrix entries, in FP64; its copy for the
 // preconditioner (rT, FP32 or the FP64 r itself); partial ||r||^2 and ||b||^2.
 template <typename T>
 __global__ void k_residual64(Level<double> L, const double* __restrict__ x, const double* __restrict__ b, double* __restrict__ r64,
                              T* __restrict__ rT, double* __restrict__ part_rr, double* __restrict__ part_bb) {
   double rr = 0.0, bb = 0.0;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
-    int i, j;
-    size_t k = cell_index(L, t, i, j);
+  GB_FLAT_FOR(L, k) {
     double ax = L.dg[k] * x[k] - L.cx[k] * x[k - 1] - L.cx[k + 1] * x[k + 1] - L.cy[k] * x[k - L.ld] - L.cy[k + L.ld] * x[k + L.ld];
     double r = b[k] - ax;
     r64[k] = r;
@@ -673,11 +693,7 @@ __global__ void k_direction(Level<double> L, const TZ* __restrict__ z, double* _
                             const int* __restrict__ done) {
   if (*done) return;
   const double bt = first ? 0.0 : sc->beta;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
-    int i, j;
-    size_t k = cell_index(L, t, i, j);
-    p[k] = first ? widen(z[k]) : widen(z[k]) + bt * p[k];
-  }
+  GB_FLAT_FOR(L, k) { p[k] = first ? widen(z[k]) : widen(z[k]) + bt * p[k]; }
 }
 
 // Ap = A p (reference entries) and p.Ap; the last block publishes
@@ -686,9 +702,7 @@ __global__ void k_apply_pap(Level<double> L, const double* __restrict__ p, doubl
                             unsigned* __restrict__ counter, const int* __restrict__ done) {
   if (*done) return;
   double acc = 0.0;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
-    int i, j;
-    size_t k = cell_index(L, t, i, j);
+  GB_FLAT_FOR(L, k) {
     const double pc = p[k];
     double y = L.dg[k] * pc - L.cx[k] * p[k - 1] - L.cx[k + 1] * p[k + 1] - L.cy[k] * p[k - L.ld] - L.cy[k + L.ld] * p[k + L.ld];
     ap[k] = y;
@@ -713,9 +727,7 @@ __global__ void k_update(Level<double> L, double* __restrict__ x, double* __rest
   if (*done) return;
   const double al = sc->alpha;
   Acc<T> acc;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
-    int i, j;
-    size_t k = cell_index(L, t, i, j);
+  GB_FLAT_FOR(L, k) {
     x[k] += al * p[k];
     const double rn = r[k] - al * ap[k];
     r[k] = rn;
@@ -1048,14 +1060,21 @@ void build_level0_f64(cudaStream_t s, Hierarchy<double>& H, const gb2d_ctx* c, d
   GB_LAUNCHED(1);
 }
 
-// Algorithmic bytes of one tiled sweep on a level: x read and written, b, 1/dg and
-// the two face arrays read once; the restricting sweep also reads dg and writes
-// the coarse b, the prolonging sweep also reads the coarse x.
+// Algorithmic bytes of one tiled smoothing launch on a level (every array read
+// or written once): pre-smoothing reads b, 1/dg, cx, cy, dg, writes x and the
+// coarse b; post-smoothing reads x, b, 1/dg, cx, cy and the coarse x, writes x.
 template <typename T>
-double sweep_bytes(const Level<T>& L, bool zero_init, bool restrict_to, bool prolong) {
-  double n = (double)L.nI * L.nJ;
-  double arrays = (zero_init ? 1.0 : 2.0) + 4.0 + (restrict_to ? 1.25 : 0.0) + (prolong ? 0.25 : 0.0);
-  return sizeof(T) * n * arrays;
+double smooth_bytes(const Level<T>& L) {
+  return sizeof(T) * (double)L.nI * L.nJ * 6.25;
+}
+
+template <typename T, int NS>
+void launch_pre(cudaStream_t s, dim3 grd, const Level<T>& L, const Level<T>& C, T* xo, const int* done) {
+  k_pre_smooth<T, NS><<<grd, dim3(BXT, BYT), pre_smem<T, NS>(), s>>>(L, C, xo, done);
+}
+template <typename T, int NS>
+void launch_post(cudaStream_t s, dim3 grd, const Level<T>& L, const Level<T>& C, T* xo, double* prz, Solver* S) {
+  k_post_smooth<T, NS><<<grd, dim3(BXT, BYT), post_smem<T, NS>(), s>>>(L, C, xo, prz, S->counter + 3, S->sc, S->done);
 }
 
 inline bool probe_begin(Probe* pr, cudaStream_t s) {
@@ -1078,33 +1097,20 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
   const int tail = cluster ? H.ctail : H.tail;
   const int* done = S->done;
   double* P_rz = slot(S, kSlotRz);
-  const dim3 blk(BXT, BYT);
-  // Sweep k of a level's 2*nu writes L.xa or L.x so that the last one writes L.x
-  // (the buffer the next finer level prolongs from, and z on the finest level).
-  auto out = [nu](const Level<T>& L, int k) { return ((2 * nu - 1 - k) & 1) ? L.xa : L.x; };
-  auto reading = [](Level<T> L, T* x) {
-    L.x = x;
-    return L;
-  };
+  // Pre-smoothing writes L.xa, post-smoothing reads it and writes L.x (the
+  // buffer the next finer level prolongs from, and z on the finest level).
   for (int l = 0; l < tail; ++l) {
     Level<T>& L = H.L[l];
     const dim3 grd = tiles(L.nI, L.nJ);
-    for (int sweep = 0; sweep < nu; ++sweep) {
-      bool last = sweep == nu - 1, zero = sweep == 0;
-      bool on = l == 0 && probe_begin(pr, s);
-      Level<T> Lin = reading(L, zero ? nullptr : out(L, sweep - 1));
-      T* xo = out(L, sweep);
-      if (zero && last)
-        k_pre_sweep<T, true, true><<<grd, blk, sweep_smem<T, 3, true>(), s>>>(Lin, H.L[l + 1], xo, done);
-      else if (zero)
-        k_pre_sweep<T, true, false><<<grd, blk, sweep_smem<T, 2, false>(), s>>>(Lin, H.L[l + 1], xo, done);
-      else if (last)
-        k_pre_sweep<T, false, true><<<grd, blk, sweep_smem<T, 3, true>(), s>>>(Lin, H.L[l + 1], xo, done);
-      else
-        k_pre_sweep<T, false, false><<<grd, blk, sweep_smem<T, 2, false>(), s>>>(Lin, H.L[l + 1], xo, done);
-      GB_LAUNCHED(1);
-      probe_end(pr, s, on, sweep_bytes(L, zero, last, false));
-    }
+    bool on = l == 0 && probe_begin(pr, s);
+    if (nu == 1)
+      launch_pre<T, 1>(s, grd, L, H.L[l + 1], L.xa, done);
+    else if (nu == 2)
+      launch_pre<T, 2>(s, grd, L, H.L[l + 1], L.xa, done);
+    else
+      launch_pre<T, 3>(s, grd, L, H.L[l + 1], L.xa, done);
+    GB_LAUNCHED(1);
+    probe_end(pr, s, on, smooth_bytes(L));
   }
   if (cluster) {
     launch_ctail<T>(s, H, ainv, nu, done, S->sc);
@@ -1125,19 +1131,18 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
   for (int l = tail - 1; l >= 0; --l) {
     Level<T>& L = H.L[l];
     const dim3 grd = tiles(L.nI, L.nJ);
-    for (int sweep = 0; sweep < nu; ++sweep) {
-      bool first = sweep == 0;
-      double* prz = (l == 0 && sweep == nu - 1) ? P_rz : nullptr;
-      bool on = l == 0 && probe_begin(pr, s);
-      Level<T> Lin = reading(L, out(L, nu + sweep - 1));
-      T* xo = out(L, nu + sweep);
-      if (first)
-        k_post_sweep<T, true><<<grd, blk, sweep_smem<T, 2, false>(), s>>>(Lin, H.L[l + 1], xo, prz, S->counter + 3, S->sc, done);
-      else
-        k_post_sweep<T, false><<<grd, blk, sweep_smem<T, 2, false>(), s>>>(Lin, H.L[l + 1], xo, prz, S->counter + 3, S->sc, done);
-      GB_LAUNCHED(1);
-      probe_end(pr, s, on, sweep_bytes(L, false, false, first));
-    }
+    Level<T> Lin = L;
+    Lin.x = L.xa;
+    double* prz = l == 0 ? P_rz : nullptr;
+    bool on = l == 0 && probe_begin(pr, s);
+    if (nu == 1)
+      launch_post<T, 1>(s, grd, Lin, H.L[l + 1], L.x, prz, S);
+    else if (nu == 2)
+      launch_post<T, 2>(s, grd, Lin, H.L[l + 1], L.x, prz, S);
+    else
+      launch_post<T, 3>(s, grd, Lin, H.L[l + 1], L.x, prz, S);
+    GB_LAUNCHED(1);
+    probe_end(pr, s, on, smooth_bytes(L));
   }
 }
 
@@ -1269,6 +1274,18 @@ int inner_pcg(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, doubl
   return iters;
 }
 
+template <typename T>
+cudaError_t set_smooth_smem() {
+  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaFuncSetAttribute(k_pre_smooth<T, 1>, a, (int)pre_smem<T, 1>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_smooth<T, 2>, a, (int)pre_smem<T, 2>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_smooth<T, 3>, a, (int)pre_smem<T, 3>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 1>, a, (int)post_smem<T, 1>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 2>, a, (int)post_smem<T, 2>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 3>, a, (int)post_smem<T, 3>());
+  return e;
+}
+
 }  // namespace
 
 Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
@@ -1304,12 +1321,8 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
   if (e == cudaSuccess) e = cudaMallocHost(&S->host, 8 * sizeof(double));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->ev[0], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->ev[1], cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_sweep<double, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 3, true>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_sweep<double, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 3, true>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_sweep<double, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 2, false>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_sweep<double, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 2, false>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_sweep<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 2, false>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_sweep<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_smem<double, 2, false>());
+  if (e == cudaSuccess) e = set_smooth_smem<float>();
+  if (e == cudaSuccess) e = set_smooth_smem<double>();
   // The attribute is per kernel for the whole process: only ever raise it.
   static size_t tail_smem_set[2] = {0, 0};
   if (e == cudaSuccess && S->h64.tail_smem > tail_smem_set[0]) {

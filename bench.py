@@ -321,7 +321,7 @@ def run_gb300(args):
         "clocks": clk,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
-        "roofline": {"bound": "hbm", "kernel": "finest-level red-black smoothing sweep (k_pre_sweep / k_post_sweep, FP32)",
+        "roofline": {"bound": "hbm", "kernel": "finest-level smoothing launch (k_pre_smooth / k_post_smooth: two red-black sweeps each, FP32)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                      "peak_source": peak_kind, "traffic": traffic, "launches_timed": nprobe,
                      "avg_launch_us": (probe_ms / nprobe * 1e3) if nprobe else None, "algorithmic_bytes_per_launch": probe_bytes},
