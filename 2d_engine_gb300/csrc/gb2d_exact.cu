@@ -22,9 +22,8 @@ inline unsigned blocks_for(size_t n, int threads = kThreads) { return (unsigned)
 __global__ void k_fill_ghost_copy(double* dst_a, int gd, const double* __restrict__ src_a, int gs, int nI, int nJ, int g) {
   DField d = dfield(dst_a, gd, nI, nJ);
   DField s = dfield((double*)src_a, gs, nI, nJ);
-  int W = nI + 2 * g, H = nJ + 2 * g;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)W * H; t += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % W) - g, j = (int)(t / W) - g;
+  GB_FOR_IJ(ii, jj, nI + 2 * g, nJ + 2 * g) {
+    int i = ii - g, j = jj - g;
     bool in_i = i >= 0 && i < nI, in_j = j >= 0 && j < nJ;
     if (in_i && in_j)
       GB_AT(d, i, j) = GB_AT(s, i, j);
@@ -124,8 +123,8 @@ __global__ void k_weno5_advect(const double* __restrict__ src_a, double* __restr
 // Sign function of Reinitialization (EULERIAN_FLUID_SOLVER_2D.h:2431-2435).
 __global__ void k_reinit_sign(const double* __restrict__ phi_a, double* __restrict__ S, int ni, int nj, double dx) {
   DField phi = dfield((double*)phi_a, 2, ni, nj);
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % ni), j = (int)(t / ni);
+  GB_FOR_IJ(i, j, ni, nj) {
+    const size_t t = (size_t)j * ni + i;
     double p = GB_AT(phi, i, j);
     S[t] = p / sqrt(p * p + dx * dx);
   }
@@ -171,8 +170,7 @@ __global__ void k_reinit_sweep(const double* __restrict__ src_a, double* __restr
 // Shu-Osher blend of the TVD-RK3 stages (EULERIAN_FLUID_SOLVER_2D.h:1706-1741): interior only.
 __global__ void k_blend(const double* __restrict__ keep_a, double* phi_a, int ni, int nj, double c0, double c1) {
   DField keep = dfield((double*)keep_a, 2, ni, nj), phi = dfield(phi_a, 2, ni, nj);
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % ni), j = (int)(t / ni);
+  GB_FOR_IJ(i, j, ni, nj) {
     GB_AT(phi, i, j) = c0 * GB_AT(keep, i, j) + c1 * GB_AT(phi, i, j);
   }
 }
@@ -188,13 +186,8 @@ struct EnoArgs {
 __global__ void k_eno3(double* __restrict__ u_a, double* __restrict__ v_a, const double* __restrict__ ua_a, const double* __restrict__ va_a,
                        EnoArgs a, double dt) {
   int ni = a.ni, nj = a.nj;
-  size_t nu = (size_t)(ni + 1) * nj, nv = (size_t)ni * (nj + 1);
   DField ua = dfield((double*)ua_a, 3, ni + 1, nj), va = dfield((double*)va_a, 3, ni, nj + 1);
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nu + nv; t += (size_t)gridDim.x * blockDim.x) {
-    bool xc = t < nu;
-    int nI = xc ? ni + 1 : ni;
-    size_t k = xc ? t : t - nu;
-    int i = (int)(k % nI), j = (int)(k / nI);
+  auto face = [&](bool xc, int i, int j) {
     const DField& g = xc ? ua : va;
     const Space& s = xc ? a.xs : a.ys;
     double q[7];
@@ -214,16 +207,45 @@ __global__ void k_eno3(double* __restrict__ u_a, double* __restrict__ v_a, const
     double fx = uu > 0 ? mx : px, fy = vv > 0 ? my : py;
     DField out = xc ? dfield(u_a, 2, ni + 1, nj) : dfield(v_a, 2, ni, nj + 1);
     GB_AT(out, i, j) = GB_AT(out, i, j) - dt * (uu * fx + vv * fy);
-  }
+  };
+  GB_FOR_IJ(i, j, ni + 1, nj) face(true, i, j);
+  GB_FOR_IJ(i, j, ni, nj + 1) face(false, i, j);
+}
+
+// IEEE comparisons evaluated on the integer pipes: an FP64 compare takes one of
+// the part's few FP64 issue slots (about two per clock per SM).  Exact for every
+// input, NaN and infinities included.
+constexpr long long kAbsBits = 0x7fffffffffffffffLL, kInfBits = 0x7ff0000000000000LL;
+__device__ __forceinline__ bool gt0(double x) {  // x > 0
+  const long long b = __double_as_longlong(x);
+  return b > 0 && b <= kInfBits;
+}
+__device__ __forceinline__ bool le0(double x) {  // x <= 0
+  const long long b = __double_as_longlong(x);
+  return b == 0 || (b < 0 && (b & kAbsBits) <= kInfBits);
+}
+__device__ __forceinline__ bool lt0(double x) {  // x < 0
+  const long long b = __double_as_longlong(x), m = b & kAbsBits;
+  return b < 0 && m != 0 && m <= kInfBits;
+}
+// x * y >= 0 as IEEE evaluates it.  When both are normal and finite and the
+// product's exponent keeps it above the subnormal range, only the signs decide;
+// zeros, subnormals, infinities, NaN and products that may round to zero take
+// the FP64 multiply.
+__device__ __forceinline__ bool prod_ge0(double x, double y) {
+  const long long bx = __double_as_longlong(x), by = __double_as_longlong(y);
+  const int ex = (int)((bx >> 52) & 0x7ff), ey = (int)((by >> 52) & 0x7ff);
+  if (ex != 0 && ey != 0 && ex != 0x7ff && ey != 0x7ff && ex + ey >= 972) return (bx ^ by) >= 0;
+  return x * y >= 0;
 }
 
 // ComputeCurvaturesThread with curvature_by_levelset (LEVELSET_2D.h:898-990);
 // phi's ghosts must already be extrapolated.
 __global__ void k_curvature(const double* __restrict__ phi_a, double* __restrict__ kappa, int ni, int nj, Space s, int* flag) {
   DField phi = dfield((double*)phi_a, 2, ni, nj);
-  double tol = 1.0 / (s.dx < s.dy ? s.dx : s.dy);
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % ni), j = (int)(t / ni);
+  const double tol = s.dx < s.dy ? s.odx : s.ody;  // 1 / min(dx, dy), taken on the host
+  GB_FOR_IJ(i, j, ni, nj) {
+    const size_t t = (size_t)j * ni + i;
     double c = GB_AT(phi, i, j);
     double l = GB_AT(phi, i - 1, j), r = GB_AT(phi, i + 1, j), b = GB_AT(phi, i, j - 1), tp = GB_AT(phi, i, j + 1);
     double px = (r - l) * s.o2dx;
@@ -234,7 +256,7 @@ __global__ void k_curvature(const double* __restrict__ phi_a, double* __restrict
     double mag = sqrt(px * px + py * py);
     double deno = mag * mag * mag;
     double curv;
-    if (deno != 0) {
+    if ((__double_as_longlong(deno) & kAbsBits) != 0) {  // deno != 0 (NaN included)
       double od = 1.0 / deno;
       curv = -(px * px * pyy - 2.0 * px * py * pxy + py * py * pxx) * od;
     } else {
@@ -242,19 +264,19 @@ __global__ void k_curvature(const double* __restrict__ phi_a, double* __restrict
       py = (tp - c) * s.ody;
       mag = sqrt(px * px + py * py);
       deno = mag * mag * mag;
-      if (deno == 0) {
+      if ((__double_as_longlong(deno) & kAbsBits) == 0) {  // deno == 0
         atomicOr(flag, 2);
         continue;
       }
       double od = 1.0 / deno;
       curv = -(px * px * pyy - 2.0 * px * py * pxy + py * py * pxx) * od;
     }
-    if (fabs(curv) <= tol)
+    // Clamp to [-tol, tol] with IEEE comparisons (tol > 0 finite; a NaN stores nothing)
+    const long long cb = __double_as_longlong(curv), cm = cb & kAbsBits, tb = __double_as_longlong(tol);
+    if (cm <= tb)
       kappa[t] = curv;
-    else if (curv > tol)
-      kappa[t] = tol;
-    else if (curv < -tol)
-      kappa[t] = -tol;
+    else if (cm <= kInfBits)
+      kappa[t] = cb > 0 ? tol : -tol;
   }
 }
 
@@ -268,8 +290,8 @@ struct AsmArgs {
 // 1/rho of a node.  The density takes two values, so the quotient is a select of
 // the host's correctly rounded reciprocals (FP64 divides are scarce on this part).
 __device__ __forceinline__ double inv_density(double phi, const AsmArgs& a) {
-  if (phi <= 0) return a.inv_air;
-  if (phi > 0) return a.inv_water;
+  if (le0(phi)) return a.inv_air;
+  if (gt0(phi)) return a.inv_water;
   return 1.0;
 }
 
@@ -290,16 +312,11 @@ __device__ __forceinline__ double face_beta(double vc, double vn, double pc, dou
 __global__ void k_faces(const double* __restrict__ phi_a, double* __restrict__ bx, double* __restrict__ by, AsmArgs a) {
   int ni = a.ni, nj = a.nj;
   DField phi = dfield((double*)phi_a, 2, ni, nj);
-  size_t nx = (size_t)(ni + 1) * nj, ny = (size_t)ni * (nj + 1);
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < nx + ny; t += (size_t)gridDim.x * blockDim.x) {
-    if (t < nx) {
-      int i = (int)(t % (ni + 1)), j = (int)(t / (ni + 1));
-      bx[t] = face_beta(vnode(phi, i, j, a), vnode(phi, i - 1, j, a), GB_AT(phi, i, j), GB_AT(phi, i - 1, j));
-    } else {
-      size_t k = t - nx;
-      int i = (int)(k % ni), j = (int)(k / ni);
-      by[k] = face_beta(vnode(phi, i, j, a), vnode(phi, i, j - 1, a), GB_AT(phi, i, j), GB_AT(phi, i, j - 1));
-    }
+  GB_FOR_IJ(i, j, ni + 1, nj) {
+    bx[(size_t)j * (ni + 1) + i] = face_beta(vnode(phi, i, j, a), vnode(phi, i - 1, j, a), GB_AT(phi, i, j), GB_AT(phi, i - 1, j));
+  }
+  GB_FOR_IJ(i, j, ni, nj + 1) {
+    by[(size_t)j * ni + i] = face_beta(vnode(phi, i, j, a), vnode(phi, i, j - 1, a), GB_AT(phi, i, j), GB_AT(phi, i, j - 1));
   }
 }
 
@@ -314,13 +331,13 @@ __device__ __forceinline__ double jc_at(const double* kappa, int i, int j, const
 // read only on arms that cross the interface.
 __device__ __forceinline__ double arm_flux(double pc, double pn, double jcc, const double* kappa, int in, int jn, double beta, double o2,
                                            const AsmArgs& a) {
-  const bool cneg = pc <= 0, nneg = pn <= 0;
-  if (cneg && !nneg && pn > 0) {
+  const bool cneg = le0(pc), nneg = le0(pn);
+  if (cneg && !nneg && gt0(pn)) {
     double ac = fabs(pc), an = fabs(pn);
     double av = (jcc * an + jc_at(kappa, in, jn, a) * ac) / (ac + an);
     return o2 * av * beta;
   }
-  if (!cneg && pc > 0 && nneg) {
+  if (!cneg && gt0(pc) && nneg) {
     double ac = fabs(pc), an = fabs(pn);
     double av = (jcc * an + jc_at(kappa, in, jn, a) * ac) / (ac + an);
     return -o2 * av * beta;
@@ -335,8 +352,8 @@ __global__ void k_rhs_diag(const double* __restrict__ phi_a, const double* __res
   int ni = a.ni, nj = a.nj;
   DField phi = dfield((double*)phi_a, 2, ni, nj);
   DField u = dfield((double*)u_a, 2, ni + 1, nj), v = dfield((double*)v_a, 2, ni, nj + 1);
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % ni), j = (int)(t / ni);
+  GB_FOR_IJ(i, j, ni, nj) {
+    const size_t t = (size_t)j * ni + i;
     double bl = bx[i + (size_t)j * (ni + 1)], br = bx[i + 1 + (size_t)j * (ni + 1)];
     double bb = by[i + (size_t)j * ni], bt = by[i + (size_t)(j + 1) * ni];
     double coef = 0;
@@ -350,7 +367,7 @@ __global__ void k_rhs_diag(const double* __restrict__ phi_a, const double* __res
       if (j - 1 < 0) coef += bb;
       if (j + 1 > nj - 1) coef += bt;
     }
-    if (coef == 0) coef = 1;
+    if ((__double_as_longlong(coef) & kAbsBits) == 0) coef = 1;  // coef == 0
     diag[t] = a.inv_dxdx * coef;
 
     double pc = GB_AT(phi, i, j);
@@ -369,8 +386,8 @@ __global__ void k_rhs_diag(const double* __restrict__ phi_a, const double* __res
 // CSR_MATRIX::Multiply in the builder's row order (left, right, bottom, top, diagonal).
 __global__ void k_apply_exact(const double* __restrict__ bx, const double* __restrict__ by, const double* __restrict__ diag,
                               const double* __restrict__ x, double* __restrict__ y, int ni, int nj, double idx2, double idy2) {
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % ni), j = (int)(t / ni);
+  GB_FOR_IJ(i, j, ni, nj) {
+    const size_t t = (size_t)j * ni + i;
     double acc = 0;
     if (i > 0) acc += -bx[i + (size_t)j * (ni + 1)] * idx2 * x[t - 1];
     if (i < ni - 1) acc += -bx[i + 1 + (size_t)j * (ni + 1)] * idx2 * x[t + 1];
@@ -390,8 +407,7 @@ __device__ __forceinline__ double heaviside(double phi, double eps) {
   return 0.5 + phi * oe * 0.5 + 0.5 * opi * sin(PI_REF * phi * oe);
 }
 
-__device__ __forceinline__ void block_max_bits(double v, unsigned long long* out) {
-  unsigned long long b = __double_as_longlong(v);
+__device__ __forceinline__ void block_max_bits(unsigned long long b, unsigned long long* out) {
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long w = __shfl_xor_sync(0xffffffffu, b, o);
     b = w > b ? w : b;
@@ -408,37 +424,36 @@ __global__ void k_velocity_update(const double* __restrict__ phi_a, const double
   int ni = a.ni, nj = a.nj;
   DField phi = dfield((double*)phi_a, 2, ni, nj), p = dfield((double*)p_a, 1, ni, nj);
   DField u = dfield(u_a, 2, ni + 1, nj), v = dfield(v_a, 2, ni, nj + 1);
-  double odx = 1.0 / a.s.dx, ody = 1.0 / a.s.dy;
+  const double odx = a.s.odx, ody = a.s.ody;  // 1 / dx, 1 / dy, taken on the host
   double eh = 1.5 * a.s.dx, ev = 1.5 * a.s.dy;
-  size_t n = (size_t)ni * nj;
-  double mx = 0, my = 0;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < 2 * n; t += (size_t)gridDim.x * blockDim.x) {
-    bool xc = t < n;
-    size_t k = xc ? t : t - n;
-    int i = (int)(k % ni), j = (int)(k / ni);
+  unsigned long long mx = 0, my = 0;  // bits of max |u|, |v| (non-negative doubles order as integers)
+  auto face = [&](bool xc, int i, int j) {
     int in = xc ? i - 1 : i, jn = xc ? j : j - 1;
     double l0 = GB_AT(phi, i, j), ln = GB_AT(phi, in, jn);
-    double oor = l0 <= 0 ? a.inv_air : a.inv_water;  // 1 / rho_ij
+    double oor = le0(l0) ? a.inv_air : a.inv_water;  // 1 / rho_ij
     double dp = GB_AT(p, i, j) - GB_AT(p, in, jn);
     double od = xc ? odx : ody;
     double* w = xc ? &GB_AT(u, i, j) : &GB_AT(v, i, j);
-    if (l0 * ln >= 0) {
+    if (prod_ge0(l0, ln)) {
       *w -= dt * dp * oor * od;
     } else {
       double jcc = jc_at(kappa, i, j, a), jcn = jc_at(kappa, in, jn, a);
       double gam = (jcn * fabs(l0) + jcc * fabs(ln)) / (fabs(l0) + fabs(ln));
       double dh = a.air + (a.water - a.air) * heaviside(0.5 * (l0 + ln), xc ? eh : ev);
       double odh = 1 / dh;
-      if (l0 < 0)
+      if (lt0(l0))
         *w -= dt * (dp + gam) * odh * od;
-      else if (l0 > 0)
+      else if (gt0(l0))
         *w -= dt * (dp - gam) * odh * od;
     }
-    double aw = fabs(*w);
-    if (xc)
-      mx = aw > mx ? aw : mx;
-    else
-      my = aw > my ? aw : my;
+    // max(|w|, m) as (|w| > m ? |w| : m): a NaN never replaces the maximum
+    const unsigned long long ab = (unsigned long long)(__double_as_longlong(*w) & kAbsBits);
+    unsigned long long& m = xc ? mx : my;
+    if (ab > m && ab <= (unsigned long long)kInfBits) m = ab;
+  };
+  GB_FOR_IJ(i, j, ni, nj) {
+    face(true, i, j);
+    face(false, i, j);
   }
   block_max_bits(mx, &sc->maxu_bits);
   block_max_bits(my, &sc->maxv_bits);
@@ -446,15 +461,9 @@ __global__ void k_velocity_update(const double* __restrict__ phi_a, const double
 
 __global__ void k_copy_interior(const double* __restrict__ src_a, int gs, double* __restrict__ dst_a, int gd, int nI, int nJ) {
   DField s = dfield((double*)src_a, gs, nI, nJ), d = dfield(dst_a, gd, nI, nJ);
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)nI * nJ; t += (size_t)gridDim.x * blockDim.x) {
-    int i = (int)(t % nI), j = (int)(t / nI);
+  GB_FOR_IJ(i, j, nI, nJ) {
     GB_AT(d, i, j) = GB_AT(s, i, j);
   }
-}
-
-inline unsigned grid_cap(size_t n) {
-  unsigned b = blocks_for(n);
-  return b < 152u * 16u ? (b ? b : 1u) : 152u * 16u;
 }
 
 inline dim3 grid2d(int W, int H, dim3 blk) { return dim3((W + blk.x - 1) / blk.x, (H + blk.y - 1) / blk.y); }
@@ -480,8 +489,7 @@ AsmArgs asm_args(const gb2d_ctx* c, double dt) {
 }  // namespace
 
 void launch_fill_ghost_copy(cudaStream_t s, double* dst, int gd, const double* src, int gs, int nI, int nJ, int g) {
-  size_t n = (size_t)(nI + 2 * g) * (nJ + 2 * g);
-  k_fill_ghost_copy<<<grid_cap(n), kThreads, 0, s>>>(dst, gd, src, gs, nI, nJ, g);
+  k_fill_ghost_copy<<<grid_ij(nI + 2 * g, nJ + 2 * g), kThreads, 0, s>>>(dst, gd, src, gs, nI, nJ, g);
   GB_LAUNCHED(1);
 }
 
@@ -502,7 +510,7 @@ void launch_weno5_advect(cudaStream_t s, const gb2d_ctx* c, const double* src, d
 }
 
 void launch_reinit_sign(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* S) {
-  k_reinit_sign<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(phi, S, c->grid.ni, c->grid.nj, c->base.dx);
+  k_reinit_sign<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, S, c->grid.ni, c->grid.nj, c->base.dx);
   GB_LAUNCHED(1);
 }
 
@@ -517,45 +525,43 @@ void launch_reinit_sweep(cudaStream_t s, const gb2d_ctx* c, const double* src, d
 }
 
 void launch_blend(cudaStream_t s, const gb2d_ctx* c, const double* keep, double* phi, double c0, double c1) {
-  k_blend<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(keep, phi, c->grid.ni, c->grid.nj, c0, c1);
+  k_blend<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(keep, phi, c->grid.ni, c->grid.nj, c0, c1);
   GB_LAUNCHED(1);
 }
 
 void launch_eno3(cudaStream_t s, const gb2d_ctx* c, double dt) {
   EnoArgs a{c->grid.ni, c->grid.nj, c->xs, c->ys};
-  size_t n = (size_t)(c->grid.ni + 1) * c->grid.nj + (size_t)c->grid.ni * (c->grid.nj + 1);
-  k_eno3<<<grid_cap(n), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, dt);
+  k_eno3<<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, dt);
   GB_LAUNCHED(1);
 }
 
 void launch_curvature(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* kappa, int* flag) {
-  k_curvature<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(phi, kappa, c->grid.ni, c->grid.nj, c->base, flag);
+  k_curvature<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, kappa, c->grid.ni, c->grid.nj, c->base, flag);
   GB_LAUNCHED(1);
 }
 
 void launch_assemble(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt) {
   AsmArgs a = asm_args(c, dt);
-  size_t nf = (size_t)(c->grid.ni + 1) * c->grid.nj + (size_t)c->grid.ni * (c->grid.nj + 1);
-  k_faces<<<grid_cap(nf), kThreads, 0, s>>>(phi, c->bx, c->by, a);
+  k_faces<<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(phi, c->bx, c->by, a);
   GB_LAUNCHED(1);
-  k_rhs_diag<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(phi, c->kappa, c->u, c->v, c->bx, c->by, c->diag, c->rhs, a);
+  k_rhs_diag<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, c->kappa, c->u, c->v, c->bx, c->by, c->diag, c->rhs, a);
   GB_LAUNCHED(1);
 }
 
 void launch_poisson_apply_exact(cudaStream_t s, const gb2d_ctx* c, const double* x, double* y) {
   double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
-  k_apply_exact<<<grid_cap((size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, x, y, c->grid.ni, c->grid.nj, idx2, idy2);
+  k_apply_exact<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, x, y, c->grid.ni, c->grid.nj, idx2, idy2);
   GB_LAUNCHED(1);
 }
 
 void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt, Scalars* sc) {
   AsmArgs a = asm_args(c, dt);
-  k_velocity_update<<<grid_cap(2 * (size_t)c->grid.ni * c->grid.nj), kThreads, 0, s>>>(phi, c->p, c->kappa, c->u, c->v, a, dt, sc);
+  k_velocity_update<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, c->p, c->kappa, c->u, c->v, a, dt, sc);
   GB_LAUNCHED(1);
 }
 
 void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst, int gd, int nI, int nJ) {
-  k_copy_interior<<<grid_cap((size_t)nI * nJ), kThreads, 0, s>>>(src, gs, dst, gd, nI, nJ);
+  k_copy_interior<<<grid_ij(nI, nJ), kThreads, 0, s>>>(src, gs, dst, gd, nI, nJ);
   GB_LAUNCHED(1);
 }
 

@@ -27,6 +27,22 @@ struct DField {
 __host__ __device__ inline DField dfield(double* a, int g, int nI, int nJ) { return DField{a, g, nI, nJ, nI + 2 * g}; }
 #define GB_AT(f, i, j) ((f).a[((i) + (f).g) + (size_t)((j) + (f).g) * (f).ld])
 
+// Grid-stride loop over an nI x nJ index space on a 2D grid (x: columns, y:
+// rows): no integer division per element.
+#define GB_FOR_IJ(i, j, nI, nJ)                            \
+  for (int j = blockIdx.y; j < (nJ); j += gridDim.y)       \
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (nI); i += gridDim.x * blockDim.x)
+
+// Launch grid for GB_FOR_IJ with kThreads-wide blocks: columns covered, rows
+// folded so that at most 152 x 16 blocks are launched.
+inline dim3 grid_ij(int nI, int nJ) {
+  unsigned gx = (unsigned)((nI + kThreads - 1) / kThreads), gy = (unsigned)nJ;
+  if (gx < 1) gx = 1;
+  if (gy < 1) gy = 1;
+  while (gx * gy > 152u * 16u && gy > 1) gy = (gy + 1) / 2;
+  return dim3(gx, gy);
+}
+
 // One multigrid level (cell-centred view of the node grid), padded with a zero
 // ring: cell (i, j) at (i+1) + (j+1)*ld, ld = nI + 2.  cx at the same index is the
 // conductance of the face between (i-1, j) and (i, j) (i = 0..nI), cy the face

@@ -82,13 +82,6 @@ __device__ double sum_partials(const double* part, int n) {
 
 __device__ __forceinline__ unsigned block_linear() { return blockIdx.x + blockIdx.y * gridDim.x; }
 
-template <typename T>
-__device__ __forceinline__ size_t cell_index(const Level<T>& L, size_t t, int& i, int& j) {
-  i = (int)(t % L.nI);
-  j = (int)(t / L.nI);
-  return (size_t)(i + 1) + (size_t)(j + 1) * L.ld;
-}
-
 // ---- level construction -----------------------------------------------------
 
 // Level 0 from the assembled FP64 system: conductances beta/dx^2 on interior
@@ -97,9 +90,9 @@ template <typename T>
 __global__ void k_build_level0(const double* __restrict__ bx, const double* __restrict__ by, const double* __restrict__ diag,
                                const double* __restrict__ rhs, Level<T> L, double* __restrict__ b64, double idx2, double idy2) {
   int ni = L.nI, nj = L.nJ;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ni * nj; t += (size_t)gridDim.x * blockDim.x) {
-    int i, j;
-    size_t k = cell_index(L, t, i, j);
+  GB_FOR_IJ(i, j, ni, nj) {
+    const size_t t = (size_t)j * ni + i;
+    const size_t k = (size_t)(i + 1) + (size_t)(j + 1) * L.ld;
     double bl = bx[i + (size_t)j * (ni + 1)];
     double bb = by[i + (size_t)j * ni], bt = by[i + (size_t)(j + 1) * ni];
     double cl = i > 0 ? bl * idx2 : 0.0, cb = j > 0 ? bb * idy2 : 0.0;
@@ -124,9 +117,8 @@ __global__ void k_build_level0(const double* __restrict__ bx, const double* __re
 template <typename T>
 __global__ void k_coarsen(Level<T> F, Level<T> C) {
   int cI = C.nI, cJ = C.nJ;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)cI * cJ; t += (size_t)gridDim.x * blockDim.x) {
-    int I, J;
-    size_t k = cell_index(C, t, I, J);
+  GB_FOR_IJ(I, J, cI, cJ) {
+    const size_t k = (size_t)(I + 1) + (size_t)(J + 1) * C.ld;
     auto fx = [&](int fi, int fj) -> double {  // fine x-face fi at fine row fj (0 outside)
       if (fj >= F.nJ) return 0.0;
       return (double)F.cx[(size_t)(fi + 1) + (size_t)(fj + 1) * F.ld];
@@ -260,6 +252,8 @@ constexpr size_t sweep_smem() {
 }
 
 // Stage the window.  LOAD_X: read x (else zero); PROLONG: add the coarse correction.
+// The window's cells are enumerated flat (division by compile-time constants
+// only), so every thread of the block has work in every pass.
 template <typename T, int H, bool LOAD_X, bool PROLONG, bool DG>
 __device__ __forceinline__ void stage_window(const Level<T>& L, const Level<T>& C, T* sm, int i0, int j0) {
   using Wn = Win<T, H>;
@@ -268,67 +262,61 @@ __device__ __forceinline__ void stage_window(const Level<T>& L, const Level<T>& 
   const int gi0 = i0 - H, gj0 = j0 - H;
   const bool inner = gi0 >= 0 && gj0 >= 0 && gi0 + W <= L.nI && gj0 + HH <= L.nJ;
   const size_t base = (size_t)(gi0 + 1) + (size_t)(gj0 + 1) * L.ld;
+  const int tid = threadIdx.x + threadIdx.y * BXT;
 #pragma unroll
-  for (int r0 = 0; r0 < HH; r0 += BYT) {
-    const int r = r0 + threadIdx.y;
-    if (r >= HH) continue;
-#pragma unroll
-    for (int c0 = 0; c0 < W; c0 += BXT) {
-      const int c = c0 + threadIdx.x;
-      if (c >= W) continue;
-      const int gi = gi0 + c, gj = gj0 + r;
-      T x = 0, b = 0, id = 0, cx = 0, cy = 0, dg = 0;
-      if (inner || (gi >= 0 && gi < L.nI && gj >= 0 && gj < L.nJ)) {
-        const size_t k = base + c + (size_t)r * L.ld;
-        if (LOAD_X) {
-          x = L.x[k];
-          if (PROLONG) x += C.x[(size_t)(gi / 2 + 1) + (size_t)(gj / 2 + 1) * C.ld];
-        }
-        b = L.b[k];
-        id = L.idg[k];
-        cx = L.cx[k];
-        cy = L.cy[k];
-        if (DG) dg = L.dg[k];
+  for (int u0 = 0; u0 < N; u0 += BXT * BYT) {
+    const int q = u0 + tid;
+    if (q >= N) continue;
+    const int r = q / W, c = q - r * W;
+    const int gi = gi0 + c, gj = gj0 + r;
+    T x = 0, b = 0, id = 0, cx = 0, cy = 0, dg = 0;
+    if (inner || (gi >= 0 && gi < L.nI && gj >= 0 && gj < L.nJ)) {
+      const size_t k = base + c + (size_t)r * L.ld;
+      if (LOAD_X) {
+        x = L.x[k];
+        if (PROLONG) x += C.x[(size_t)(gi / 2 + 1) + (size_t)(gj / 2 + 1) * C.ld];
       }
-      const int q = c + r * W;
-      xs[q] = x;
-      bs[q] = b;
-      is[q] = id;
-      cxs[q] = cx;
-      cys[q] = cy;
-      if (DG) ds[q] = dg;
+      b = L.b[k];
+      id = L.idg[k];
+      cx = L.cx[k];
+      cy = L.cy[k];
+      if (DG) dg = L.dg[k];
     }
+    xs[q] = x;
+    bs[q] = b;
+    is[q] = id;
+    cxs[q] = cx;
+    cys[q] = cy;
+    if (DG) ds[q] = dg;
   }
 }
 
-// Half sweep of one colour over the window shrunk by R cells per side; each
-// thread takes rows ty, ty+8, ... and, in each, the colour's cells 2m+parity for
-// m = tx, tx+32, ...
+// Half sweep of one colour over the window shrunk by R cells per side: the
+// colour's RH x RW/2 cells are enumerated flat over the block's threads.
 template <typename T, int H, int R>
 __device__ __forceinline__ void window_half(T* sm, int i0, int j0, int nI, int nJ, int color) {
   using Wn = Win<T, H>;
   constexpr int W = Wn::W, HH = Wn::HH, N = Wn::N;
-  constexpr int RW = W - 2 * R, RH = HH - 2 * R, HALF = RW / 2;
+  constexpr int RW = W - 2 * R, RH = HH - 2 * R, HALF = RW / 2, TOT = RH * HALF;
   static_assert(RW % 2 == 0, "window rows must hold an even number of cells");
   T* xs = sm;
   const T *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N;
   const int gi0 = i0 - H, gj0 = j0 - H;
+  const bool inner = gi0 + R >= 0 && gj0 + R >= 0 && gi0 + W - R <= nI && gj0 + HH - R <= nJ;
+  const int tid = threadIdx.x + threadIdx.y * BXT;
 #pragma unroll
-  for (int q = 0; q < (RH + BYT - 1) / BYT; ++q) {
-    const int r = R + threadIdx.y + q * BYT;
-    if (r >= HH - R) continue;
-    const int gj = gj0 + r;
-    const int par = (color - (gi0 + R) - gj) & 1;
-#pragma unroll
-    for (int p = 0; p < (HALF + BXT - 1) / BXT; ++p) {
-      const int m = threadIdx.x + p * BXT;
-      if (m >= HALF) continue;
-      const int c = R + 2 * m + par;
+  for (int u0 = 0; u0 < TOT; u0 += BXT * BYT) {
+    const int u = u0 + tid;
+    if (u >= TOT) continue;
+    const int rr = u / HALF, m = u - rr * HALF;
+    const int r = R + rr, gj = gj0 + r;
+    const int c = R + 2 * m + ((color - (gi0 + R) - gj) & 1);
+    if (!inner) {
       const int gi = gi0 + c;
       if (gi < 0 || gi >= nI || gj < 0 || gj >= nJ) continue;
-      const int s = c + r * W;
-      xs[s] = (bs[s] + cxs[s] * xs[s - 1] + cxs[s + 1] * xs[s + 1] + cys[s] * xs[s - W] + cys[s + W] * xs[s + W]) * is[s];
     }
+    const int s = c + r * W;
+    xs[s] = (bs[s] + cxs[s] * xs[s - 1] + cxs[s + 1] * xs[s + 1] + cys[s] * xs[s - W] + cys[s + W] * xs[s + W]) * is[s];
   }
 }
 
@@ -396,8 +384,13 @@ __device__ __forceinline__ void window_halves(T* sm, int i0, int j0, int nI, int
 
 template <typename T, int NS>
 constexpr size_t pre_smem() {
-  return sweep_smem<T, 2 * NS + 1, true>();
+  return sweep_smem<T, 2 * NS + 1, false>();
 }
+
+// The diagonal from its staged reciprocal (the residual after pre-smoothing;
+// keeps dg out of shared memory).
+__device__ __forceinline__ float diag_of(float idg) { return __frcp_rn(idg); }
+__device__ __forceinline__ double diag_of(double idg) { return __drcp_rn(idg); }
 template <typename T, int NS>
 constexpr size_t post_smem() {
   return sweep_smem<T, 2 * NS, false>();
@@ -405,7 +398,8 @@ constexpr size_t post_smem() {
 
 // Pre-smoothing: NS red-black sweeps (red first) from x = 0, then the residual
 // of the red cells (the black ones are zero after the last black half sweep)
-// averaged into the coarse right-hand side.  x is written to xout.
+// averaged into the coarse right-hand side, with the diagonal recovered from
+// 1/dg.  x is written to xout.
 template <typename T, int NS>
 __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C, T* __restrict__ xout, const int* __restrict__ done) {
   if (*done) return;
@@ -415,10 +409,10 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C,
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int i0 = blockIdx.x * TXS, j0 = blockIdx.y * TYS;
-  stage_window<T, H, false, false, true>(L, C, sm, i0, j0);
+  stage_window<T, H, false, false, false>(L, C, sm, i0, j0);
   __syncthreads();
   window_halves<T, H, 1, 2 * NS, 0>(sm, i0, j0, L.nI, L.nJ);
-  const T *xs = sm, *bs = sm + N, *cxs = sm + 3 * N, *cys = sm + 4 * N, *ds = sm + 5 * N;
+  const T *xs = sm, *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N;
   T acc = 0;
 #pragma unroll
   for (int dr = 0; dr < 2; ++dr)
@@ -430,7 +424,7 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C,
       const int s = (ti + H) + (tj + H) * W;
       xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
       if (!((gi + gj) & 1)) {  // red cells: black residuals are zero after the black half sweep
-        T ax = ds[s] * xs[s] - cxs[s] * xs[s - 1] - cxs[s + 1] * xs[s + 1] - cys[s] * xs[s - W] - cys[s + W] * xs[s + W];
+        T ax = diag_of(is[s]) * xs[s] - cxs[s] * xs[s - 1] - cxs[s + 1] * xs[s + 1] - cys[s] * xs[s - W] - cys[s + W] * xs[s + W];
         acc += bs[s] - ax;
       }
     }
@@ -756,9 +750,8 @@ __global__ void k_jacobi(Level<T> L, const T* __restrict__ r, T* __restrict__ z,
                          unsigned* __restrict__ counter, const int* __restrict__ done) {
   if (*done) return;
   Acc<T> acc;
-  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)L.nI * L.nJ; t += (size_t)gridDim.x * blockDim.x) {
-    int i, j;
-    size_t k = cell_index(L, t, i, j);
+  for (size_t k = (size_t)L.ld + blockIdx.x * (size_t)blockDim.x + threadIdx.x, k_end = (size_t)L.ld * (L.nJ + 1); k < k_end;
+       k += (size_t)gridDim.x * blockDim.x) {  // flat over the padded rows: r and 1/dg are zero on the ring
     T zv = r[k] * L.idg[k];
     z[k] = zv;
     acc.add(r[k] * zv);
@@ -1042,10 +1035,10 @@ template <typename T>
 void build_hierarchy(cudaStream_t s, Hierarchy<T>& H, const gb2d_ctx* c, double* b64, double* ainv) {
   double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
   Level<T>& L0 = H.L[0];
-  k_build_level0<T><<<nblocks((size_t)L0.nI * L0.nJ, 1216), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, L0, b64, idx2, idy2);
+  k_build_level0<T><<<grid_ij(L0.nI, L0.nJ), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, L0, b64, idx2, idy2);
   GB_LAUNCHED(1);
   for (int l = 1; l < H.nlev; ++l) {
-    k_coarsen<T><<<nblocks((size_t)H.L[l].nI * H.L[l].nJ, 1216), kThreads, 0, s>>>(H.L[l - 1], H.L[l]);
+    k_coarsen<T><<<grid_ij(H.L[l].nI, H.L[l].nJ), kThreads, 0, s>>>(H.L[l - 1], H.L[l]);
     GB_LAUNCHED(1);
   }
   k_dense_inverse<T><<<1, 1024, 0, s>>>(H.L[H.nlev - 1], ainv);
@@ -1056,7 +1049,7 @@ void build_hierarchy(cudaStream_t s, Hierarchy<T>& H, const gb2d_ctx* c, double*
 void build_level0_f64(cudaStream_t s, Hierarchy<double>& H, const gb2d_ctx* c, double* b64) {
   double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
   Level<double>& L0 = H.L[0];
-  k_build_level0<double><<<nblocks((size_t)L0.nI * L0.nJ, 1216), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, L0, b64, idx2, idy2);
+  k_build_level0<double><<<grid_ij(L0.nI, L0.nJ), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, L0, b64, idx2, idy2);
   GB_LAUNCHED(1);
 }
 
@@ -1400,7 +1393,7 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
   if (prec && use_mg) build_hierarchy<float>(s, S->h32, c, nullptr, S->ainv32);
   if (prec && !use_mg) {
     double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
-    k_build_level0<float><<<nblocks((size_t)c->grid.ni * c->grid.nj, 1216), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, S->h32.L[0], nullptr,
+    k_build_level0<float><<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, S->h32.L[0], nullptr,
                                                                                                 idx2, idy2);
     GB_LAUNCHED(1);
   }
