@@ -3,7 +3,7 @@
 // Included by gb2d_solver.cu inside its anonymous namespace (uses Level, Scalars,
 // block_sum, publish_rz, kMaxLevels, kCoarseMax).
 //
-// Every level from the cluster's top level (a few 10^4 cells) down to the dense
+// Every level from the cluster's top level (at most 128^2 cells) down to the dense
 // coarse solve runs inside one launch of a cluster of P CTAs (16 where the part
 // allows it, else 8), each CTA one SM with 1024 threads:
 //
@@ -32,6 +32,10 @@ constexpr int kCtMaxLevels = 10;
 constexpr int kCtMinRows = 4;           // rows per CTA on the coarsest distributed level
 constexpr int kCtOwnerRows = 256;       // rows of the bottom distributed level (owner table)
 constexpr size_t kCtSmemCap = 220 * 1024;
+// Largest top level: a 256^2 FP32 level fits in the cluster's shared memory, but
+// measured at 1024^2 the projection is faster with 256^2 in the tiled kernels
+// (one launch per smoothing side, no cluster barriers) and the cluster from 128^2.
+constexpr int kCtMaxTopCells = 128 * 128;
 
 template <typename T>
 struct CtLevel {

@@ -894,6 +894,7 @@ bool plan_ctail(Hierarchy<T>& H, int P) {
   const int nl = H.nlev;
   for (int top = 0; top < nl - 1; ++top) {
     if (nl - top > kCtMaxLevels) continue;
+    if (H.L[top].nI * H.L[top].nJ > kCtMaxTopCells) continue;
     int lb = top - 1;
     while (lb + 1 < nl - 1 && H.L[lb + 1].nJ >= P * kCtMinRows) ++lb;
     if (lb < top || H.L[lb].nJ > kCtOwnerRows) continue;
