@@ -131,6 +131,9 @@ void free_ctx(gb2d_ctx* c) {
     delete[] c->probe.bytes_each;
   }
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  if (c->side) cudaStreamDestroy(c->side);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
   delete c;
 }
 
@@ -168,6 +171,9 @@ int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out
   c->ys = make_space(ni, nj + 1, grid->x_min, grid->y_min - 0.5 * c->base.dy, grid->x_max, grid->y_max + 0.5 * c->base.dy);
   cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
   c->stream = c->own_stream;
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
   struct A {
     double** p;
     size_t n;
@@ -441,13 +447,27 @@ int gb2d_curvature(gb2d_ctx* c) {
   return read_flag(c);
 }
 
+// Curvature and the jump-system assembly: the curvature runs on the side stream
+// while the face weights (which do not need it) run on the context stream.
+static int curvature_and_assemble(gb2d_ctx* c, double dt) {
+  double* phi = c->phi_buf[c->phi_cur];
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->flag, 0, sizeof(int), c->stream));
+  launch_extrapolate_ghosts(c->stream, phi, 2, c->grid.ni, c->grid.nj);
+  GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_fork, c->stream));
+  GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+  launch_curvature(c->side, c, phi, c->kappa, &c->sc->flag);
+  GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
+  launch_faces(c->stream, c, phi, dt);
+  GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+  launch_rhs_diag(c->stream, c, phi, dt);
+  return check_launch(c, "assemble");
+}
+
 int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
   if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
   double* phi = c->phi_buf[c->phi_cur];
-  int rc = curvature_impl(c);
+  int rc = curvature_and_assemble(c, dt);
   if (rc) return rc;
-  launch_assemble(c->stream, c, phi, dt);
-  if ((rc = check_launch(c, "assemble"))) return rc;
   gb2d_solve_stats local;
   memset(&local, 0, sizeof local);
   int src = solver_solve(c, c->rhs, c->p, o, &local);
@@ -467,10 +487,8 @@ int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve
 
 int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {
   if (!c || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
-  int rc = curvature_impl(c);
+  int rc = curvature_and_assemble(c, dt);
   if (rc) return rc;
-  launch_assemble(c->stream, c, c->phi_buf[c->phi_cur], dt);
-  if ((rc = check_launch(c, "assemble"))) return rc;
   size_t ni = c->grid.ni, nj = c->grid.nj;
   if (bx) GB2D_CUDA_TRY(c, cudaMemcpyAsync(bx, c->bx, (ni + 1) * nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   if (by) GB2D_CUDA_TRY(c, cudaMemcpyAsync(by, c->by, ni * (nj + 1) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

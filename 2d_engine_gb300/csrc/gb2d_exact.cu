@@ -540,10 +540,15 @@ void launch_curvature(cudaStream_t s, const gb2d_ctx* c, const double* phi, doub
   GB_LAUNCHED(1);
 }
 
-void launch_assemble(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt) {
+void launch_faces(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt) {
   AsmArgs a = asm_args(c, dt);
   k_faces<<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(phi, c->bx, c->by, a);
   GB_LAUNCHED(1);
+}
+
+// Needs the face weights and the curvature.
+void launch_rhs_diag(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt) {
+  AsmArgs a = asm_args(c, dt);
   k_rhs_diag<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, c->kappa, c->u, c->v, c->bx, c->by, c->diag, c->rhs, a);
   GB_LAUNCHED(1);
 }

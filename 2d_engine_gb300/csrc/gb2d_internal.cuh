@@ -90,6 +90,8 @@ struct gb2d_ctx {
   gb2d::Space base, xs, ys;
   cudaStream_t stream;
   cudaStream_t own_stream;
+  cudaStream_t side;              // second stream for independent setup branches
+  cudaEvent_t ev_fork, ev_join;   // fork / join of the side stream
   gb2d::Probe probe;
   // Level-set buffers (ghost 2): current index into phi_buf.
   double* phi_buf[4];
@@ -119,7 +121,8 @@ void launch_reinit_sweep(cudaStream_t s, const gb2d_ctx* c, const double* src, d
 void launch_blend(cudaStream_t s, const gb2d_ctx* c, const double* keep, double* phi, double c0, double c1);
 void launch_eno3(cudaStream_t s, const gb2d_ctx* c, double dt);
 void launch_curvature(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* kappa, int* flag);
-void launch_assemble(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt);
+void launch_faces(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt);
+void launch_rhs_diag(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt);
 void launch_poisson_apply_exact(cudaStream_t s, const gb2d_ctx* c, const double* x, double* y);
 void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt, Scalars* sc);
 void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst, int gd, int nI, int nJ);

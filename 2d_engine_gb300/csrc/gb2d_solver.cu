@@ -82,70 +82,111 @@ __device__ double sum_partials(const double* part, int n) {
 
 __device__ __forceinline__ unsigned block_linear() { return blockIdx.x + blockIdx.y * gridDim.x; }
 
+// Exact FP32 -> FP64 (every FP32 value is an FP64 value); FP32 subnormals, below
+// 1.2e-38, become signed zero.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  unsigned long long bits = (unsigned long long)(u >> 31) << 63;
+  if (e != 0u) {
+    const unsigned long long E = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
+    bits |= (E << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+  }
+  return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double widen(double d) { return d; }
+
+// FP64 -> FP32 by truncation of the significand (the preconditioner's input
+// only); magnitudes below the FP32 normal range become signed zero, above it
+// infinity.
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned s = (unsigned)(b >> 63) << 31;
+  const int E = (int)((b >> 52) & 0x7ffull);
+  const int e = E - 896;
+  unsigned bits;
+  if (E == 0x7ff)
+    bits = s | 0x7f800000u | (unsigned)((b >> 29) & 0x7fffffull) | ((b & 0xfffffffffffffull) ? 0x400000u : 0u);
+  else if (e <= 0)
+    bits = s;
+  else if (e >= 255)
+    bits = s | 0x7f800000u;
+  else
+    bits = s | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffull);
+  return __uint_as_float(bits);
+}
+
 // ---- level construction -----------------------------------------------------
+
+// The FP64 inputs in the hierarchy's precision: FP32 levels are built in FP32
+// arithmetic from truncated inputs (preconditioner data; FP64 divides and
+// conversions would take the scarce FP64 issue slots).
+__device__ __forceinline__ float in_prec(double v, float) { return narrow(v); }
+__device__ __forceinline__ double in_prec(double v, double) { return v; }
 
 // Level 0 from the assembled FP64 system: conductances beta/dx^2 on interior
 // faces, zero on walls; diagonal as assembled; shift = pin + (dx != dy) terms.
 template <typename T>
 __global__ void k_build_level0(const double* __restrict__ bx, const double* __restrict__ by, const double* __restrict__ diag,
-                               const double* __restrict__ rhs, Level<T> L, double* __restrict__ b64, double idx2, double idy2) {
+                               const double* __restrict__ rhs, Level<T> L, double* __restrict__ b64, double idx2_, double idy2_) {
   int ni = L.nI, nj = L.nJ;
+  const T idx2 = in_prec(idx2_, T()), idy2 = in_prec(idy2_, T()), zero = 0;
   GB_FOR_IJ(i, j, ni, nj) {
     const size_t t = (size_t)j * ni + i;
     const size_t k = (size_t)(i + 1) + (size_t)(j + 1) * L.ld;
-    double bl = bx[i + (size_t)j * (ni + 1)];
-    double bb = by[i + (size_t)j * ni], bt = by[i + (size_t)(j + 1) * ni];
-    double cl = i > 0 ? bl * idx2 : 0.0, cb = j > 0 ? bb * idy2 : 0.0;
-    L.cx[k] = (T)cl;
-    L.cy[k] = (T)cb;
-    if (i == ni - 1) L.cx[k + 1] = (T)0;
-    if (j == nj - 1) L.cy[k + L.ld] = (T)0;
-    double d = diag[t];
-    L.dg[k] = (T)d;
-    L.idg[k] = (T)(1.0 / d);
-    double ybeta = (j > 0 ? bb : 0.0) + (j < nj - 1 ? bt : 0.0);
-    double pin = (i == 0 && j == 0) ? (bl + bb) : 0.0;
-    L.sh[k] = (T)(pin * idx2 + ybeta * (idx2 - idy2));
+    const T bl = in_prec(bx[i + (size_t)j * (ni + 1)], T());
+    const T bb = in_prec(by[i + (size_t)j * ni], T()), bt = in_prec(by[i + (size_t)(j + 1) * ni], T());
+    L.cx[k] = i > 0 ? bl * idx2 : zero;
+    L.cy[k] = j > 0 ? bb * idy2 : zero;
+    if (i == ni - 1) L.cx[k + 1] = zero;
+    if (j == nj - 1) L.cy[k + L.ld] = zero;
+    const T d = in_prec(diag[t], T());
+    L.dg[k] = d;
+    L.idg[k] = (T)1 / d;
+    const T ybeta = (j > 0 ? bb : zero) + (j < nj - 1 ? bt : zero);
+    const T pin = (i == 0 && j == 0) ? (bl + bb) : zero;
+    L.sh[k] = pin * idx2 + ybeta * (idx2 - idy2);
     if (b64) b64[k] = rhs[t];
-
   }
 }
 
 // Coarse level: cell (I, J) covers fine cells (2I..2I+1, 2J..2J+1) that exist.
 // Face conductances: sum of the two fine faces / 8 (face-averaged weight over
-// the doubled spacing); shift: average of the children's shifts.
+// the doubled spacing); shift: average of the children's shifts.  In the
+// level's precision.
 template <typename T>
 __global__ void k_coarsen(Level<T> F, Level<T> C) {
   int cI = C.nI, cJ = C.nJ;
+  const T eighth = (T)0.125, zero = 0;
   GB_FOR_IJ(I, J, cI, cJ) {
     const size_t k = (size_t)(I + 1) + (size_t)(J + 1) * C.ld;
-    auto fx = [&](int fi, int fj) -> double {  // fine x-face fi at fine row fj (0 outside)
-      if (fj >= F.nJ) return 0.0;
-      return (double)F.cx[(size_t)(fi + 1) + (size_t)(fj + 1) * F.ld];
+    auto fx = [&](int fi, int fj) -> T {  // fine x-face fi at fine row fj (0 outside)
+      if (fj >= F.nJ) return zero;
+      return F.cx[(size_t)(fi + 1) + (size_t)(fj + 1) * F.ld];
     };
-    auto fy = [&](int fi, int fj) -> double {
-      if (fi >= F.nI) return 0.0;
-      return (double)F.cy[(size_t)(fi + 1) + (size_t)(fj + 1) * F.ld];
+    auto fy = [&](int fi, int fj) -> T {
+      if (fi >= F.nI) return zero;
+      return F.cy[(size_t)(fi + 1) + (size_t)(fj + 1) * F.ld];
     };
-    double cl = I > 0 ? (fx(2 * I, 2 * J) + fx(2 * I, 2 * J + 1)) / 8.0 : 0.0;
-    double cr = I < cI - 1 ? (fx(2 * I + 2, 2 * J) + fx(2 * I + 2, 2 * J + 1)) / 8.0 : 0.0;
-    double cb = J > 0 ? (fy(2 * I, 2 * J) + fy(2 * I + 1, 2 * J)) / 8.0 : 0.0;
-    double ct = J < cJ - 1 ? (fy(2 * I, 2 * J + 2) + fy(2 * I + 1, 2 * J + 2)) / 8.0 : 0.0;
-    double s = 0.0;
+    const T cl = I > 0 ? (fx(2 * I, 2 * J) + fx(2 * I, 2 * J + 1)) * eighth : zero;
+    const T cr = I < cI - 1 ? (fx(2 * I + 2, 2 * J) + fx(2 * I + 2, 2 * J + 1)) * eighth : zero;
+    const T cb = J > 0 ? (fy(2 * I, 2 * J) + fy(2 * I + 1, 2 * J)) * eighth : zero;
+    const T ct = J < cJ - 1 ? (fy(2 * I, 2 * J + 2) + fy(2 * I + 1, 2 * J + 2)) * eighth : zero;
+    T s = 0;
     for (int b = 0; b < 2; ++b)
       for (int a = 0; a < 2; ++a) {
         int fi = 2 * I + a, fj = 2 * J + b;
-        if (fi < F.nI && fj < F.nJ) s += (double)F.sh[(size_t)(fi + 1) + (size_t)(fj + 1) * F.ld];
+        if (fi < F.nI && fj < F.nJ) s += F.sh[(size_t)(fi + 1) + (size_t)(fj + 1) * F.ld];
       }
-    s *= 0.25;
-    C.cx[k] = (T)cl;
-    C.cy[k] = (T)cb;
-    if (I == cI - 1) C.cx[k + 1] = (T)0;
-    if (J == cJ - 1) C.cy[k + C.ld] = (T)0;
-    double d = cl + cr + cb + ct + s;
-    C.dg[k] = (T)d;
-    C.idg[k] = (T)(1.0 / d);
-    C.sh[k] = (T)s;
+    s *= (T)0.25;
+    C.cx[k] = cl;
+    C.cy[k] = cb;
+    if (I == cI - 1) C.cx[k + 1] = zero;
+    if (J == cJ - 1) C.cy[k + C.ld] = zero;
+    const T d = cl + cr + cb + ct + s;
+    C.dg[k] = d;
+    C.idg[k] = (T)1 / d;
+    C.sh[k] = s;
   }
 }
 
@@ -607,40 +648,6 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(TailArgs<T> a, const doub
 // per SM), so each kernel does at most a handful per cell; FP32 <-> FP64 moves
 // are bit manipulations on the integer pipes.
 
-// Exact FP32 -> FP64 (every FP32 value is an FP64 value); FP32 subnormals, below
-// 1.2e-38, become signed zero.
-__device__ __forceinline__ double widen(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  unsigned long long bits = (unsigned long long)(u >> 31) << 63;
-  if (e != 0u) {
-    const unsigned long long E = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
-    bits |= (E << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
-  }
-  return __longlong_as_double((long long)bits);
-}
-__device__ __forceinline__ double widen(double d) { return d; }
-
-// FP64 -> FP32 by truncation of the significand (the preconditioner's input
-// only); magnitudes below the FP32 normal range become signed zero, above it
-// infinity.
-__device__ __forceinline__ float narrow(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned s = (unsigned)(b >> 63) << 31;
-  const int E = (int)((b >> 52) & 0x7ffull);
-  const int e = E - 896;
-  unsigned bits;
-  if (E == 0x7ff)
-    bits = s | 0x7f800000u | (unsigned)((b >> 29) & 0x7fffffull) | ((b & 0xfffffffffffffull) ? 0x400000u : 0u);
-  else if (e <= 0)
-    bits = s;
-  else if (e >= 255)
-    bits = s | 0x7f800000u;
-  else
-    bits = s | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffull);
-  return __uint_as_float(bits);
-}
-
 // The CG kernels below run flat over the padded rows 1..nJ, ghost columns
 // included: every vector here is zero on the padding ring and so are the
 // padded coefficients (wall conductances are zero), so ghost entries stay zero
@@ -680,6 +687,36 @@ __global__ void k_reduce_two(const double* __restrict__ pa, const double* __rest
   }
 }
 
+// Pairs of neighbouring elements of the padded rows 1..nJ, 16-byte aligned:
+// the pair loop starts at the even index at or below ld and ends at the even
+// index at or above ld (nJ + 1); the extra elements are ghosts (zero).
+#define GB_FLAT_PAIRS(L, k)                                                                                   \
+  for (size_t k = ((size_t)(L).ld & ~(size_t)1) + 2 * (blockIdx.x * (size_t)blockDim.x + threadIdx.x),        \
+              k##_end = ((size_t)(L).ld * ((L).nJ + 1) + 1) & ~(size_t)1;                                    \
+       k < k##_end; k += 2 * (size_t)gridDim.x * blockDim.x)
+
+template <typename T>
+struct Pair;
+template <>
+struct Pair<float> {
+  using V = float2;
+};
+template <>
+struct Pair<double> {
+  using V = double2;
+};
+template <typename T>
+__device__ __forceinline__ typename Pair<T>::V ld2(const T* a, size_t k) {
+  return *reinterpret_cast<const typename Pair<T>::V*>(a + k);
+}
+template <typename T>
+__device__ __forceinline__ void st2(T* a, size_t k, T v0, T v1) {
+  typename Pair<T>::V v;
+  v.x = v0;
+  v.y = v1;
+  *reinterpret_cast<typename Pair<T>::V*>(a + k) = v;
+}
+
 // p = z + beta p (p = z when first).  z is the preconditioner's output in its
 // precision; one FP64 operation per cell.
 template <typename TZ>
@@ -687,20 +724,43 @@ __global__ void k_direction(Level<double> L, const TZ* __restrict__ z, double* _
                             const int* __restrict__ done) {
   if (*done) return;
   const double bt = first ? 0.0 : sc->beta;
-  GB_FLAT_FOR(L, k) { p[k] = first ? widen(z[k]) : widen(z[k]) + bt * p[k]; }
+  GB_FLAT_PAIRS(L, k) {
+    const auto zv = ld2(z, k);
+    if (first) {
+      st2(p, k, widen(zv.x), widen(zv.y));
+    } else {
+      const double2 pv = ld2(p, k);
+      st2(p, k, widen(zv.x) + bt * pv.x, widen(zv.y) + bt * pv.y);
+    }
+  }
 }
 
 // Ap = A p (reference entries) and p.Ap; the last block publishes
-// alpha = rz_new / p.Ap and rz_cur = rz_new.
+// alpha = rz_new / p.Ap and rz_cur = rz_new.  With an even row length two
+// neighbouring cells per thread (16-byte loads), else one.
 __global__ void k_apply_pap(Level<double> L, const double* __restrict__ p, double* __restrict__ ap, Scalars* sc, double* __restrict__ part,
                             unsigned* __restrict__ counter, const int* __restrict__ done) {
   if (*done) return;
   double acc = 0.0;
-  GB_FLAT_FOR(L, k) {
-    const double pc = p[k];
-    double y = L.dg[k] * pc - L.cx[k] * p[k - 1] - L.cx[k + 1] * p[k + 1] - L.cy[k] * p[k - L.ld] - L.cy[k + L.ld] * p[k + L.ld];
-    ap[k] = y;
-    acc += pc * y;
+  const size_t ld = L.ld;
+  if ((ld & 1) == 0) {
+    GB_FLAT_PAIRS(L, k) {
+      const double2 pc = ld2(p, k), pb = ld2(p, k - ld), pt = ld2(p, k + ld);
+      const double2 dg = ld2(L.dg, k), cx = ld2(L.cx, k), cy = ld2(L.cy, k), cyt = ld2(L.cy, k + ld);
+      const double pl = p[k - 1], pr = p[k + 2], cx2 = L.cx[k + 2];
+      const double y0 = dg.x * pc.x - cx.x * pl - cx.y * pc.y - cy.x * pb.x - cyt.x * pt.x;
+      const double y1 = dg.y * pc.y - cx.y * pc.x - cx2 * pr - cy.y * pb.y - cyt.y * pt.y;
+      st2(ap, k, y0, y1);
+      acc += pc.x * y0;
+      acc += pc.y * y1;
+    }
+  } else {
+    GB_FLAT_FOR(L, k) {
+      const double pc = p[k];
+      double y = L.dg[k] * pc - L.cx[k] * p[k - 1] - L.cx[k + 1] * p[k + 1] - L.cy[k] * p[k - L.ld] - L.cy[k + L.ld] * p[k + L.ld];
+      ap[k] = y;
+      acc += pc * y;
+    }
   }
   double pap;
   if (last_block_sum(acc, part, gridDim.x, counter, &pap) && threadIdx.x == 0) {
@@ -713,7 +773,7 @@ __global__ void k_apply_pap(Level<double> L, const double* __restrict__ p, doubl
 // x += alpha p;  r -= alpha Ap;  the preconditioner's copy of r (FP32: rT; FP64:
 // r is read in place);  ||r||^2 (from the FP32 copy when there is one).  The
 // last block stores ||r||^2 for the host and raises the done flag at the
-// threshold (or on a non-finite value).
+// threshold (or on a non-finite value).  Two neighbouring cells per thread.
 template <typename T>
 __global__ void k_update(Level<double> L, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
                          const double* __restrict__ ap, T* __restrict__ rT, Scalars* sc, double* __restrict__ part,
@@ -721,16 +781,19 @@ __global__ void k_update(Level<double> L, double* __restrict__ x, double* __rest
   if (*done) return;
   const double al = sc->alpha;
   Acc<T> acc;
-  GB_FLAT_FOR(L, k) {
-    x[k] += al * p[k];
-    const double rn = r[k] - al * ap[k];
-    r[k] = rn;
+  GB_FLAT_PAIRS(L, k) {
+    const double2 pv = ld2(p, k), av = ld2(ap, k), xv = ld2(x, k), rv = ld2(r, k);
+    st2(x, k, xv.x + al * pv.x, xv.y + al * pv.y);
+    const double r0 = rv.x - al * av.x, r1 = rv.y - al * av.y;
+    st2(r, k, r0, r1);
     if constexpr (sizeof(T) == 4) {
-      const float rf = narrow(rn);
-      rT[k] = rf;
-      acc.add(rf * rf);
+      const float f0 = narrow(r0), f1 = narrow(r1);
+      st2(rT, k, f0, f1);
+      acc.add(f0 * f0);
+      acc.add(f1 * f1);
     } else {
-      acc.add(rn * rn);
+      acc.add(r0 * r0);
+      acc.add(r1 * r1);
     }
   }
   double rr;
@@ -1391,7 +1454,15 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
     build_level0_f64(s, S->h64, c, S->b64);
   else
     build_hierarchy<double>(s, S->h64, c, S->b64, S->ainv64);
-  if (prec && use_mg) build_hierarchy<float>(s, S->h32, c, nullptr, S->ainv32);
+  if (prec && use_mg) {
+    // The FP32 hierarchy (its dense coarse inverse keeps one SM busy) builds on
+    // the side stream while the FP64 residual runs; joined before the first V-cycle.
+    cudaEventRecord(c->ev_fork, s);
+    cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+    build_hierarchy<float>(c->side, S->h32, c, nullptr, S->ainv32);
+    cudaEventRecord(c->ev_join, c->side);
+  }
+  bool joined = !(prec && use_mg);
   if (prec && !use_mg) {
     double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
     k_build_level0<float><<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, S->h32.L[0], nullptr,
@@ -1429,6 +1500,10 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
     }
     double rr_in = rr;
     int it;
+    if (!joined) {
+      cudaStreamWaitEvent(s, c->ev_join, 0);
+      joined = true;
+    }
     if (prec)
       it = inner_pcg<float>(c, S, S->h32, S->ainv32, x, thr2, max_it - total, prec, use_mg, nu, &rr_in);
     else
@@ -1446,6 +1521,7 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
       break;
     }
   }
+  if (!joined) cudaStreamWaitEvent(s, c->ev_join, 0);  // later work on the context stream follows the side build
   if (st) {
     st->iterations = total;
     st->outer_iterations = outer;
