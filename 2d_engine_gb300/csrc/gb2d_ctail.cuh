@@ -161,6 +161,7 @@ __device__ __forceinline__ void ct_prolong(const CtView<T>& f, const CtLevel<T>&
 
 template <typename T>
 __global__ void __launch_bounds__(kCtThreads, 1) k_ctail(CtArgs<T> a, const double* __restrict__ ainv, int nu, const int* __restrict__ done) {
+  pdl_enter();
   if (*done) return;  // uniform over the cluster: no CTA reaches a cluster barrier
   cgx::cluster_group cl = cgx::this_cluster();
   const int P = (int)cl.num_blocks();

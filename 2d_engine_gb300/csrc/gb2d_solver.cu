@@ -35,6 +35,7 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <utility>
 
 #include "gb2d_internal.cuh"
 
@@ -81,6 +82,16 @@ __device__ double sum_partials(const double* part, int n) {
 }
 
 __device__ __forceinline__ unsigned block_linear() { return blockIdx.x + blockIdx.y * gridDim.x; }
+
+// Programmatic dependent launch inside the solver's launch chains: wait until the
+// previous kernel in the stream has completed (its writes visible), then let the
+// next kernel start launching, so launch latency and block scheduling overlap
+// this kernel's tail instead of following it.  Both are no-ops for kernels
+// launched without the programmatic-serialization attribute.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
 
 // Exact FP32 -> FP64 (every FP32 value is an FP64 value); FP32 subnormals, below
 // 1.2e-38, become signed zero.
@@ -443,6 +454,7 @@ constexpr size_t post_smem() {
 // 1/dg.  x is written to xout.
 template <typename T, int NS>
 __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C, T* __restrict__ xout, const int* __restrict__ done) {
+  pdl_enter();
   if (*done) return;
   constexpr int H = 2 * NS + 1;
   using Wn = Win<T, H>;
@@ -479,6 +491,7 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C,
 template <typename T, int NS>
 __global__ void __launch_bounds__(BXT* BYT) k_post_smooth(Level<T> L, Level<T> C, T* __restrict__ xout, double* __restrict__ part_rz,
                                                          unsigned* __restrict__ counter, Scalars* sc, const int* __restrict__ done) {
+  pdl_enter();
   if (*done) return;
   constexpr int H = 2 * NS;
   using Wn = Win<T, H>;
@@ -545,6 +558,7 @@ __device__ __forceinline__ void tail_half(const Level<T>& L, const TailLevel<T>&
 
 template <typename T>
 __global__ void __launch_bounds__(kTailThreads) k_tail(TailArgs<T> a, const double* __restrict__ ainv, int nu, const int* __restrict__ done) {
+  pdl_enter();
   if (*done) return;
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
@@ -722,6 +736,7 @@ __device__ __forceinline__ void st2(T* a, size_t k, T v0, T v1) {
 template <typename TZ>
 __global__ void k_direction(Level<double> L, const TZ* __restrict__ z, double* __restrict__ p, const Scalars* sc, int first,
                             const int* __restrict__ done) {
+  pdl_enter();
   if (*done) return;
   const double bt = first ? 0.0 : sc->beta;
   GB_FLAT_PAIRS(L, k) {
@@ -740,6 +755,7 @@ __global__ void k_direction(Level<double> L, const TZ* __restrict__ z, double* _
 // neighbouring cells per thread (16-byte loads), else one.
 __global__ void k_apply_pap(Level<double> L, const double* __restrict__ p, double* __restrict__ ap, Scalars* sc, double* __restrict__ part,
                             unsigned* __restrict__ counter, const int* __restrict__ done) {
+  pdl_enter();
   if (*done) return;
   double acc = 0.0;
   const size_t ld = L.ld;
@@ -778,6 +794,7 @@ template <typename T>
 __global__ void k_update(Level<double> L, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
                          const double* __restrict__ ap, T* __restrict__ rT, Scalars* sc, double* __restrict__ part,
                          unsigned* __restrict__ counter, int* __restrict__ done, double* __restrict__ host_rr) {
+  pdl_enter();
   if (*done) return;
   const double al = sc->alpha;
   Acc<T> acc;
@@ -811,6 +828,7 @@ __global__ void k_update(Level<double> L, double* __restrict__ x, double* __rest
 template <typename T>
 __global__ void k_jacobi(Level<T> L, const T* __restrict__ r, T* __restrict__ z, Scalars* sc, double* __restrict__ part_rz,
                          unsigned* __restrict__ counter, const int* __restrict__ done) {
+  pdl_enter();
   if (*done) return;
   Acc<T> acc;
   for (size_t k = (size_t)L.ld + blockIdx.x * (size_t)blockDim.x + threadIdx.x, k_end = (size_t)L.ld * (L.nJ + 1); k < k_end;
@@ -1067,17 +1085,19 @@ void launch_ctail(cudaStream_t s, const Hierarchy<T>& H, const double* ainv, int
   CtArgs<T> a = H.ct;
   a.sc = H.ctail == 0 ? sc : nullptr;
   cudaLaunchConfig_t cfg = {};
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
   at[0].val.clusterDim.x = H.ct_P;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.gridDim = dim3(H.ct_P);
   cfg.blockDim = dim3(kCtThreads);
   cfg.dynamicSmemBytes = H.ct_smem;
   cfg.stream = s;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = 2;
   cudaLaunchKernelEx(&cfg, k_ctail<T>, a, ainv, nu, done);
 }
 
@@ -1125,13 +1145,29 @@ double smooth_bytes(const Level<T>& L) {
   return sizeof(T) * (double)L.nI * L.nJ * 6.25;
 }
 
+// Launch with programmatic stream serialization (see pdl_enter).
+template <typename... P, typename... A>
+void pdl_launch(cudaStream_t s, dim3 grid, dim3 block, size_t smem, void (*k)(P...), A&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
+
 template <typename T, int NS>
 void launch_pre(cudaStream_t s, dim3 grd, const Level<T>& L, const Level<T>& C, T* xo, const int* done) {
-  k_pre_smooth<T, NS><<<grd, dim3(BXT, BYT), pre_smem<T, NS>(), s>>>(L, C, xo, done);
+  pdl_launch(s, grd, dim3(BXT, BYT), pre_smem<T, NS>(), k_pre_smooth<T, NS>, L, C, xo, done);
 }
 template <typename T, int NS>
 void launch_post(cudaStream_t s, dim3 grd, const Level<T>& L, const Level<T>& C, T* xo, double* prz, Solver* S) {
-  k_post_smooth<T, NS><<<grd, dim3(BXT, BYT), post_smem<T, NS>(), s>>>(L, C, xo, prz, S->counter + 3, S->sc, S->done);
+  pdl_launch(s, grd, dim3(BXT, BYT), post_smem<T, NS>(), k_post_smooth<T, NS>, L, C, xo, prz, S->counter + 3, S->sc, (const int*)S->done);
 }
 
 inline bool probe_begin(Probe* pr, cudaStream_t s) {
@@ -1182,7 +1218,7 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
       off += 6 * (ta.L[l].nI + 2) * (ta.L[l].nJ + 2);
     }
     ta.sc = tail == 0 ? S->sc : nullptr;
-    k_tail<T><<<1, kTailThreads, H.tail_smem, s>>>(ta, ainv, nu, done);
+    pdl_launch(s, dim3(1), dim3(kTailThreads), H.tail_smem, k_tail<T>, ta, ainv, nu, done);
   }
   GB_LAUNCHED(1);
   for (int l = tail - 1; l >= 0; --l) {
@@ -1209,7 +1245,8 @@ void precondition(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv
   if (use_mg) {
     vcycle<T>(s, S, H, ainv, nu, pr);
   } else {
-    k_jacobi<T><<<S->G, kThreads, 0, s>>>(H.L[0], H.r, H.L[0].x, S->sc, slot(S, kSlotRz), S->counter + 2, S->done);
+    pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_jacobi<T>, H.L[0], (const T*)H.r, H.L[0].x, S->sc, slot(S, kSlotRz), S->counter + 2,
+               (const int*)S->done);
     GB_LAUNCHED(1);
   }
 }
@@ -1219,8 +1256,9 @@ template <typename T>
 void enqueue_init(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int use_mg, int nu, Probe* pr) {
   const Level<double>& L = S->h64.L[0];
   precondition<T>(s, S, H, ainv, use_mg, nu, pr);
-  k_direction<T><<<S->G, kThreads, 0, s>>>(L, H.L[0].x, S->p, S->sc, 1, S->done);
-  k_apply_pap<<<S->G, kThreads, 0, s>>>(L, S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter, S->done);
+  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_direction<T>, L, (const T*)H.L[0].x, S->p, (const Scalars*)S->sc, 1, (const int*)S->done);
+  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_apply_pap, L, (const double*)S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter,
+             (const int*)S->done);
   GB_LAUNCHED(2);
 }
 
@@ -1230,11 +1268,13 @@ template <typename T>
 void enqueue_iter(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, double* x64, int use_mg, int nu, int par, Probe* pr) {
   const Level<double>& L = S->h64.L[0];
   T* rT = sizeof(T) == 4 ? H.r : nullptr;
-  k_update<T><<<S->G, kThreads, 0, s>>>(L, x64, S->h64.r, S->p, S->ap, rT, S->sc, slot(S, kSlotRr), S->counter + 1, S->done, S->host + par);
+  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_update<T>, L, x64, S->h64.r, (const double*)S->p, (const double*)S->ap, rT, S->sc,
+             slot(S, kSlotRr), S->counter + 1, S->done, S->host + par);
   GB_LAUNCHED(1);
   precondition<T>(s, S, H, ainv, use_mg, nu, pr);
-  k_direction<T><<<S->G, kThreads, 0, s>>>(L, H.L[0].x, S->p, S->sc, 0, S->done);
-  k_apply_pap<<<S->G, kThreads, 0, s>>>(L, S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter, S->done);
+  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_direction<T>, L, (const T*)H.L[0].x, S->p, (const Scalars*)S->sc, 0, (const int*)S->done);
+  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_apply_pap, L, (const double*)S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter,
+             (const int*)S->done);
   GB_LAUNCHED(2);
 }
 
