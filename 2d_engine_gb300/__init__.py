@@ -89,6 +89,7 @@ def library():
         "gb2d_probe_read": [vp, ctypes.POINTER(i), ctypes.POINTER(d), ctypes.POINTER(d)],
         "gb2d_kernel_launches": [ctypes.POINTER(ctypes.c_ulonglong)],
         "gb2d_solver_layout": [vp, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)],
+        "gb2d_check_exact_division": [ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)],
         "gb2d_checkpoint_save": [vp],
         "gb2d_checkpoint_restore": [vp],
         "gb2d_poisson_solve_noalloc": [i, i, d, d, vp, vp, vp, vp, vp, d, i, vp, ctypes.POINTER(i), ctypes.POINTER(d)],
@@ -108,6 +109,15 @@ def kernel_launches():
     n = ctypes.c_ulonglong()
     library().gb2d_kernel_launches(ctypes.byref(n))
     return n.value
+
+
+def check_exact_division(n, seed=1):
+    """Mismatches of the FP64 division by 3 and 6 of the WENO5 kernels against IEEE division on 2n inputs."""
+    m = ctypes.c_ulonglong()
+    rc = library().gb2d_check_exact_division(n, seed, ctypes.byref(m))
+    if rc != 0:
+        raise GB2DError(rc, "gb2d_check_exact_division failed")
+    return m.value
 
 
 def _ptr(a):

@@ -327,6 +327,13 @@ int gb2d_solver_layout(gb2d_ctx* c, int precision, int* levels, int* cluster_top
   return GB2D_OK;
 }
 
+int gb2d_check_exact_division(unsigned long long n, unsigned long long seed, unsigned long long* mismatches) {
+  if (!mismatches) return GB2D_ERR_ARG;
+  int err = 0;
+  *mismatches = gb2d::check_div_by(n, seed, &err);
+  return err ? GB2D_ERR_CUDA : GB2D_OK;
+}
+
 int gb2d_kernel_launches(unsigned long long* count) {
   if (!count) return GB2D_ERR_ARG;
   *count = gb2d::g_launches;

@@ -486,7 +486,48 @@ AsmArgs asm_args(const gb2d_ctx* c, double dt) {
   return a;
 }
 
+// Self-check of div_by<3> / div_by<6> against the IEEE division: n pseudo-random
+// 64-bit patterns (every exponent, sign, NaN and infinity included) and n more
+// with exponents in the range the schemes meet; counts results whose bits differ
+// (NaN == NaN).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+  x ^= x >> 33;
+  x *= 0xff51afd7ed558ccdull;
+  x ^= x >> 33;
+  x *= 0xc4ceb9fe1a85ec53ull;
+  x ^= x >> 33;
+  return x;
+}
+__global__ void k_check_div_by(unsigned long long n, unsigned long long seed, unsigned long long* bad) {
+  unsigned long long local = 0;
+  for (unsigned long long t = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; t < 2 * n; t += (unsigned long long)gridDim.x * blockDim.x) {
+    unsigned long long b = mix64(t * 0x9e3779b97f4a7c15ull + seed);
+    if (t >= n) b = (b & 0x800fffffffffffffull) | ((unsigned long long)(1023 - 40 + (int)((b >> 52) % 80)) << 52);  // |a| in [2^-40, 2^40)
+    const double a = __longlong_as_double((long long)b);
+    const double q3 = div_by<3>(a), r3 = a / 3.0, q6 = div_by<6>(a), r6 = a / 6.0;
+    const bool ok3 = __double_as_longlong(q3) == __double_as_longlong(r3) || (isnan(q3) && isnan(r3));
+    const bool ok6 = __double_as_longlong(q6) == __double_as_longlong(r6) || (isnan(q6) && isnan(r6));
+    local += (ok3 ? 0 : 1) + (ok6 ? 0 : 1);
+  }
+  if (local) atomicAdd(bad, local);
+}
+
 }  // namespace
+
+unsigned long long check_div_by(unsigned long long n, unsigned long long seed, int* cuda_error) {
+  unsigned long long* d = nullptr;
+  unsigned long long h = ~0ull;
+  cudaError_t e = cudaMalloc(&d, sizeof h);
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof h);
+  if (e == cudaSuccess) {
+    k_check_div_by<<<152 * 8, 256>>>(n, seed, d);
+    GB_LAUNCHED(1);
+    e = cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost);
+  }
+  if (d) cudaFree(d);
+  *cuda_error = e == cudaSuccess ? 0 : 1;
+  return h;
+}
 
 void launch_fill_ghost_copy(cudaStream_t s, double* dst, int gd, const double* src, int gs, int nI, int nJ, int g) {
   k_fill_ghost_copy<<<grid_ij(nI + 2 * g, nJ + 2 * g), kThreads, 0, s>>>(dst, gd, src, gs, nI, nJ, g);

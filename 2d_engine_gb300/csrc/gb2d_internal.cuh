@@ -114,6 +114,7 @@ namespace gb2d {
 
 // ---- gb2d_exact.cu (FP64 kernels compiled without FMA contraction) ----
 void launch_fill_ghost_copy(cudaStream_t s, double* dst, int gd, const double* src, int gs, int nI, int nJ, int g);
+unsigned long long check_div_by(unsigned long long n, unsigned long long seed, int* cuda_error);
 void launch_extrapolate_ghosts(cudaStream_t s, double* f, int g, int nI, int nJ);
 void launch_weno5_advect(cudaStream_t s, const gb2d_ctx* c, const double* src, double* dst, double dt, int mixed);
 void launch_reinit_sign(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* S);

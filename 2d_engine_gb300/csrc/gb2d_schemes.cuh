@@ -8,6 +8,34 @@
 
 namespace gb2d {
 
+// a / 3 and a / 6, correctly rounded (IEEE binary64, round to nearest), in three
+// FP64 operations instead of a division: with z = RN(1/d), q = RN(a z) lies within
+// two ulps of a/d; the residual r = a - d q is then exactly representable and the
+// FMA forms it exactly; RN(q + r z) has an error below 1e-15 ulp against a/d
+// (the FMA correction step of P. Markstein, IBM J. Res. Dev. 34(1), 1990).  Since
+// a is a multiple of 2 (d = 3) or 4 (d = 6) ulps of the quotient's binade, a/d
+// sits at 0, 1/3 or 2/3 of an ulp from a representable number, never within 1/6
+// ulp of a rounding midpoint, so that RN is the correctly rounded quotient.
+// Magnitudes that could leave the normal range, zeros, infinities and NaN take
+// the division.
+template <int D>
+__device__ __forceinline__ double div_by(double a) {
+  static_assert(D == 3 || D == 6, "exact for 3 and 6");
+  constexpr double z = D == 3 ? 0.33333333333333331483 : 0.16666666666666665741;  // RN(1/D)
+  const int e = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+  if (e < 64 || e > 1984) return a / (double)D;
+  const double q = __dmul_rn(a, z);
+  const double r = __fma_rn(-q, (double)D, a);
+  return __fma_rn(r, z, q);
+}
+
+// Division by the scheme's constants 3 and 6 in the type of the expression: the
+// exact FP64 path uses div_by, FP32 divides.
+__device__ __forceinline__ double cdiv3(double a) { return div_by<3>(a); }
+__device__ __forceinline__ double cdiv6(double a) { return div_by<6>(a); }
+__device__ __forceinline__ float cdiv3(float a) { return a / 3.0f; }
+__device__ __forceinline__ float cdiv6(float a) { return a / 6.0f; }
+
 // WENO5 one-sided derivative from five first differences (ADVECTION_METHOD_2D.h:545-619).
 template <typename R>
 __device__ __forceinline__ R weno5_side(R a1, R a2, R a3, R a4, R a5, R eps) {
@@ -25,8 +53,8 @@ __device__ __forceinline__ R weno5_side(R a1, R a2, R a3, R a4, R a5, R eps) {
   R sum = al1 + al2 + al3;
   R w1 = al1 / sum, w2 = al2 / sum, w3 = al3 / sum;
   const R cm16 = R((-1.0) / 6.0);
-  return w1 * (a1 / R(3) - a2 * R(7) / R(6) + a3 * R(11) / R(6)) + w2 * (a2 * cm16 + a3 * R(5) / R(6) + a4 / R(3)) +
-         w3 * (a3 / R(3) + a4 * R(5) / R(6) - a5 / R(6));
+  return w1 * (cdiv3(a1) - cdiv6(a2 * R(7)) + cdiv6(a3 * R(11))) + w2 * (a2 * cm16 + cdiv6(a3 * R(5)) + cdiv3(a4)) +
+         w3 * (cdiv3(a3) + cdiv6(a4 * R(5)) - cdiv6(a5));
 }
 
 // Exact FP64 pair: q[0..6] are values at offsets -3..+3 (ADVECTION_METHOD_2D.h:521-543).

@@ -119,6 +119,13 @@ int gb2d_probe_read(gb2d_ctx* ctx, int* launches, double* total_ms, double* byte
 /* Kernels this library has launched in this process so far (all contexts). */
 int gb2d_kernel_launches(unsigned long long* count);
 
+/* Self-check of the exact FP64 division by 3 and 6 used in the WENO5 kernels
+ * (three FP64 operations instead of a division): compares it bit for bit with
+ * the IEEE division on 2 n pseudo-random inputs (every exponent, NaN and
+ * infinity included) and stores the number of differing results.  No
+ * counterpart in the reference (diagnostics). */
+int gb2d_check_exact_division(unsigned long long n, unsigned long long seed, unsigned long long* mismatches);
+
 /* Multigrid layout of the pressure solver for one precision (GB2D_PRECISION_FP64
  * or GB2D_PRECISION_MIXED, whose V-cycles run in FP32): the number of levels, the
  * first level handled by the thread-block-cluster tail kernel (-1 when the
