@@ -17,6 +17,18 @@ namespace {
 
 inline unsigned blocks_for(size_t n, int threads = kThreads) { return (unsigned)((n + threads - 1) / threads); }
 
+// x * y >= 0 as IEEE evaluates it.  When both are normal and finite and the
+// product's exponent keeps it above the subnormal range, only the signs decide;
+// zeros, subnormals, infinities, NaN and products that may round to zero take
+// the FP64 multiply.
+__device__ __forceinline__ bool prod_ge0(double x, double y) {
+  const long long bx = __double_as_longlong(x), by = __double_as_longlong(y);
+  const int ex = (int)((bx >> 52) & 0x7ff), ey = (int)((by >> 52) & 0x7ff);
+  if (ex != 0 && ey != 0 && ex != 0x7ff && ey != 0x7ff && ex + ey >= 972) return (bx ^ by) >= 0;
+  return x * y >= 0;
+}
+
+
 // FillGhostCellsFrom (FIELD_STRUCTURE_2D.h:374-449): interior copied, each ghost
 // layer copies the second interior line, corners untouched.
 __global__ void k_fill_ghost_copy(double* dst_a, int gd, const double* __restrict__ src_a, int gs, int nI, int nJ, int g) {
@@ -77,6 +89,7 @@ __device__ __forceinline__ void gather_y(const DField& s, int i, int j, double q
 struct LSArgs {
   int ni, nj;
   double odx, ody, eps;
+  float odx_f, ody_f, eps_f;  // the same in FP32 for the FP32 flux path
 };
 
 // WENO5th (ADVECTION_METHOD_2D.h:508-663) for the node-grid level set: writes
@@ -103,19 +116,19 @@ __global__ void k_weno5_advect(const double* __restrict__ src_a, double* __restr
   if (MIXED) {
     float m, p;
     gather_x(src, i, j, q);
-    weno5_pair_f32(q, (float)a.odx, (float)a.eps, m, p);
-    fx = u > 0 ? (double)m : (double)p;
+    weno5_pair_f32(q, a.odx_f, a.eps_f, m, p);
+    fx = gtz(u) ? widen(m) : widen(p);
     gather_y(src, i, j, q);
-    weno5_pair_f32(q, (float)a.ody, (float)a.eps, m, p);
-    fy = v > 0 ? (double)m : (double)p;
+    weno5_pair_f32(q, a.ody_f, a.eps_f, m, p);
+    fy = gtz(v) ? widen(m) : widen(p);
   } else {
     double m, p;
     gather_x(src, i, j, q);
     weno5_pair(q, a.odx, a.eps, m, p);
-    fx = u > 0 ? m : p;
+    fx = gtz(u) ? m : p;
     gather_y(src, i, j, q);
     weno5_pair(q, a.ody, a.eps, m, p);
-    fy = v > 0 ? m : p;
+    fy = gtz(v) ? m : p;
   }
   GB_AT(dst, i, j) = GB_AT(src, i, j) - dt * (u * fx + v * fy);
 }
@@ -150,11 +163,11 @@ __global__ void k_reinit_sweep(const double* __restrict__ src_a, double* __restr
   if (MIXED) {
     float mx, px, my, py, h;
     gather_x(src, i, j, q);
-    weno5_pair_f32(q, (float)a.odx, (float)a.eps, mx, px);
+    weno5_pair_f32(q, a.odx_f, a.eps_f, mx, px);
     gather_y(src, i, j, q);
-    weno5_pair_f32(q, (float)a.ody, (float)a.eps, my, py);
+    weno5_pair_f32(q, a.ody_f, a.eps_f, my, py);
     double s = __ldg(&S[i + (size_t)j * ni]);
-    if (godunov_h<float>((float)s, mx, px, my, py, h)) out = old - dtau * s * (double)h;
+    if (godunov_h<float>(narrow(s), mx, px, my, py, h)) out = old - dtau * s * widen(h);
   } else {
     double mx, px, my, py, h;
     gather_x(src, i, j, q);
@@ -204,39 +217,12 @@ __global__ void k_eno3(double* __restrict__ u_a, double* __restrict__ v_a, const
       uu = (GB_AT(ua, i, j - 1) + GB_AT(ua, i + 1, j - 1) + GB_AT(ua, i, j) + GB_AT(ua, i + 1, j)) * 0.25;
       vv = GB_AT(va, i, j);
     }
-    double fx = uu > 0 ? mx : px, fy = vv > 0 ? my : py;
+    double fx = gtz(uu) ? mx : px, fy = gtz(vv) ? my : py;
     DField out = xc ? dfield(u_a, 2, ni + 1, nj) : dfield(v_a, 2, ni, nj + 1);
     GB_AT(out, i, j) = GB_AT(out, i, j) - dt * (uu * fx + vv * fy);
   };
   GB_FOR_IJ(i, j, ni + 1, nj) face(true, i, j);
   GB_FOR_IJ(i, j, ni, nj + 1) face(false, i, j);
-}
-
-// IEEE comparisons evaluated on the integer pipes: an FP64 compare takes one of
-// the part's few FP64 issue slots (about two per clock per SM).  Exact for every
-// input, NaN and infinities included.
-constexpr long long kAbsBits = 0x7fffffffffffffffLL, kInfBits = 0x7ff0000000000000LL;
-__device__ __forceinline__ bool gt0(double x) {  // x > 0
-  const long long b = __double_as_longlong(x);
-  return b > 0 && b <= kInfBits;
-}
-__device__ __forceinline__ bool le0(double x) {  // x <= 0
-  const long long b = __double_as_longlong(x);
-  return b == 0 || (b < 0 && (b & kAbsBits) <= kInfBits);
-}
-__device__ __forceinline__ bool lt0(double x) {  // x < 0
-  const long long b = __double_as_longlong(x), m = b & kAbsBits;
-  return b < 0 && m != 0 && m <= kInfBits;
-}
-// x * y >= 0 as IEEE evaluates it.  When both are normal and finite and the
-// product's exponent keeps it above the subnormal range, only the signs decide;
-// zeros, subnormals, infinities, NaN and products that may round to zero take
-// the FP64 multiply.
-__device__ __forceinline__ bool prod_ge0(double x, double y) {
-  const long long bx = __double_as_longlong(x), by = __double_as_longlong(y);
-  const int ex = (int)((bx >> 52) & 0x7ff), ey = (int)((by >> 52) & 0x7ff);
-  if (ex != 0 && ey != 0 && ex != 0x7ff && ey != 0x7ff && ex + ey >= 972) return (bx ^ by) >= 0;
-  return x * y >= 0;
 }
 
 // ComputeCurvaturesThread with curvature_by_levelset (LEVELSET_2D.h:898-990);
@@ -290,8 +276,8 @@ struct AsmArgs {
 // 1/rho of a node.  The density takes two values, so the quotient is a select of
 // the host's correctly rounded reciprocals (FP64 divides are scarce on this part).
 __device__ __forceinline__ double inv_density(double phi, const AsmArgs& a) {
-  if (le0(phi)) return a.inv_air;
-  if (gt0(phi)) return a.inv_water;
+  if (lez(phi)) return a.inv_air;
+  if (gtz(phi)) return a.inv_water;
   return 1.0;
 }
 
@@ -331,13 +317,13 @@ __device__ __forceinline__ double jc_at(const double* kappa, int i, int j, const
 // read only on arms that cross the interface.
 __device__ __forceinline__ double arm_flux(double pc, double pn, double jcc, const double* kappa, int in, int jn, double beta, double o2,
                                            const AsmArgs& a) {
-  const bool cneg = le0(pc), nneg = le0(pn);
-  if (cneg && !nneg && gt0(pn)) {
+  const bool cneg = lez(pc), nneg = lez(pn);
+  if (cneg && !nneg && gtz(pn)) {
     double ac = fabs(pc), an = fabs(pn);
     double av = (jcc * an + jc_at(kappa, in, jn, a) * ac) / (ac + an);
     return o2 * av * beta;
   }
-  if (!cneg && gt0(pc) && nneg) {
+  if (!cneg && gtz(pc) && nneg) {
     double ac = fabs(pc), an = fabs(pn);
     double av = (jcc * an + jc_at(kappa, in, jn, a) * ac) / (ac + an);
     return -o2 * av * beta;
@@ -430,7 +416,7 @@ __global__ void k_velocity_update(const double* __restrict__ phi_a, const double
   auto face = [&](bool xc, int i, int j) {
     int in = xc ? i - 1 : i, jn = xc ? j : j - 1;
     double l0 = GB_AT(phi, i, j), ln = GB_AT(phi, in, jn);
-    double oor = le0(l0) ? a.inv_air : a.inv_water;  // 1 / rho_ij
+    double oor = lez(l0) ? a.inv_air : a.inv_water;  // 1 / rho_ij
     double dp = GB_AT(p, i, j) - GB_AT(p, in, jn);
     double od = xc ? odx : ody;
     double* w = xc ? &GB_AT(u, i, j) : &GB_AT(v, i, j);
@@ -441,9 +427,9 @@ __global__ void k_velocity_update(const double* __restrict__ phi_a, const double
       double gam = (jcn * fabs(l0) + jcc * fabs(ln)) / (fabs(l0) + fabs(ln));
       double dh = a.air + (a.water - a.air) * heaviside(0.5 * (l0 + ln), xc ? eh : ev);
       double odh = 1 / dh;
-      if (lt0(l0))
+      if (ltz(l0))
         *w -= dt * (dp + gam) * odh * od;
-      else if (gt0(l0))
+      else if (gtz(l0))
         *w -= dt * (dp - gam) * odh * od;
     }
     // max(|w|, m) as (|w| > m ? |w| : m): a NaN never replaces the maximum
@@ -468,7 +454,10 @@ __global__ void k_copy_interior(const double* __restrict__ src_a, int gs, double
 
 inline dim3 grid2d(int W, int H, dim3 blk) { return dim3((W + blk.x - 1) / blk.x, (H + blk.y - 1) / blk.y); }
 
-LSArgs ls_args(const gb2d_ctx* c) { return LSArgs{c->grid.ni, c->grid.nj, c->base.odx, c->base.ody, c->prm.weno_epsilon}; }
+LSArgs ls_args(const gb2d_ctx* c) {
+  return LSArgs{c->grid.ni, c->grid.nj, c->base.odx, c->base.ody, c->prm.weno_epsilon,
+                (float)c->base.odx, (float)c->base.ody, (float)c->prm.weno_epsilon};
+}
 
 AsmArgs asm_args(const gb2d_ctx* c, double dt) {
   AsmArgs a;

@@ -27,6 +27,44 @@ struct DField {
 __host__ __device__ inline DField dfield(double* a, int g, int nI, int nJ) { return DField{a, g, nI, nJ, nI + 2 * g}; }
 #define GB_AT(f, i, j) ((f).a[((i) + (f).g) + (size_t)((j) + (f).g) * (f).ld])
 
+// FP32 <-> FP64 moves as bit manipulations on the integer pipes (FP64 issue
+// slots, which conversions use, are scarce on this part).
+// Exact FP32 -> FP64 (every FP32 value is an FP64 value); FP32 subnormals, below
+// 1.2e-38, become signed zero.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  unsigned long long bits = (unsigned long long)(u >> 31) << 63;
+  if (e != 0u) {
+    const unsigned long long E = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
+    bits |= (E << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+  }
+  return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double widen(double d) { return d; }
+
+// FP64 -> FP32 by truncation of the significand (the preconditioner's input
+// only); magnitudes below the FP32 normal range become signed zero, above it
+// infinity.
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+  const unsigned s = (unsigned)(b >> 63) << 31;
+  const int E = (int)((b >> 52) & 0x7ffull);
+  const int e = E - 896;
+  unsigned bits;
+  if (E == 0x7ff)
+    bits = s | 0x7f800000u | (unsigned)((b >> 29) & 0x7fffffull) | ((b & 0xfffffffffffffull) ? 0x400000u : 0u);
+  else if (e <= 0)
+    bits = s;
+  else if (e >= 255)
+    bits = s | 0x7f800000u;
+  else
+    bits = s | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffull);
+  return __uint_as_float(bits);
+}
+
+// ---- level construction -----------------------------------------------------
+
 // Grid-stride loop over an nI x nJ index space on a 2D grid (x: columns, y:
 // rows): no integer division per element.
 #define GB_FOR_IJ(i, j, nI, nJ)                            \

@@ -6,7 +6,39 @@
 
 #include <cuda_runtime.h>
 
+#include "gb2d_internal.cuh"
+
 namespace gb2d {
+
+// IEEE comparisons with zero.  FP64: on the integer pipes (an FP64 compare takes
+// one of the part's few FP64 issue slots), exact for every input, NaN and
+// infinities included.  FP32: the native compare.
+constexpr long long kAbsBits = 0x7fffffffffffffffLL, kInfBits = 0x7ff0000000000000LL;
+__device__ __forceinline__ bool gtz(double x) {  // x > 0
+  const long long b = __double_as_longlong(x);
+  return b > 0 && b <= kInfBits;
+}
+__device__ __forceinline__ bool gez(double x) {  // x >= 0
+  const long long b = __double_as_longlong(x);
+  return (b >= 0 && b <= kInfBits) || b == (long long)0x8000000000000000ull;
+}
+__device__ __forceinline__ bool lez(double x) {  // x <= 0
+  const long long b = __double_as_longlong(x);
+  return b == 0 || (b < 0 && (b & kAbsBits) <= kInfBits);
+}
+__device__ __forceinline__ bool ltz(double x) {  // x < 0
+  const long long b = __double_as_longlong(x), m = b & kAbsBits;
+  return b < 0 && m != 0 && m <= kInfBits;
+}
+// |a| <= |b| (false when either is NaN), on the integer pipes.
+__device__ __forceinline__ bool abs_le(double a, double b) {
+  const long long ma = __double_as_longlong(a) & kAbsBits, mb = __double_as_longlong(b) & kAbsBits;
+  return ma <= mb && mb <= kInfBits;
+}
+__device__ __forceinline__ bool gtz(float x) { return x > 0.0f; }
+__device__ __forceinline__ bool gez(float x) { return x >= 0.0f; }
+__device__ __forceinline__ bool lez(float x) { return x <= 0.0f; }
+__device__ __forceinline__ bool ltz(float x) { return x < 0.0f; }
 
 // a / 3 and a / 6, correctly rounded (IEEE binary64, round to nearest), in three
 // FP64 operations instead of a division: with z = RN(1/d), q = RN(a z) lies within
@@ -29,12 +61,16 @@ __device__ __forceinline__ double div_by(double a) {
   return __fma_rn(r, z, q);
 }
 
-// Division by the scheme's constants 3 and 6 in the type of the expression: the
-// exact FP64 path uses div_by, FP32 divides.
+// Divisions in the type of the expression.  The exact FP64 path keeps IEEE
+// quotients (div_by for the constants 3 and 6).  The FP32 flux path is an
+// approximation of the scheme anyway: constants become reciprocal multiplies and
+// the weights use the fast division (about 2 ulp).
 __device__ __forceinline__ double cdiv3(double a) { return div_by<3>(a); }
 __device__ __forceinline__ double cdiv6(double a) { return div_by<6>(a); }
-__device__ __forceinline__ float cdiv3(float a) { return a / 3.0f; }
-__device__ __forceinline__ float cdiv6(float a) { return a / 6.0f; }
+__device__ __forceinline__ float cdiv3(float a) { return a * (1.0f / 3.0f); }
+__device__ __forceinline__ float cdiv6(float a) { return a * (1.0f / 6.0f); }
+__device__ __forceinline__ double vdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float vdiv(float a, float b) { return __fdividef(a, b); }
 
 // WENO5 one-sided derivative from five first differences (ADVECTION_METHOD_2D.h:545-619).
 template <typename R>
@@ -47,11 +83,11 @@ __device__ __forceinline__ R weno5_side(R a1, R a2, R a3, R a4, R a5, R eps) {
   R s1 = c13 * A1 * A1 + q * B1 * B1;
   R s2 = c13 * A2 * A2 + q * B2 * B2;
   R s3 = c13 * A3 * A3 + q * B3 * B3;
-  R al1 = R(1.0 / 10.0) / ((eps + s1) * (eps + s1));
-  R al2 = R(6.0 / 10.0) / ((eps + s2) * (eps + s2));
-  R al3 = R(3.0 / 10.0) / ((eps + s3) * (eps + s3));
+  R al1 = vdiv(R(1.0 / 10.0), (eps + s1) * (eps + s1));
+  R al2 = vdiv(R(6.0 / 10.0), (eps + s2) * (eps + s2));
+  R al3 = vdiv(R(3.0 / 10.0), (eps + s3) * (eps + s3));
   R sum = al1 + al2 + al3;
-  R w1 = al1 / sum, w2 = al2 / sum, w3 = al3 / sum;
+  R w1 = vdiv(al1, sum), w2 = vdiv(al2, sum), w3 = vdiv(al3, sum);
   const R cm16 = R((-1.0) / 6.0);
   return w1 * (cdiv3(a1) - cdiv6(a2 * R(7)) + cdiv6(a3 * R(11))) + w2 * (a2 * cm16 + cdiv6(a3 * R(5)) + cdiv3(a4)) +
          w3 * (cdiv3(a3) + cdiv6(a4 * R(5)) - cdiv6(a5));
@@ -66,11 +102,12 @@ __device__ __forceinline__ void weno5_pair(const double q[7], double o, double e
   dp = weno5_side<double>(d[5], d[4], d[3], d[2], d[1], eps);
 }
 
-// Mixed pair: differences of the FP64 state formed in FP64, everything after in FP32.
+// Mixed pair: differences of the FP64 state formed in FP64, everything after in
+// FP32 (the FP64 -> FP32 moves by truncation on the integer pipes).
 __device__ __forceinline__ void weno5_pair_f32(const double q[7], float o, float eps, float& dm, float& dp) {
   float d[6];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) d[k] = (float)(q[k + 1] - q[k]) * o;
+  for (int k = 0; k < 6; ++k) d[k] = narrow(q[k + 1] - q[k]) * o;
   dm = weno5_side<float>(d[0], d[1], d[2], d[3], d[4], eps);
   dp = weno5_side<float>(d[5], d[4], d[3], d[2], d[1], eps);
 }
@@ -82,31 +119,31 @@ template <typename R>
 __device__ __forceinline__ bool godunov_h(R s, R mx, R px, R my, R py, R& h) {
   R smx = s * mx, spx = s * px, smy = s * my, spy = s * py;
   int xs, ys;
-  if (spx >= 0 && smx >= 0)
+  if (gez(spx) && gez(smx))
     xs = 0;
-  else if (spx <= 0 && smx <= 0)
+  else if (lez(spx) && lez(smx))
     xs = 1;
-  else if (spx > 0 && smx < 0)
+  else if (gtz(spx) && ltz(smx))
     xs = 2;
-  else if (spx < 0 && smx > 0) {
+  else if (ltz(spx) && gtz(smx)) {
     R sss = s * (fabs(px) - fabs(mx)) / (px - mx);
-    if (sss > 0)
+    if (gtz(sss))
       xs = 0;
-    else if (sss < 0)
+    else if (ltz(sss))
       xs = 1;
     else
       return false;
   } else
     return false;
-  if (spy >= 0 && smy >= 0)
+  if (gez(spy) && gez(smy))
     ys = 0;
-  else if (spy <= 0 && smy <= 0)
+  else if (lez(spy) && lez(smy))
     ys = 1;
-  else if (spy > 0 && smy < 0)
+  else if (gtz(spy) && ltz(smy))
     ys = 2;
-  else if (spy < 0 && smy > 0) {
+  else if (ltz(spy) && gtz(smy)) {
     R ss = s * (fabs(py) - fabs(my)) / (py - my);
-    ys = (ss > 0) ? 0 : 1;
+    ys = gtz(ss) ? 0 : 1;
   } else
     return false;
   R gx = xs == 0 ? mx : px, gy = ys == 0 ? my : py;
@@ -128,24 +165,24 @@ __device__ __forceinline__ void eno3_pair(const double q[7], double o, double o2
   double d2n2 = o2 * (d1n2 - d1n3), d2n1 = o2 * (d1n1 - d1n2), d20 = o2 * (d10 - d1n1);
   double d2p1 = o2 * (d1p1 - d10), d2p2 = o2 * (d1p2 - d1p1);
   double d3n2 = o3 * (d2n1 - d2n2), d3n1 = o3 * (d20 - d2n1), d30 = o3 * (d2p1 - d20), d3p1 = o3 * (d2p2 - d2p1);
-  if (fabs(d2n1) <= fabs(d20)) {
-    if (fabs(d3n2) <= fabs(d3n1))
+  if (abs_le(d2n1, d20)) {
+    if (abs_le(d3n2, d3n1))
       dm = d1n1 + d2n1 * h + 2 * d3n2 * h * h;
     else
       dm = d1n1 + d2n1 * h + 2 * d3n1 * h * h;
   } else {
-    if (fabs(d3n1) <= fabs(d30))
+    if (abs_le(d3n1, d30))
       dm = d1n1 + d20 * h - d3n1 * h * h;
     else
       dm = d1n1 + d20 * h - d30 * h * h;
   }
-  if (fabs(d20) <= fabs(d2p1)) {
-    if (fabs(d3n1) <= fabs(d30))
+  if (abs_le(d20, d2p1)) {
+    if (abs_le(d3n1, d30))
       dp = d10 - d20 * h - d3n1 * h * h;
     else
       dp = d10 - d20 * h - d30 * h * h;
   } else {
-    if (fabs(d30) <= fabs(d3p1))
+    if (abs_le(d30, d3p1))
       dp = d10 - d2p1 * h + 2 * d30 * h * h;
     else
       dp = d10 - d2p1 * h + 2 * d3p1 * h * h;

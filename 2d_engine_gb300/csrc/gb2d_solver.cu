@@ -93,42 +93,6 @@ __device__ __forceinline__ void pdl_enter() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
-// Exact FP32 -> FP64 (every FP32 value is an FP64 value); FP32 subnormals, below
-// 1.2e-38, become signed zero.
-__device__ __forceinline__ double widen(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  unsigned long long bits = (unsigned long long)(u >> 31) << 63;
-  if (e != 0u) {
-    const unsigned long long E = e == 0xffu ? 0x7ffull : (unsigned long long)(e + 896u);
-    bits |= (E << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
-  }
-  return __longlong_as_double((long long)bits);
-}
-__device__ __forceinline__ double widen(double d) { return d; }
-
-// FP64 -> FP32 by truncation of the significand (the preconditioner's input
-// only); magnitudes below the FP32 normal range become signed zero, above it
-// infinity.
-__device__ __forceinline__ float narrow(double d) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-  const unsigned s = (unsigned)(b >> 63) << 31;
-  const int E = (int)((b >> 52) & 0x7ffull);
-  const int e = E - 896;
-  unsigned bits;
-  if (E == 0x7ff)
-    bits = s | 0x7f800000u | (unsigned)((b >> 29) & 0x7fffffull) | ((b & 0xfffffffffffffull) ? 0x400000u : 0u);
-  else if (e <= 0)
-    bits = s;
-  else if (e >= 255)
-    bits = s | 0x7f800000u;
-  else
-    bits = s | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffull);
-  return __uint_as_float(bits);
-}
-
-// ---- level construction -----------------------------------------------------
-
 // The FP64 inputs in the hierarchy's precision: FP32 levels are built in FP32
 // arithmetic from truncated inputs (preconditioner data; FP64 divides and
 // conversions would take the scarce FP64 issue slots).
