@@ -740,3 +740,170 @@ out:
   free(x);
   return rc;
 }
+
+/* ------------------------------------------------------------------------- */
+/* Rest of SolveForRK (EULERIAN_FLUID_SOLVER_2D.h:1857-1879) for air/water. */
+
+/* ApplyGraivity (EULERIAN_FLUID_SOLVER_2D.h:3249-3268): every face of both MAC
+ * grids, walls included, gains dt * gravity. */
+int or_apply_gravity(const or_grid* gr, const or_flow* fl, double* u_a, double* v_a, double dt) {
+  if (!gr || !fl || !u_a || !v_a) return OR_BAD_ARG;
+  int ni = gr->ni, nj = gr->nj;
+  double gx = dt * fl->gravity_x, gy = dt * fl->gravity_y;
+  fld u = F(u_a, 2, ni + 1, nj), v = F(v_a, 2, ni, nj + 1);
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i <= ni; ++i) AT(u, i, j) += gx;
+  for (int j = 0; j <= nj; ++j)
+    for (int i = 0; i < ni; ++i) AT(v, i, j) += gy;
+  return OR_OK;
+}
+
+/* SetupBoundaryConditionForVelocity (EULERIAN_FLUID_SOLVER_2D.h:2227-2263,
+ * air_bubble_rising): the normal velocity on the four walls is zero. */
+void or_velocity_bc(const or_grid* gr, double* u_a, double* v_a) {
+  int ni = gr->ni, nj = gr->nj;
+  fld u = F(u_a, 2, ni + 1, nj), v = F(v_a, 2, ni, nj + 1);
+  for (int j = 0; j < nj; ++j) AT(u, 0, j) = AT(u, ni, j) = 0.0;
+  for (int i = 0; i < ni; ++i) AT(v, i, 0) = AT(v, i, nj) = 0.0;
+}
+
+/* Sourcing (EULERIAN_FLUID_SOLVER_2D.h:2082-2097): DetermineDensity (:2162-2180,
+ * air_bubble_rising: air where phi <= 0, water where phi > 0; interior nodes of the
+ * ghost-2 density field), then, when fl->viscosity is set, the explicit
+ * delta-function viscosity of VISCOSITY_2D::ApplyViscosity (VISCOSITY_2D.h:460-532).
+ *
+ * The viscosity update reads a copy of u and v whose ghosts are zero
+ * (FIELD_STRUCTURE_2D::Initialize zero-fills, ARRAY_2D.h:48-72), and smeared
+ * densities and viscosities (HeavisideFunction, VISCOSITY_2D.h:688-708, eps = 1.5 dx,
+ * EULERIAN_FLUID_SOLVER_2D.h:347) of phi averaged to the face (x_half), to the
+ * face's upper/lower corners (cu/cd; for y-faces right/left: cu/cl) and taken at
+ * the two nodes beside it (r/c; for y-faces u/c). */
+int or_sourcing(const or_grid* gr, const or_params* pr, const or_flow* fl, const double* phi_a, double* u_a, double* v_a,
+                double* density_a, double dt) {
+  if (!gr || !pr || !fl || !phi_a || !u_a || !v_a) return OR_BAD_ARG;
+  int ni = gr->ni, nj = gr->nj;
+  fld phi = F((double*)phi_a, 2, ni, nj);
+  if (density_a) {
+    fld d = F(density_a, 2, ni, nj);
+    for (int j = 0; j < nj; ++j)
+      for (int i = 0; i < ni; ++i) AT(d, i, j) = AT(phi, i, j) <= 0 ? pr->air_density : pr->water_density;
+  }
+  if (!fl->viscosity) return OR_OK;
+  space_t s = base_space(gr);
+  size_t nu = (size_t)(ni + 5) * (nj + 4), nv = (size_t)(ni + 4) * (nj + 5);
+  double* tu_a = zalloc(nu);
+  double* tv_a = zalloc(nv);
+  if (!tu_a || !tv_a) {
+    free(tu_a);
+    free(tv_a);
+    return OR_NO_MEMORY;
+  }
+  fld u = F(u_a, 2, ni + 1, nj), v = F(v_a, 2, ni, nj + 1);
+  fld tu = F(tu_a, 2, ni + 1, nj), tv = F(tv_a, 2, ni, nj + 1);
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i <= ni; ++i) AT(tu, i, j) = AT(u, i, j);
+  for (int j = 0; j <= nj; ++j)
+    for (int i = 0; i < ni; ++i) AT(tv, i, j) = AT(v, i, j);
+  const double eps = 1.5 * s.dx, odx = s.odx, ody = s.ody;
+  const double rw = pr->water_density, ra = pr->air_density, mw = fl->water_viscosity, ma = fl->air_viscosity;
+#define RHO_H(l) (ra + (rw - ra) * heaviside((l), eps))
+#define MU_H(l) (ma + (mw - ma) * heaviside((l), eps))
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i <= ni; ++i) {
+      double half = 0.5 * (AT(phi, i - 1, j) + AT(phi, i, j));
+      double cu = 0.25 * (AT(phi, i - 1, j) + AT(phi, i, j) + AT(phi, i - 1, j + 1) + AT(phi, i, j + 1));
+      double cd = 0.25 * (AT(phi, i - 1, j - 1) + AT(phi, i, j - 1) + AT(phi, i - 1, j) + AT(phi, i, j));
+      double mu_cu = MU_H(cu), mu_cd = MU_H(cd), mu_r = MU_H(AT(phi, i, j)), mu_c = MU_H(AT(phi, i - 1, j));
+      double coef = dt * (1 / RHO_H(half));
+      double first = 2.0 * coef * odx *
+                     (mu_r * odx * (AT(tu, i + 1, j) - AT(tu, i, j)) - mu_c * odx * (AT(tu, i, j) - AT(tu, i - 1, j)));
+      double second = coef * ody *
+                      (mu_cu * (ody * (AT(tu, i, j + 1) - AT(tu, i, j)) + odx * (AT(tv, i, j + 1) - AT(tv, i - 1, j + 1))) -
+                       mu_cd * (ody * (AT(tu, i, j) - AT(tu, i, j - 1)) + odx * (AT(tv, i, j) - AT(tv, i - 1, j))));
+      AT(u, i, j) += first + second;
+    }
+  for (int j = 0; j <= nj; ++j)
+    for (int i = 0; i < ni; ++i) {
+      double half = 0.5 * (AT(phi, i, j - 1) + AT(phi, i, j));
+      double cu = 0.25 * (AT(phi, i, j - 1) + AT(phi, i + 1, j - 1) + AT(phi, i, j) + AT(phi, i + 1, j));
+      double cl = 0.25 * (AT(phi, i - 1, j - 1) + AT(phi, i, j - 1) + AT(phi, i - 1, j) + AT(phi, i, j));
+      double mu_cu = MU_H(cu), mu_cl = MU_H(cl), mu_u = MU_H(AT(phi, i, j)), mu_c = MU_H(AT(phi, i, j - 1));
+      double coef = dt * (1 / RHO_H(half));
+      double first = 2.0 * coef * ody *
+                     (mu_u * ody * (AT(tv, i, j + 1) - AT(tv, i, j)) - mu_c * ody * (AT(tv, i, j) - AT(tv, i, j - 1)));
+      double second = coef * odx *
+                      (mu_cu * (ody * (AT(tu, i + 1, j) - AT(tu, i + 1, j - 1)) + odx * (AT(tv, i + 1, j) - AT(tv, i, j))) -
+                       mu_cl * (ody * (AT(tu, i, j) - AT(tu, i, j - 1)) + odx * (AT(tv, i, j) - AT(tv, i - 1, j))));
+      AT(v, i, j) += first + second;
+    }
+#undef RHO_H
+#undef MU_H
+  free(tu_a);
+  free(tv_a);
+  return OR_OK;
+}
+
+/* SolveForRK (EULERIAN_FLUID_SOLVER_2D.h:1857-1879): velocity advection,
+ * gravity, sourcing, wall conditions, projection. */
+int or_solve_for_rk(const or_grid* gr, const or_params* pr, const or_flow* fl, double* phi, double* u, double* v, double* ua,
+                    double* va, double* p, double* kappa, double* density, double dt, or_stats* st) {
+  int rc;
+  if ((rc = or_velocity_advection(gr, pr, u, v, ua, va, dt))) return rc;
+  if ((rc = or_apply_gravity(gr, fl, u, v, dt))) return rc;
+  if ((rc = or_sourcing(gr, pr, fl, phi, u, v, density, dt))) return rc;
+  or_velocity_bc(gr, u, v);
+  return or_projection(gr, pr, phi, u, v, p, kappa, dt, st);
+}
+
+/* AdvanceOneTimeStepThread, order_for_time_advancing = 3 (EULERIAN_FLUID_SOLVER_2D.h:1694-1794):
+ * level-set and reinitialisation TVD-RK3, then the velocity TVD-RK3 over three
+ * SolveForRK stages, blended on every MAC face.  st sums the three projections'
+ * iterations; its residual and maxima are the last projection's. */
+int or_time_step(const or_grid* gr, const or_params* pr, const or_flow* fl, double* phi, double* u_a, double* v_a, double* ua,
+                 double* va, double* p, double* kappa, double* density, double dt, or_stats* st) {
+  if (!gr || !pr || !fl || !phi || !u_a || !v_a) return OR_BAD_ARG;
+  int ni = gr->ni, nj = gr->nj, rc, its = 0;
+  or_stats s1;
+  memset(&s1, 0, sizeof s1);
+  if ((rc = or_levelset_rk3(gr, pr, phi, ua, va, dt))) return rc;
+  size_t nu = (size_t)(ni + 5) * (nj + 4), nv = (size_t)(ni + 4) * (nj + 5);
+  double* ku_a = zalloc(nu);
+  double* kv_a = zalloc(nv);
+  if (!ku_a || !kv_a) {
+    rc = OR_NO_MEMORY;
+    goto out;
+  }
+  fld u = F(u_a, 2, ni + 1, nj), v = F(v_a, 2, ni, nj + 1), ku = F(ku_a, 2, ni + 1, nj), kv = F(kv_a, 2, ni, nj + 1);
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i <= ni; ++i) AT(ku, i, j) = AT(u, i, j);
+  for (int j = 0; j <= nj; ++j)
+    for (int i = 0; i < ni; ++i) AT(kv, i, j) = AT(v, i, j);
+#define STAGE()                                                                                     \
+  do {                                                                                              \
+    if ((rc = or_solve_for_rk(gr, pr, fl, phi, u_a, v_a, ua, va, p, kappa, density, dt, &s1))) goto out; \
+    its += s1.iterations;                                                                           \
+  } while (0)
+#define BLEND(c0, c1)                                                                     \
+  do {                                                                                    \
+    for (int j = 0; j < nj; ++j)                                                          \
+      for (int i = 0; i <= ni; ++i) AT(u, i, j) = (c0) * AT(ku, i, j) + (c1) * AT(u, i, j); \
+    for (int j = 0; j <= nj; ++j)                                                         \
+      for (int i = 0; i < ni; ++i) AT(v, i, j) = (c0) * AT(kv, i, j) + (c1) * AT(v, i, j); \
+  } while (0)
+  STAGE();
+  STAGE();
+  BLEND(0.75, 0.25);
+  STAGE();
+  BLEND(1 / 3.0, 2 / 3.0);
+#undef STAGE
+#undef BLEND
+  rc = OR_OK;
+out:
+  if (st) {
+    *st = s1;
+    st->iterations = its;
+  }
+  free(ku_a);
+  free(kv_a);
+  return rc;
+}

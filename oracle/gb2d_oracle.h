@@ -47,6 +47,16 @@ typedef struct {
                                       timing to a relative residual; the reference has no such test) */
 } or_params;
 
+/* Flow constants of SolveForRK's sourcing stages (EULERIAN_FLUID_SOLVER_2D.h:170-262). */
+typedef struct {
+  double water_viscosity;          /* phi > 0 */
+  double air_viscosity;            /* phi <= 0 */
+  double gravity_x, gravity_y;     /* ApplyGraivity adds dt * gravity */
+  int viscosity;                   /* 1: explicit delta-function viscosity (VISCOSITY_2D.h:460-532);
+                                      0: none, which is what the reference's air/water setup runs
+                                      (its viscosity solver is never configured) */
+} or_flow;
+
 typedef struct {
   int iterations;
   double residual;                 /* sqrt(r.z) at exit, as the reference prints it */
@@ -75,6 +85,17 @@ int or_velocity_advection(const or_grid* gr, const or_params* pr, double* u, dou
 int or_curvature(const or_grid* gr, double* phi, double* kappa);
 /* a9-a14: one PROJECTION_2D::Solve(dt, tid); p is the warm start and the result. */
 int or_projection(const or_grid* gr, const or_params* pr, double* phi, double* u, double* v, double* p, double* kappa, double dt, or_stats* st);
+
+/* Rest of SolveForRK (EULERIAN_FLUID_SOLVER_2D.h:1857-1879). */
+int or_apply_gravity(const or_grid* gr, const or_flow* fl, double* u, double* v, double dt);
+/* DetermineDensity into density (ghost 2; may be null), then the viscosity if fl->viscosity. */
+int or_sourcing(const or_grid* gr, const or_params* pr, const or_flow* fl, const double* phi, double* u, double* v, double* density, double dt);
+void or_velocity_bc(const or_grid* gr, double* u, double* v);
+int or_solve_for_rk(const or_grid* gr, const or_params* pr, const or_flow* fl, double* phi, double* u, double* v, double* ua,
+                    double* va, double* p, double* kappa, double* density, double dt, or_stats* st);
+/* AdvanceOneTimeStepThread, order 3 (EULERIAN_FLUID_SOLVER_2D.h:1694-1794). */
+int or_time_step(const or_grid* gr, const or_params* pr, const or_flow* fl, double* phi, double* u, double* v, double* ua,
+                 double* va, double* p, double* kappa, double* density, double dt, or_stats* st);
 
 /* a10 in matrix-free form.  bx: x-faces (ni+1) x nj (face i between nodes i-1 and i),
  * by: y-faces ni x (nj+1), diag, rhs: ni x nj.  phi must already hold the ghost

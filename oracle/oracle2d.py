@@ -6,7 +6,7 @@ product package.
 
 All arrays follow the reference's ghost-inclusive ARRAY_2D layout
 (ARRAY_2D.h:140-146) as numpy arrays of shape (rows = j, cols = i):
-    phi (nj+4, ni+4)   u (nj+4, ni+5)   v (nj+5, ni+4)
+    phi (nj+4, ni+4)   u (nj+4, ni+5)   v (nj+5, ni+4)   density (nj+4, ni+4)
     ua  (nj+6, ni+7)   va (nj+7, ni+6)  p (nj+2, ni+2)   kappa (nj, ni)
 """
 import ctypes
@@ -32,6 +32,11 @@ class Params(ctypes.Structure):
                 ("reinit_iterations", ctypes.c_int), ("reinit_scaling", ctypes.c_int),
                 ("pcg_tolerance", ctypes.c_double), ("pcg_max_iterations", ctypes.c_int),
                 ("pcg_rel_residual", ctypes.c_double)]
+
+
+class Flow(ctypes.Structure):
+    _fields_ = [("water_viscosity", ctypes.c_double), ("air_viscosity", ctypes.c_double),
+                ("gravity_x", ctypes.c_double), ("gravity_y", ctypes.c_double), ("viscosity", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -63,8 +68,15 @@ def lib():
         L.or_poisson_apply.argtypes = [G, P, P, P, P, P]
         L.or_pcg_ic0.argtypes = [G, R, P, P, P, P, P, S]
         L.or_fill_ghost_extrapolate.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        W = ctypes.POINTER(Flow)
+        L.or_apply_gravity.argtypes = [G, W, P, P, d]
+        L.or_sourcing.argtypes = [G, R, W, P, P, P, P, d]
+        L.or_velocity_bc.argtypes = [G, P, P]
+        L.or_solve_for_rk.argtypes = [G, R, W, P, P, P, P, P, P, P, P, d, S]
+        L.or_time_step.argtypes = [G, R, W, P, P, P, P, P, P, P, P, d, S]
         for f in ("or_levelset_advection", "or_reinitialization", "or_levelset_rk3", "or_velocity_advection",
-                  "or_curvature", "or_projection", "or_poisson_assemble", "or_pcg_ic0"):
+                  "or_curvature", "or_projection", "or_poisson_assemble", "or_pcg_ic0", "or_apply_gravity",
+                  "or_sourcing", "or_solve_for_rk", "or_time_step"):
             getattr(L, f).restype = ctypes.c_int
         _lib = L
     return _lib
@@ -134,4 +146,39 @@ def poisson_apply(g, bx, by, dg, x):
 def pcg_ic0(g, pr, bx, by, dg, rhs, x):
     st = Stats()
     _check(lib().or_pcg_ic0(ctypes.byref(g), ctypes.byref(pr), _p(bx), _p(by), _p(dg), _p(rhs), _p(x), ctypes.byref(st)), "pcg_ic0")
+    return st
+
+
+def flow(water_viscosity=1.0, air_viscosity=0.01, gravity=(0.0, -9.8), viscosity=False):
+    return Flow(water_viscosity, air_viscosity, gravity[0], gravity[1], int(bool(viscosity)))
+
+
+def _opt(a):
+    return None if a is None else _p(a)
+
+
+def apply_gravity(g, fl, u, v, dt):
+    _check(lib().or_apply_gravity(ctypes.byref(g), ctypes.byref(fl), _p(u), _p(v), dt), "apply_gravity")
+
+
+def sourcing(g, pr, fl, phi, u, v, density, dt):
+    _check(lib().or_sourcing(ctypes.byref(g), ctypes.byref(pr), ctypes.byref(fl), _p(phi), _p(u), _p(v), _opt(density), dt),
+           "sourcing")
+
+
+def velocity_bc(g, u, v):
+    lib().or_velocity_bc(ctypes.byref(g), _p(u), _p(v))
+
+
+def solve_for_rk(g, pr, fl, phi, u, v, ua, va, p, kappa, density, dt):
+    st = Stats()
+    _check(lib().or_solve_for_rk(ctypes.byref(g), ctypes.byref(pr), ctypes.byref(fl), _p(phi), _p(u), _p(v), _p(ua), _p(va),
+                                 _p(p), _p(kappa), _opt(density), dt, ctypes.byref(st)), "solve_for_rk")
+    return st
+
+
+def time_step(g, pr, fl, phi, u, v, ua, va, p, kappa, density, dt):
+    st = Stats()
+    _check(lib().or_time_step(ctypes.byref(g), ctypes.byref(pr), ctypes.byref(fl), _p(phi), _p(u), _p(v), _p(ua), _p(va),
+                              _p(p), _p(kappa), _opt(density), dt, ctypes.byref(st)), "time_step")
     return st

@@ -10,7 +10,9 @@
  * (EULERIAN_FLUID_SOLVER_2D.h:159-727) from a SCRIPT_BLOCK whose values this
  * file fills in, then exposes the solver's own step functions:
  *   Levelset_Advection (:1896), Reinitialization (:2402), Velocity_Advection
- *   (:1886), Projection (:2359), AdvanceOneTimeStepThread (:1140),
+ *   (:1886), Projection (:2359), AdvanceOneTimeStepThread (:1140), SolveForRK
+ *   (:1857), ApplyGraivity (:3249), Sourcing (:2082), SetupBoundaryConditionForVelocity
+ *   (:2227),
  *   LEVELSET_2D::ComputeCurvaturesThread (LEVELSET_2D.h:898).
  * Every call runs on one worker (thread_id 0 of a 1-thread MULTITHREADING),
  * which is how the reference's head thread runs the pressure solve anyway
@@ -119,6 +121,9 @@ ARRAY_2D<T>* field(RefSim* s, int id) {
     case 9: return &f.water_projection->divergence_field.array_for_this;     // div/dt, ghost 1
     case 10: return &f.sign_function.array_for_this;                         // reinit S, ghost 3
     case 11: return &f.scalar_field_ghost.array_for_this;                    // WENO scratch, ghost 3
+    case 12: return &f.density_field.array_for_this;                         // node density, ghost 2
+    case 13: return &f.water_velocity_field_x_rk_3rd.array_for_this;         // velocity RK3 keep, x
+    case 14: return &f.water_velocity_field_y_rk_3rd.array_for_this;         // velocity RK3 keep, y
     default: return 0;
   }
 }
@@ -181,7 +186,40 @@ void* ref_create(int ni, int nj, double x_min, double y_min, double x_max, doubl
   s->solver.world_discretization = &s->world;
   s->solver.air_water_simulation = true;
   s->solver.InitializeFromScriptBlock(grid, b, &s->mt);
+  /* For air/water the reference constructs its VISCOSITY_2D (EULERIAN_FLUID_SOLVER_2D.h:646-652)
+   * but never calls VISCOSITY_2D::InitializeFromScriptBlock (only the oil/water branch does,
+   * :668), and the constructor's initialiser list (VISCOSITY_2D.h:107-111) leaves
+   * use_delta_function_formulation unset.  With it false, ApplyViscosity does nothing for
+   * air/water; the driver sets it so, making that behaviour deterministic.
+   * ref_configure_viscosity(h, 1) runs the configuration step the air/water branch skips. */
+  s->solver.viscosity_solver->use_delta_function_formulation = false;
   return s;
+}
+
+/* Configure the viscosity solver as VISCOSITY_2D::InitializeFromScriptBlock (VISCOSITY_2D.h:117-276)
+ * would for this script (enable = 1), so that ApplyViscosity applies the delta-function
+ * formulation (:460-532) with the script's viscosities and densities; enable = 0 returns
+ * to the reference's as-shipped air/water behaviour (no viscous term). */
+void ref_configure_viscosity(void* h, int enable) {
+  RefSim* s = static_cast<RefSim*>(h);
+  VISCOSITY_2D* vs = s->solver.viscosity_solver;
+  if (!enable) {
+    vs->use_delta_function_formulation = false;
+    return;
+  }
+  SCRIPT_BLOCK blk;
+  for (size_t k = 0; k < s->block.values.size(); ++k) {
+    const SCRIPT_VALUE* v = s->block.values[k];
+    if (v->value_name != "use_delta_function_formulation") put(blk, v->value_name.c_str(), v->val);
+  }
+  put(blk, "use_delta_function_formulation", "true");
+  SCRIPT_BLOCK* pw = child(blk, "PROJECTION_WATER");
+  put(*pw, "air_bubble_rising", "true");
+  SCRIPT_BLOCK* pr = child(blk, "PROJECTION");
+  put(*pr, "poisson_solver_type", "PCG");
+  vs->air_water_simulation = true;
+  vs->oil_water_simulation = false;
+  vs->InitializeFromScriptBlock(blk);
 }
 
 void ref_destroy(void* h) { delete static_cast<RefSim*>(h); }
@@ -214,6 +252,10 @@ void ref_reinitialization(void* h, double dt) { static_cast<RefSim*>(h)->solver.
 void ref_velocity_advection(void* h, double dt) { static_cast<RefSim*>(h)->solver.Velocity_Advection(dt, 0); }
 void ref_projection(void* h, double dt) { static_cast<RefSim*>(h)->solver.Projection(dt, 0); }
 void ref_curvature(void* h) { static_cast<RefSim*>(h)->solver.water_levelset->ComputeCurvaturesThread(0); }
+void ref_apply_gravity(void* h, double dt) { static_cast<RefSim*>(h)->solver.ApplyGraivity(dt, 0); }
+void ref_sourcing(void* h, double dt) { static_cast<RefSim*>(h)->solver.Sourcing(dt, 0); }
+void ref_velocity_bc(void* h) { static_cast<RefSim*>(h)->solver.SetupBoundaryConditionForVelocity(); }
+void ref_solve_for_rk(void* h, double dt) { static_cast<RefSim*>(h)->solver.SolveForRK(dt, 0); }
 void ref_step(void* h, double dt) { static_cast<RefSim*>(h)->solver.AdvanceOneTimeStepThread(dt, 0); }
 double ref_cfl_dt(void* h) { return static_cast<RefSim*>(h)->solver.CFLOneTimeStep(); }
 

@@ -12,7 +12,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "..", "_ref", "libref2d.so")
 
-PHI, U, V, UA, VA, P, KAPPA, RHO, JC, DIV, SIGN, SCRATCH = range(12)
+PHI, U, V, UA, VA, P, KAPPA, RHO, JC, DIV, SIGN, SCRATCH, DENSITY, U_RK3, V_RK3 = range(15)
 
 
 def available():
@@ -31,9 +31,12 @@ class RefSim:
         L.ref_create.restype = vp
         L.ref_create.argtypes = [i, i, d, d, d, d, ctypes.POINTER(d)]
         L.ref_destroy.argtypes = [vp]
-        for f in ("ref_levelset_advection", "ref_reinitialization", "ref_velocity_advection", "ref_projection", "ref_step"):
+        for f in ("ref_levelset_advection", "ref_reinitialization", "ref_velocity_advection", "ref_projection", "ref_step",
+                  "ref_apply_gravity", "ref_sourcing", "ref_solve_for_rk"):
             getattr(L, f).argtypes = [vp, d]
         L.ref_curvature.argtypes = [vp]
+        L.ref_velocity_bc.argtypes = [vp]
+        L.ref_configure_viscosity.argtypes = [vp, i]
         L.ref_cfl_dt.argtypes = [vp]
         L.ref_cfl_dt.restype = d
         L.ref_field_shape.argtypes = [vp, i] + [ctypes.POINTER(i)] * 4
@@ -86,6 +89,23 @@ class RefSim:
 
     def step(self, dt):
         self.L.ref_step(self.h, dt)
+
+    def apply_gravity(self, dt):
+        self.L.ref_apply_gravity(self.h, dt)
+
+    def sourcing(self, dt):
+        self.L.ref_sourcing(self.h, dt)
+
+    def velocity_bc(self):
+        self.L.ref_velocity_bc(self.h)
+
+    def solve_for_rk(self, dt):
+        self.L.ref_solve_for_rk(self.h, dt)
+
+    def configure_viscosity(self, enable):
+        """1: apply the delta-function explicit viscosity (the configuration the reference's
+        air/water setup skips); 0: the reference's as-shipped air/water behaviour (none)."""
+        self.L.ref_configure_viscosity(self.h, int(enable))
 
     def cfl_dt(self):
         return self.L.ref_cfl_dt(self.h)

@@ -12,6 +12,13 @@ tests/golden/cases.py and stores inputs and outputs:
   curvature           ComputeCurvaturesThread
   projection          PROJECTION_2D::Solve(dt) with PCG-IC(0) at a tight tolerance,
                       plus the assembled CSR system and A*x for a seeded x
+  gravity / sourcing / velocity_bc
+                      ApplyGraivity, Sourcing (DetermineDensity and, with the
+                      viscosity solver configured, ApplyViscosity) and
+                      SetupBoundaryConditionForVelocity applied in turn
+  solve_for_rk        one SolveForRK stage (viscosity configured)
+  time_step           AdvanceOneTimeStepThread (order 3), without viscosity (the
+                      reference's air/water setup) and with it configured
 
 Usage:  python tests/golden/make_golden.py   (needs the reference sources)
 """
@@ -29,6 +36,7 @@ import refsim as R  # noqa: E402
 from tests.golden.cases import bubbles_case, rising_bubble_case  # noqa: E402
 
 PHYS = dict(water_density=1000.0, air_density=1.0, surface_tension=0.0728)
+FLOW = dict(water_viscosity=1.0, air_viscosity=0.01, gravity=(0.0, -9.8))
 
 
 def csr_apply(rp, col, val, x):
@@ -41,7 +49,7 @@ def csr_apply(rp, col, val, x):
     return y
 
 
-def make_case(name, c, dt, pcg_tolerance):
+def make_case(name, c, dt, pcg_tolerance, flow=True):
     ni, nj, xm, ym = c["ni"], c["nj"], c["x_max"], c["y_max"]
     out = {k: np.asarray(c[k]) for k in ("phi", "u", "v", "ua", "va", "p")}
     out.update(ni=ni, nj=nj, x_max=xm, y_max=ym, dt=dt, pcg_tolerance=pcg_tolerance)
@@ -96,9 +104,44 @@ def make_case(name, c, dt, pcg_tolerance):
     out["sys_ax"] = csr_apply(rp, col, val, xr)
     out["sys_diag"] = np.array([val[rp[r + 1] - 1] for r in range(ni * nj)])
     s.close()
+    if flow:
+        make_flow(out, c, dt, pcg_tolerance)
     path = os.path.join(HERE, f"{name}.npz")
     np.savez_compressed(path, **out)
     print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB, PCG {it} iterations, residual {res:.3e}")
+
+
+def make_flow(out, c, dt, pcg_tolerance):
+    """The SolveForRK stages around the projection and the whole order-3 time step."""
+    ni, nj, xm, ym = c["ni"], c["nj"], c["x_max"], c["y_max"]
+    mk = lambda: R.RefSim(ni, nj, 0.0, 0.0, xm, ym, **PHYS, **FLOW, pcg_tolerance=pcg_tolerance, pcg_max_iterations=200000)
+
+    def load(s):
+        for f, k in ((R.PHI, "phi"), (R.U, "u"), (R.V, "v"), (R.UA, "ua"), (R.VA, "va"), (R.P, "p")):
+            s.set(f, c[k])
+
+    # gravity -> sourcing (with and without viscosity) -> wall conditions, from the same start
+    for visc in (0, 1):
+        s = mk(); s.configure_viscosity(visc); load(s)
+        s.apply_gravity(dt)
+        out["grav_u"], out["grav_v"] = s.get(R.U), s.get(R.V)
+        s.sourcing(dt)
+        out[f"src{visc}_u"], out[f"src{visc}_v"], out[f"src{visc}_density"] = s.get(R.U), s.get(R.V), s.get(R.DENSITY)
+        s.velocity_bc()
+        out[f"bc{visc}_u"], out[f"bc{visc}_v"] = s.get(R.U), s.get(R.V)
+        s.close()
+    s = mk(); s.configure_viscosity(1); load(s)
+    s.solve_for_rk(dt)
+    for f, k in ((R.PHI, "phi"), (R.U, "u"), (R.V, "v"), (R.UA, "ua"), (R.VA, "va"), (R.P, "p"), (R.KAPPA, "kappa")):
+        out["rk_" + k] = s.get(f)
+    s.close()
+    for visc in (0, 1):
+        s = mk(); s.configure_viscosity(visc); load(s)
+        s.step(dt)
+        for f, k in ((R.PHI, "phi"), (R.U, "u"), (R.V, "v"), (R.UA, "ua"), (R.VA, "va"), (R.P, "p"),
+                     (R.DENSITY, "density")):
+            out[f"step{visc}_{k}"] = s.get(f)
+        s.close()
 
 
 def main():
@@ -108,7 +151,7 @@ def main():
     make_case("bubbles_33", bubbles_case(33, seed=2), 0.5 / 32, 1e-13)
     make_case("rising_bubble_40x24", rising_bubble_case(40, 24, seed=3), 0.01, 1e-13)
     make_case("tall_24x40", bubbles_case(24, 40, seed=4, x_max=1.0, y_max=2.0), 0.02, 1e-13)
-    make_case("bubbles_65", bubbles_case(65, seed=5), 0.5 / 64, 1e-12)
+    make_case("bubbles_65", bubbles_case(65, seed=5), 0.5 / 64, 1e-12, flow=False)
 
 
 if __name__ == "__main__":

@@ -85,3 +85,59 @@ def test_projection(oracle, name):
     # Interface faces use sin() in the smeared Heaviside: libm may differ by an ulp across hosts.
     for got, key in ((u, "proj_u"), (v, "proj_v")):
         np.testing.assert_allclose(got, g[key], rtol=1e-14, atol=1e-14 * np.abs(g[key]).max())
+
+
+FLOW_NAMES = [n for n in NAMES if "step0_u" in load_golden(n)]
+FIELDS6 = ("phi", "u", "v", "ua", "va", "p")
+
+
+@pytest.mark.parametrize("name", FLOW_NAMES)
+def test_gravity_sourcing_velocity_bc(oracle, name):
+    g = load_golden(name)
+    gr, ni, nj = setup(oracle, g)
+    pr = oracle.params()
+    dt = float(g["dt"])
+    for visc in (0, 1):
+        fl = oracle.flow(viscosity=visc)
+        phi, u, v = g["phi"].copy(), g["u"].copy(), g["v"].copy()
+        oracle.apply_gravity(gr, fl, u, v, dt)
+        np.testing.assert_array_equal(u, g["grav_u"])
+        np.testing.assert_array_equal(v, g["grav_v"])
+        density = np.zeros_like(phi)
+        oracle.sourcing(gr, pr, fl, phi, u, v, density, dt)
+        np.testing.assert_array_equal(density, g[f"src{visc}_density"])
+        np.testing.assert_array_equal(u, g[f"src{visc}_u"])
+        np.testing.assert_array_equal(v, g[f"src{visc}_v"])
+        oracle.velocity_bc(gr, u, v)
+        np.testing.assert_array_equal(u, g[f"bc{visc}_u"])
+        np.testing.assert_array_equal(v, g[f"bc{visc}_v"])
+    # without viscosity, sourcing leaves the velocity alone
+    np.testing.assert_array_equal(g["src0_u"], g["grav_u"])
+
+
+@pytest.mark.parametrize("name", FLOW_NAMES)
+def test_solve_for_rk(oracle, name):
+    g = load_golden(name)
+    gr, ni, nj = setup(oracle, g)
+    pr = oracle.params(pcg_tolerance=float(g["pcg_tolerance"]), pcg_max_iterations=200000)
+    phi, u, v, ua, va, p = (g[k].copy() for k in FIELDS6)
+    k = np.zeros((nj, ni))
+    oracle.solve_for_rk(gr, pr, oracle.flow(viscosity=True), phi, u, v, ua, va, p, k, None, float(g["dt"]))
+    for got, key in ((phi, "phi"), (ua, "ua"), (va, "va"), (p, "p"), (k, "kappa"), (u, "u"), (v, "v")):
+        np.testing.assert_array_equal(got, g["rk_" + key])
+
+
+@pytest.mark.parametrize("name", FLOW_NAMES)
+@pytest.mark.parametrize("visc", [0, 1])
+def test_time_step(oracle, name, visc):
+    """AdvanceOneTimeStepThread, order 3: level-set RK3 and three SolveForRK stages."""
+    g = load_golden(name)
+    gr, ni, nj = setup(oracle, g)
+    pr = oracle.params(pcg_tolerance=float(g["pcg_tolerance"]), pcg_max_iterations=200000)
+    phi, u, v, ua, va, p = (g[k].copy() for k in FIELDS6)
+    k = np.zeros((nj, ni))
+    density = np.zeros_like(phi)
+    st = oracle.time_step(gr, pr, oracle.flow(viscosity=visc), phi, u, v, ua, va, p, k, density, float(g["dt"]))
+    assert st.iterations > 0
+    for got, key in zip((phi, u, v, ua, va, p, density), FIELDS6 + ("density",)):
+        np.testing.assert_array_equal(got, g[f"step{visc}_{key}"])
