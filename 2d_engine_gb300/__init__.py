@@ -3,12 +3,13 @@
 The product is the CUDA library 2d_engine_gb300/_build/libgb2d.so; this module
 loads it with ctypes and mirrors the step interface of the reference solver's
 EULERIAN_FLUID_SOLVER_2D (Levelset_Advection, Reinitialization,
-Velocity_Advection, Projection).  There is no CPU fallback: if the library is
+Velocity_Advection, Projection, SolveForRK and its gravity / sourcing / wall
+stages, AdvanceOneTimeStepThread).  There is no CPU fallback: if the library is
 missing or no GPU is visible, the calls raise.
 
 Arrays are numpy float64 in the reference's ghost-inclusive ARRAY_2D layout,
 shape (rows = j, cols = i):  phi (nj+4, ni+4), u (nj+4, ni+5), v (nj+5, ni+4),
-ua (nj+6, ni+7), va (nj+7, ni+6), p (nj+2, ni+2), kappa (nj, ni).
+ua (nj+6, ni+7), va (nj+7, ni+6), p (nj+2, ni+2), kappa (nj, ni), density (nj+4, ni+4).
 """
 import ctypes
 import os
@@ -18,7 +19,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libgb2d.so")
 
-FIELD_PHI, FIELD_U, FIELD_V, FIELD_UA, FIELD_VA, FIELD_P, FIELD_KAPPA = range(7)
+FIELD_PHI, FIELD_U, FIELD_V, FIELD_UA, FIELD_VA, FIELD_P, FIELD_KAPPA, FIELD_DENSITY = range(8)
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 SOLVER_MGPCG, SOLVER_PCG_JACOBI = 0, 1
 
@@ -36,6 +37,11 @@ class ParamsT(ctypes.Structure):
     _fields_ = [("water_density", ctypes.c_double), ("air_density", ctypes.c_double), ("surface_tension", ctypes.c_double),
                 ("weno_epsilon", ctypes.c_double), ("reinit_iterations", ctypes.c_int), ("reinit_scaling", ctypes.c_int),
                 ("advection_precision", ctypes.c_int)]
+
+
+class FlowParamsT(ctypes.Structure):
+    _fields_ = [("water_viscosity", ctypes.c_double), ("air_viscosity", ctypes.c_double), ("gravity_x", ctypes.c_double),
+                ("gravity_y", ctypes.c_double), ("viscosity", ctypes.c_int)]
 
 
 class SolveOptsT(ctypes.Structure):
@@ -81,6 +87,12 @@ def library():
         "gb2d_velocity_advection": [vp, d],
         "gb2d_curvature": [vp],
         "gb2d_projection": [vp, d, O, S],
+        "gb2d_set_flow_params": [vp, ctypes.POINTER(FlowParamsT)],
+        "gb2d_apply_gravity": [vp, d],
+        "gb2d_sourcing": [vp, d],
+        "gb2d_velocity_boundary": [vp],
+        "gb2d_solve_for_rk": [vp, d, O, S],
+        "gb2d_advance_time_step": [vp, d, O, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
         "gb2d_poisson_solve": [vp, vp, vp, O, S],
@@ -232,6 +244,38 @@ class Context:
         opts = opts or solve_opts()
         st = SolveStatsT()
         rc = self.L.gb2d_projection(self.h, dt, ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return st
+
+    def set_flow_params(self, water_viscosity=1.0, air_viscosity=0.0, gravity=(0.0, -9.8), viscosity=False):
+        """Constants of SolveForRK's gravity and sourcing stages; viscosity=False is the reference's
+        air/water behaviour (no viscous term), True applies VISCOSITY_2D::ApplyViscosity's explicit term."""
+        f = FlowParamsT(water_viscosity, air_viscosity, gravity[0], gravity[1], int(bool(viscosity)))
+        self._check(self.L.gb2d_set_flow_params(self.h, ctypes.byref(f)))
+
+    def apply_gravity(self, dt):
+        self._check(self.L.gb2d_apply_gravity(self.h, dt))
+
+    def sourcing(self, dt):
+        self._check(self.L.gb2d_sourcing(self.h, dt))
+
+    def velocity_boundary(self):
+        self._check(self.L.gb2d_velocity_boundary(self.h))
+
+    def solve_for_rk(self, dt, opts=None, allow_max_iters=False):
+        opts = opts or solve_opts()
+        st = SolveStatsT()
+        rc = self.L.gb2d_solve_for_rk(self.h, dt, ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return st
+
+    def advance_time_step(self, dt, opts=None, allow_max_iters=False):
+        """AdvanceOneTimeStepThread (order 3): level-set + reinit RK3, then velocity RK3 over three SolveForRK."""
+        opts = opts or solve_opts()
+        st = SolveStatsT()
+        rc = self.L.gb2d_advance_time_step(self.h, dt, ctypes.byref(opts), ctypes.byref(st))
         if rc != 0 and not (allow_max_iters and rc == -4):
             self._check(rc)
         return st

@@ -2,8 +2,9 @@
 
 Compiles the csrc/ translation units in parallel with nvcc and links them into
 2d_engine_gb300/_build/libgb2d.so (static CUDA runtime, C ABI of include/gb2d.h).
-gb2d_exact.cu is built with --fmad=false: its FP64 kernels must round every
-multiply and add separately, exactly as the reference's CPU arithmetic.
+gb2d_exact.cu and gb2d_flow.cu are built with --fmad=false: their FP64 kernels
+must round every multiply and add separately, exactly as the reference's CPU
+arithmetic.
 """
 import os
 import shutil
@@ -19,6 +20,7 @@ LIB = os.path.join(OUT, "libgb2d.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "gb2d_exact.cu": ["--fmad=false"],
+    "gb2d_flow.cu": ["--fmad=false"],
     "gb2d_solver.cu": [],
     "gb2d_api.cu": [],
     "gb2d_noalloc.cu": [],

@@ -47,6 +47,7 @@ bool field_desc(const gb2d_grid* g, int field, FieldDesc* d) {
     case GB2D_FIELD_VA: *d = {3, ni, nj + 1}; return true;
     case GB2D_FIELD_P: *d = {1, ni, nj}; return true;
     case GB2D_FIELD_KAPPA: *d = {0, ni, nj}; return true;
+    case GB2D_FIELD_DENSITY: *d = {2, ni, nj}; return true;
     default: return false;
   }
 }
@@ -62,6 +63,7 @@ double* field_ptr(gb2d_ctx* c, int field) {
     case GB2D_FIELD_VA: return c->va;
     case GB2D_FIELD_P: return c->p;
     case GB2D_FIELD_KAPPA: return c->kappa;
+    case GB2D_FIELD_DENSITY: return c->density;
     default: return nullptr;
   }
 }
@@ -118,7 +120,8 @@ void free_ctx(gb2d_ctx* c) {
   if (!c) return;
   if (c->solver) solver_destroy(c->solver);
   double* bufs[] = {c->phi_buf[0], c->phi_buf[1], c->phi_buf[2], c->phi_buf[3], c->u, c->v, c->ua, c->va, c->p,
-                    c->kappa, c->sign, c->bx, c->by, c->diag, c->rhs, c->tmp_a, c->tmp_b, c->xw};
+                    c->kappa, c->sign, c->bx, c->by, c->diag, c->rhs, c->tmp_a, c->tmp_b, c->xw, c->u_alt, c->v_alt,
+                    c->u_keep, c->v_keep, c->density};
   for (auto b : bufs)
     if (b) cudaFree(b);
   for (auto b : c->ckpt)
@@ -165,6 +168,11 @@ int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out
   if (!c) return GB2D_ERR_ARG;
   c->grid = *grid;
   c->prm = *params;
+  c->flow.water_viscosity = 1.0;  // script defaults (EULERIAN_FLUID_SOLVER_2D.h:183-194)
+  c->flow.air_viscosity = 0.0;
+  c->flow.gravity_x = 0.0;
+  c->flow.gravity_y = -9.8;
+  c->flow.viscosity = 0;
   int ni = grid->ni, nj = grid->nj;
   c->base = make_space(ni, nj, grid->x_min, grid->y_min, grid->x_max, grid->y_max);
   c->xs = make_space(ni + 1, nj, grid->x_min - 0.5 * c->base.dx, grid->y_min, grid->x_max + 0.5 * c->base.dx, grid->y_max);
@@ -187,6 +195,9 @@ int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out
       {&c->by, (size_t)ni * (nj + 1)},               {&c->diag, (size_t)ni * nj},
       {&c->rhs, (size_t)ni * nj},                    {&c->tmp_a, (size_t)ni * nj},
       {&c->tmp_b, (size_t)ni * nj},                  {&c->xw, (size_t)(ni + 2) * (nj + 2)},
+      {&c->u_alt, (size_t)(ni + 5) * (nj + 4)},      {&c->v_alt, (size_t)(ni + 4) * (nj + 5)},
+      {&c->u_keep, (size_t)(ni + 5) * (nj + 4)},     {&c->v_keep, (size_t)(ni + 4) * (nj + 5)},
+      {&c->density, (size_t)(ni + 4) * (nj + 4)},
   };
   for (auto& a : allocs) {
     if (e != cudaSuccess) break;
@@ -490,6 +501,71 @@ int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve
   local.max_velocity_y = mv;
   if (st) *st = local;
   return src;
+}
+
+int gb2d_set_flow_params(gb2d_ctx* c, const gb2d_flow_params* f) {
+  if (!c || !f || !std::isfinite(f->water_viscosity) || !std::isfinite(f->air_viscosity) || !std::isfinite(f->gravity_x) ||
+      !std::isfinite(f->gravity_y))
+    return GB2D_ERR_ARG;
+  c->flow = *f;
+  return GB2D_OK;
+}
+
+int gb2d_apply_gravity(gb2d_ctx* c, double dt) {
+  if (!c || !std::isfinite(dt)) return GB2D_ERR_ARG;
+  launch_flow(c->stream, c, dt, 1, 0, 0, nullptr);
+  return check_launch(c, "apply_gravity");
+}
+
+int gb2d_sourcing(gb2d_ctx* c, double dt) {
+  if (!c || !std::isfinite(dt)) return GB2D_ERR_ARG;
+  launch_flow(c->stream, c, dt, 0, c->flow.viscosity, 0, c->density);
+  return check_launch(c, "sourcing");
+}
+
+int gb2d_velocity_boundary(gb2d_ctx* c) {
+  if (!c) return GB2D_ERR_ARG;
+  launch_flow(c->stream, c, 0.0, 0, 0, 1, nullptr);
+  return check_launch(c, "velocity_boundary");
+}
+
+int gb2d_solve_for_rk(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
+  if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
+  int rc = gb2d_velocity_advection(c, dt);
+  if (rc) return rc;
+  launch_flow(c->stream, c, dt, 1, c->flow.viscosity, 1, c->density);
+  if ((rc = check_launch(c, "solve_for_rk"))) return rc;
+  return gb2d_projection(c, dt, o, st);
+}
+
+int gb2d_advance_time_step(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
+  if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
+  int rc = gb2d_levelset_rk3(c, dt);
+  if (rc) return rc;
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->u_keep, c->u, (size_t)(ni + 5) * (nj + 4) * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->v_keep, c->v, (size_t)(ni + 4) * (nj + 5) * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  gb2d_solve_stats sum, one;
+  memset(&sum, 0, sizeof sum);
+  int capped = 0;
+  for (int stage = 0; stage < 3; ++stage) {
+    memset(&one, 0, sizeof one);
+    rc = gb2d_solve_for_rk(c, dt, o, &one);
+    if (rc == GB2D_ERR_MAX_ITERS)
+      capped = 1;
+    else if (rc)
+      return rc;
+    sum.iterations += one.iterations;
+    sum.outer_iterations += one.outer_iterations;
+    if (one.rel_residual > sum.rel_residual) sum.rel_residual = one.rel_residual;
+    sum.max_velocity_x = one.max_velocity_x;
+    sum.max_velocity_y = one.max_velocity_y;
+    if (stage == 1) launch_face_blend(c->stream, c, 0.75, 0.25);
+    if (stage == 2) launch_face_blend(c->stream, c, 1 / 3.0, 2 / 3.0);
+  }
+  if ((rc = check_launch(c, "advance_time_step"))) return rc;
+  if (st) *st = sum;
+  return capped ? GB2D_ERR_MAX_ITERS : GB2D_OK;
 }
 
 int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {

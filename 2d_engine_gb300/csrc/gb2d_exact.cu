@@ -271,6 +271,7 @@ struct AsmArgs {
   Space s;
   double water, air, sigma, one_over_dt, inv_dxdx, inv_dydy;
   double inv_water, inv_air;  // 1/water, 1/air: IEEE quotients taken once on the host
+  double oeh, oev;            // 1 / (1.5 dx), 1 / (1.5 dy): smeared-Heaviside scales
 };
 
 // 1/rho of a node.  The density takes two values, so the quotient is a select of
@@ -384,15 +385,6 @@ __global__ void k_apply_exact(const double* __restrict__ bx, const double* __res
   }
 }
 
-// HeavisideFunction (PROJECTION_2D.h:1441-1461) with the reference's PI = 3.141592.
-__device__ __forceinline__ double heaviside(double phi, double eps) {
-  const double PI_REF = 3.141592;
-  if (phi < -eps) return 0;
-  if (phi > eps) return 1;
-  double oe = 1.0 / eps, opi = 1.0 / PI_REF;
-  return 0.5 + phi * oe * 0.5 + 0.5 * opi * sin(PI_REF * phi * oe);
-}
-
 __device__ __forceinline__ void block_max_bits(unsigned long long b, unsigned long long* out) {
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long w = __shfl_xor_sync(0xffffffffu, b, o);
@@ -425,7 +417,7 @@ __global__ void k_velocity_update(const double* __restrict__ phi_a, const double
     } else {
       double jcc = jc_at(kappa, i, j, a), jcn = jc_at(kappa, in, jn, a);
       double gam = (jcn * fabs(l0) + jcc * fabs(ln)) / (fabs(l0) + fabs(ln));
-      double dh = a.air + (a.water - a.air) * heaviside(0.5 * (l0 + ln), xc ? eh : ev);
+      double dh = a.air + (a.water - a.air) * heaviside(0.5 * (l0 + ln), xc ? eh : ev, xc ? a.oeh : a.oev);
       double odh = 1 / dh;
       if (ltz(l0))
         *w -= dt * (dp + gam) * odh * od;
@@ -472,6 +464,8 @@ AsmArgs asm_args(const gb2d_ctx* c, double dt) {
   a.inv_dydy = 1.0 / (c->base.dy * c->base.dy);
   a.inv_water = 1.0 / a.water;
   a.inv_air = 1.0 / a.air;
+  a.oeh = 1.0 / (1.5 * c->base.dx);
+  a.oev = 1.0 / (1.5 * c->base.dy);
   return a;
 }
 

@@ -1,0 +1,190 @@
+// The stages of SolveForRK around the projection (EULERIAN_FLUID_SOLVER_2D.h:1857-1879)
+// and the velocity TVD-RK3 blends (:1753-1794): gravity, DetermineDensity, the
+// explicit delta-function viscosity (VISCOSITY_2D.h:460-532) and the wall
+// conditions, fused into one pass over the two MAC face grids.
+// Built with --fmad=false, in the reference's association order, like
+// gb2d_exact.cu: the results are the reference's FP64 results bit for bit, except
+// where the smeared Heaviside's sine (the only libm call) differs in the last ulp.
+#include "gb2d_internal.cuh"
+#include "gb2d_schemes.cuh"
+
+namespace gb2d {
+
+namespace {
+
+// lo + (hi - lo) * H(phi): a smeared density or viscosity.  at0 / at1 are its
+// values where H is 0 or 1, formed on the host with the same two operations.
+struct Smear {
+  double lo, d, at0, at1;
+};
+Smear make_smear(double lo, double hi) {
+  Smear s;
+  s.lo = lo;
+  s.d = hi - lo;
+  s.at0 = lo + s.d * 0.0;
+  s.at1 = lo + s.d * 1.0;
+  return s;
+}
+
+struct FlowArgs {
+  int ni, nj;
+  int grav, bc;        // add dt * gravity to every face; zero the wall faces' normal velocity
+  double gx, gy;       // dt * gravity
+  double dt, odx, ody;
+  double eps, oe;      // smearing width 1.5 dx (EULERIAN_FLUID_SOLVER_2D.h:347) and its reciprocal
+  Smear rho, mu;       // face density and viscosity
+  double coef0, coef1; // dt * (1 / rho.at0), dt * (1 / rho.at1)
+  double air, water;   // node densities of DetermineDensity
+};
+
+__device__ __forceinline__ double smear(double l, const Smear& s, const FlowArgs& a) {
+  if (lt_neg(l, a.eps)) return s.at0;
+  if (gt_pos(l, a.eps)) return s.at1;
+  return s.lo + s.d * heaviside_band(l, a.oe);
+}
+
+// dt / rho of a face: rho takes two values outside the band, whose quotients the
+// host formed (FP64 divisions are scarce on this part).
+__device__ __forceinline__ double face_coef(double l, const FlowArgs& a) {
+  if (lt_neg(l, a.eps)) return a.coef0;
+  if (gt_pos(l, a.eps)) return a.coef1;
+  return a.dt * (1 / (a.rho.lo + a.rho.d * heaviside_band(l, a.oe)));
+}
+
+// One pass over the (ni+1) x (nj+1) face index space: x-face (i, j), i <= ni,
+// j < nj; y-face (i, j), i < ni, j <= nj; node (i, j) for the density.
+//   VISC = false: gravity and wall conditions in place (u_out may equal u_in).
+//   VISC = true:  ApplyViscosity from the copies temp_x / temp_y of the faces after
+//                 gravity, whose values off the face grids are zero (the reference's
+//                 freshly initialised temporaries), written to u_out / v_out.
+// density (ghost 2, may be null) receives DetermineDensity (:2162-2180): air where
+// phi <= 0, water where phi > 0, unchanged for NaN.
+template <bool VISC>
+__global__ void k_flow(const double* __restrict__ phi_a, const double* u_in_a, const double* v_in_a, double* u_out_a,
+                       double* v_out_a, double* __restrict__ dens_a, FlowArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const DField phi = dfield((double*)phi_a, 2, ni, nj);
+  const DField ui = dfield((double*)u_in_a, 2, ni + 1, nj), vi = dfield((double*)v_in_a, 2, ni, nj + 1);
+  const DField uo = dfield(u_out_a, 2, ni + 1, nj), vo = dfield(v_out_a, 2, ni, nj + 1);
+  auto tu = [&](int i, int j) -> double {
+    if (i < 0 || i > ni || j < 0 || j >= nj) return 0.0;
+    const double w = GB_AT(ui, i, j);
+    return a.grav ? w + a.gx : w;
+  };
+  auto tv = [&](int i, int j) -> double {
+    if (i < 0 || i >= ni || j < 0 || j > nj) return 0.0;
+    const double w = GB_AT(vi, i, j);
+    return a.grav ? w + a.gy : w;
+  };
+  auto P = [&](int i, int j) -> double { return __ldg(&GB_AT(phi, i, j)); };
+  GB_FOR_IJ(i, j, ni + 1, nj + 1) {
+    if (dens_a && i < ni && j < nj) {
+      const double l = P(i, j);
+      DField dn = dfield(dens_a, 2, ni, nj);
+      if (lez(l))
+        GB_AT(dn, i, j) = a.air;
+      else if (gtz(l))
+        GB_AT(dn, i, j) = a.water;
+    }
+    if (j < nj) {  // x-face between nodes (i-1, j) and (i, j)
+      double w;
+      if (VISC) {
+        const double pl = P(i - 1, j), pc = P(i, j);
+        const double half = 0.5 * (pl + pc);
+        const double cu = 0.25 * (pl + pc + P(i - 1, j + 1) + P(i, j + 1));
+        const double cd = 0.25 * (P(i - 1, j - 1) + P(i, j - 1) + pl + pc);
+        const double mu_cu = smear(cu, a.mu, a), mu_cd = smear(cd, a.mu, a);
+        const double mu_r = smear(pc, a.mu, a), mu_c = smear(pl, a.mu, a);
+        const double coef = face_coef(half, a);
+        const double t0 = tu(i, j);
+        const double first = 2.0 * coef * a.odx * (mu_r * a.odx * (tu(i + 1, j) - t0) - mu_c * a.odx * (t0 - tu(i - 1, j)));
+        const double second = coef * a.ody *
+                               (mu_cu * (a.ody * (tu(i, j + 1) - t0) + a.odx * (tv(i, j + 1) - tv(i - 1, j + 1))) -
+                                mu_cd * (a.ody * (t0 - tu(i, j - 1)) + a.odx * (tv(i, j) - tv(i - 1, j))));
+        w = t0 + (first + second);
+      } else {
+        w = tu(i, j);
+      }
+      if (a.bc && (i == 0 || i == ni)) w = 0.0;
+      GB_AT(uo, i, j) = w;
+    }
+    if (i < ni) {  // y-face between nodes (i, j-1) and (i, j)
+      double w;
+      if (VISC) {
+        const double pb = P(i, j - 1), pc = P(i, j);
+        const double half = 0.5 * (pb + pc);
+        const double cu = 0.25 * (pb + P(i + 1, j - 1) + pc + P(i + 1, j));
+        const double cl = 0.25 * (P(i - 1, j - 1) + pb + P(i - 1, j) + pc);
+        const double mu_cu = smear(cu, a.mu, a), mu_cl = smear(cl, a.mu, a);
+        const double mu_u = smear(pc, a.mu, a), mu_c = smear(pb, a.mu, a);
+        const double coef = face_coef(half, a);
+        const double t0 = tv(i, j);
+        const double first = 2.0 * coef * a.ody * (mu_u * a.ody * (tv(i, j + 1) - t0) - mu_c * a.ody * (t0 - tv(i, j - 1)));
+        const double second = coef * a.odx *
+                              (mu_cu * (a.ody * (tu(i + 1, j) - tu(i + 1, j - 1)) + a.odx * (tv(i + 1, j) - t0)) -
+                               mu_cl * (a.ody * (tu(i, j) - tu(i, j - 1)) + a.odx * (t0 - tv(i - 1, j))));
+        w = t0 + (first + second);
+      } else {
+        w = tv(i, j);
+      }
+      if (a.bc && (j == 0 || j == nj)) w = 0.0;
+      GB_AT(vo, i, j) = w;
+    }
+  }
+}
+
+// Velocity TVD-RK3 blend on every MAC face: w = c0 * keep + c1 * w.
+__global__ void k_face_blend(const double* __restrict__ ku_a, double* __restrict__ u_a, const double* __restrict__ kv_a,
+                             double* __restrict__ v_a, int ni, int nj, double c0, double c1) {
+  const DField ku = dfield((double*)ku_a, 2, ni + 1, nj), u = dfield(u_a, 2, ni + 1, nj);
+  const DField kv = dfield((double*)kv_a, 2, ni, nj + 1), v = dfield(v_a, 2, ni, nj + 1);
+  GB_FOR_IJ(i, j, ni + 1, nj + 1) {
+    if (j < nj) GB_AT(u, i, j) = c0 * GB_AT(ku, i, j) + c1 * GB_AT(u, i, j);
+    if (i < ni) GB_AT(v, i, j) = c0 * GB_AT(kv, i, j) + c1 * GB_AT(v, i, j);
+  }
+}
+
+}  // namespace
+
+void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int bc, double* density) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  FlowArgs a;
+  a.ni = ni;
+  a.nj = nj;
+  a.grav = grav;
+  a.bc = bc;
+  a.gx = dt * c->flow.gravity_x;
+  a.gy = dt * c->flow.gravity_y;
+  a.dt = dt;
+  a.odx = c->base.odx;
+  a.ody = c->base.ody;
+  a.eps = 1.5 * c->base.dx;
+  a.oe = 1.0 / a.eps;
+  a.rho = make_smear(c->prm.air_density, c->prm.water_density);
+  a.mu = make_smear(c->flow.air_viscosity, c->flow.water_viscosity);
+  a.coef0 = dt * (1 / a.rho.at0);
+  a.coef1 = dt * (1 / a.rho.at1);
+  a.air = c->prm.air_density;
+  a.water = c->prm.water_density;
+  const double* phi = c->phi_buf[c->phi_cur];
+  if (visc) {
+    k_flow<true><<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(phi, c->u, c->v, c->u_alt, c->v_alt, density, a);
+    double* t = c->u;
+    c->u = c->u_alt;
+    c->u_alt = t;
+    t = c->v;
+    c->v = c->v_alt;
+    c->v_alt = t;
+  } else {
+    k_flow<false><<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(phi, c->u, c->v, c->u, c->v, density, a);
+  }
+  GB_LAUNCHED(1);
+}
+
+void launch_face_blend(cudaStream_t s, gb2d_ctx* c, double c0, double c1) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  k_face_blend<<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(c->u_keep, c->u, c->v_keep, c->v, ni, nj, c0, c1);
+  GB_LAUNCHED(1);
+}
+
+}  // namespace gb2d

@@ -125,6 +125,7 @@ struct Probe {
 struct gb2d_ctx {
   gb2d_grid grid;
   gb2d_params prm;
+  gb2d_flow_params flow;
   gb2d::Space base, xs, ys;
   cudaStream_t stream;
   cudaStream_t own_stream;
@@ -135,6 +136,9 @@ struct gb2d_ctx {
   double* phi_buf[4];
   int phi_cur;
   double *u, *v, *ua, *va, *p, *kappa;
+  double *u_alt, *v_alt;    // second face buffers: the viscosity pass writes them, then they swap with u, v
+  double *u_keep, *v_keep;  // velocity TVD-RK3 stage-0 copies (water_velocity_field_*_rk_3rd)
+  double* density;          // DetermineDensity's node density, ghost 2
   double* sign;  // reinit S (interior)
   // Assembled pressure system (FP64): faces bx ((ni+1) x nj), by (ni x (nj+1)), diag/rhs (ni x nj).
   double *bx, *by, *diag, *rhs;
@@ -165,6 +169,14 @@ void launch_rhs_diag(cudaStream_t s, const gb2d_ctx* c, const double* phi, doubl
 void launch_poisson_apply_exact(cudaStream_t s, const gb2d_ctx* c, const double* x, double* y);
 void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt, Scalars* sc);
 void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst, int gd, int nI, int nJ);
+
+// ---- gb2d_flow.cu (FP64, compiled without FMA contraction) ----
+// Gravity (grav), viscosity (visc) and wall conditions (bc) over the face grids, and
+// DetermineDensity into density (may be null).  With visc the result lands in the
+// alternate face buffers, which then swap with c->u / c->v.
+void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int bc, double* density);
+// u = c0 * u_keep + c1 * u on every face of both grids (velocity TVD-RK3).
+void launch_face_blend(cudaStream_t s, gb2d_ctx* c, double c0, double c1);
 
 // ---- gb2d_solver.cu ----
 Solver* solver_create(int ni, int nj, char* err, size_t errlen);

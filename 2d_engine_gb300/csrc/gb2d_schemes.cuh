@@ -35,6 +35,29 @@ __device__ __forceinline__ bool abs_le(double a, double b) {
   const long long ma = __double_as_longlong(a) & kAbsBits, mb = __double_as_longlong(b) & kAbsBits;
   return ma <= mb && mb <= kInfBits;
 }
+// x < -e and x > e for a finite e > 0, on the integer pipes (false for NaN).
+__device__ __forceinline__ bool lt_neg(double x, double e) {
+  const long long b = __double_as_longlong(x), m = b & kAbsBits;
+  return b < 0 && m > __double_as_longlong(e) && m <= kInfBits;
+}
+__device__ __forceinline__ bool gt_pos(double x, double e) {
+  const long long b = __double_as_longlong(x);
+  return b > __double_as_longlong(e) && b <= kInfBits;
+}
+
+// Smeared Heaviside inside its band |phi| <= eps (HeavisideFunction,
+// PROJECTION_2D.h:1441-1461 and VISCOSITY_2D.h:688-708), with the reference's
+// PI = 3.141592 (MACROS.h:5); oe = 1/eps taken on the host.
+__device__ __forceinline__ double heaviside_band(double phi, double oe) {
+  const double PI_REF = 3.141592, opi = 1.0 / PI_REF;
+  return 0.5 + phi * oe * 0.5 + 0.5 * opi * sin(PI_REF * phi * oe);
+}
+__device__ __forceinline__ double heaviside(double phi, double eps, double oe) {
+  if (lt_neg(phi, eps)) return 0;
+  if (gt_pos(phi, eps)) return 1;
+  return heaviside_band(phi, oe);
+}
+
 __device__ __forceinline__ bool gtz(float x) { return x > 0.0f; }
 __device__ __forceinline__ bool gez(float x) { return x >= 0.0f; }
 __device__ __forceinline__ bool lez(float x) { return x <= 0.0f; }

@@ -292,6 +292,60 @@ def run_gb300(args):
         if step >= args.warmup:
             e2e.append(e0.elapsed_time(e1))
 
+    # Level-set path of the same workload (not part of the metric): one level-set
+    # TVD-RK3 step with its reinitialisation (3 WENO5 sweeps + 3 x 25 reinit sweeps),
+    # for the bit-exact FP64 kernels and the FP32-flux variant.
+    levelset = {}
+    for name, aprec in (("fp64_exact", gb.PRECISION_FP64), ("fp32_flux", gb.PRECISION_MIXED)):
+        cl = gb.Context(N, N, advection_precision=aprec)
+        cl.set_stream(stream.cuda_stream)
+        for f, k in ((gb.FIELD_PHI, "phi"), (gb.FIELD_UA, "ua"), (gb.FIELD_VA, "va")):
+            cl.set(f, case[k])
+        cl.checkpoint_save()
+        cl.synchronize()
+        ts = []
+        for step in range(4):
+            cl.checkpoint_restore()
+            with torch.cuda.stream(stream):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                cl.levelset_rk3(dt)
+                e1.record(stream)
+            e1.synchronize()
+            if step >= 1:
+                ts.append(e0.elapsed_time(e1))
+        levelset[name + "_rk3_ms"] = statistics.median(ts)
+        cl.close()
+
+    # One whole time step of the same workload (not part of the metric): level-set and
+    # reinit RK3, then three SolveForRK stages (ENO3 velocity advection, gravity +
+    # explicit viscosity + wall conditions, projection) and the velocity RK3 blends.
+    time_step = {}
+    for name, aprec, sopts in (("fp64", gb.PRECISION_FP64, fp64), ("mixed", gb.PRECISION_MIXED, mixed)):
+        cs = gb.Context(N, N, advection_precision=aprec)
+        cs.set_stream(stream.cuda_stream)
+        cs.set_flow_params(water_viscosity=1.0, air_viscosity=0.01, gravity=(0.0, -9.8), viscosity=True)
+        for f, k in ((gb.FIELD_PHI, "phi"), (gb.FIELD_U, "u"), (gb.FIELD_V, "v"), (gb.FIELD_P, "p"),
+                     (gb.FIELD_UA, "ua"), (gb.FIELD_VA, "va")):
+            cs.set(f, case[k])
+        cs.checkpoint_save()
+        cs.synchronize()
+        ts, its = [], []
+        for step in range(3):
+            cs.checkpoint_restore()
+            with torch.cuda.stream(stream):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                st_s = cs.advance_time_step(dt, sopts)
+                e1.record(stream)
+            e1.synchronize()
+            if step >= 1:
+                ts.append(e0.elapsed_time(e1))
+                its.append(st_s.iterations)
+        time_step[name + "_ms"] = statistics.median(ts)
+        time_step[name + "_projection_iterations"] = statistics.mean(its)
+        cs.close()
+
     ms_step = max_over_ranks(dist, statistics.mean(ms_m))
     value = ms_step / ws
     e2e_ms = max_over_ranks(dist, statistics.mean(e2e)) / ws
@@ -317,7 +371,8 @@ def run_gb300(args):
                    "iterations_mixed": statistics.mean(it_m), "outer_iterations_mixed": st_m.outer_iterations,
                    "rel_residual_mixed": st_m.rel_residual,
                    "fp64_mgpcg_ms": statistics.mean(ms_64), "iterations_fp64": statistics.mean(it_64), "rel_residual_fp64": st_64.rel_residual,
-                   "mixed_vs_fp64_rel_l2_p": diff, "replicas": ws},
+                   "mixed_vs_fp64_rel_l2_p": diff, "replicas": ws,
+                   "levelset_rk3_1024": levelset, "time_step_1024": time_step},
         "clocks": clk,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

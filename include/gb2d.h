@@ -8,6 +8,9 @@
  *   Velocity_Advection(dt, tid)        EULERIAN_FLUID_SOLVER_2D.h:1886-1889
  *   Projection(dt, tid)                EULERIAN_FLUID_SOLVER_2D.h:2359-2363
  *   level-set/reinit TVD-RK3 blocks    EULERIAN_FLUID_SOLVER_2D.h:1694-1741
+ *   SolveForRK(dt, tid), its gravity /   EULERIAN_FLUID_SOLVER_2D.h:1857-1879, 3249-3268,
+ *   sourcing / wall stages, velocity RK3     2082-2097, 2227-2263, 1753-1794
+ *   AdvanceOneTimeStepThread (order 3)    EULERIAN_FLUID_SOLVER_2D.h:1140, 1694-1794
  *   LEVELSET_2D::ComputeCurvaturesThread  LEVELSET_2D.h:898-990
  *   POISSON_SOLVER::Solve + PCG_METHOD    POISSON_SOLVER.cpp:127-145, PCG_METHOD.cpp:176-264
  * Plain pointers and sizes only.  Every call returns a status (GB2D_OK = 0,
@@ -45,6 +48,7 @@ extern "C" {
 #define GB2D_FIELD_VA 4    /* advecting y-velocity copy (ghost 3): velocity_field_mac_ghost_y */
 #define GB2D_FIELD_P 5     /* pressure, ghost 1 */
 #define GB2D_FIELD_KAPPA 6 /* curvature, no ghost */
+#define GB2D_FIELD_DENSITY 7 /* node density of DetermineDensity (EULERIAN_FLUID_SOLVER_2D.h:81,379), ghost 2 */
 
 #define GB2D_PRECISION_FP64 0  /* FP64 everywhere: reproduces the reference's FP64 results */
 #define GB2D_PRECISION_MIXED 1 /* FP32 where it only affects speed, FP64 where it sets the result (see gb2d_solve_opts) */
@@ -71,6 +75,21 @@ typedef struct {
   int reinit_scaling;      /* scaling_number_for_reinitialization: dtau = dx/scaling */
   int advection_precision; /* GB2D_PRECISION_FP64: exact FP64 WENO; MIXED: FP32 flux evaluation, FP64 state */
 } gb2d_params;
+
+/* Constants of the stages SolveForRK runs around the projection (gravity, viscosity;
+ * EULERIAN_FLUID_SOLVER_2D.h:180-194, 246).  A new context starts with the script
+ * defaults: water_viscosity 1, air_viscosity 0, gravity (0, -9.8), viscosity 0. */
+typedef struct {
+  double water_viscosity;  /* phi > 0 */
+  double air_viscosity;    /* phi <= 0 */
+  double gravity_x, gravity_y;
+  int viscosity;           /* 1: explicit delta-function viscosity (VISCOSITY_2D::ApplyViscosity,
+                              VISCOSITY_2D.h:460-532).  0: none, which is what the reference runs for
+                              air/water even with is_viscosity_active: it never configures that
+                              solver for air/water (only the oil/water branch calls its
+                              InitializeFromScriptBlock, EULERIAN_FLUID_SOLVER_2D.h:645-669), so its
+                              use_delta_function_formulation stays off and ApplyViscosity does nothing */
+} gb2d_flow_params;
 
 /* Pressure-solve options (replace PROJECTION block's tolerance/max_iteration/
  * poisson_solver_type, PROJECTION_2D.h:132-160). */
@@ -102,7 +121,9 @@ int gb2d_field_extent(const gb2d_grid* grid, int field, int* ires, int* jres);
 /* Host <-> device state transfer of one ghost-inclusive field (blocking). */
 int gb2d_set_field(gb2d_ctx* ctx, int field, const double* host);
 int gb2d_get_field(gb2d_ctx* ctx, int field, double* host);
-/* Device-side copy of a whole field (for callers that keep their own device state). */
+/* Device address of a whole field (for callers that keep their own device state).
+ * PHI, and U / V after a viscosity pass, are double-buffered: the address is valid
+ * until the next call that advances the state. */
 int gb2d_field_device_ptr(gb2d_ctx* ctx, int field, double** dptr);
 int gb2d_synchronize(gb2d_ctx* ctx);
 /* Run the context's work on a caller-owned CUDA stream (a cudaStream_t passed as
@@ -153,6 +174,27 @@ int gb2d_curvature(gb2d_ctx* ctx);
 /* One PROJECTION_2D::Solve(dt): density, divergence, sigma*kappa jump, matrix-free
  * ghost-fluid Poisson system, solve (P is the warm start), GFM velocity update (a9-a14). */
 int gb2d_projection(gb2d_ctx* ctx, double dt, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+
+/* Flow constants for the stages below (see gb2d_flow_params). */
+int gb2d_set_flow_params(gb2d_ctx* ctx, const gb2d_flow_params* flow);
+/* ApplyGraivity (EULERIAN_FLUID_SOLVER_2D.h:3249-3268): every U and V face, walls
+ * included, gains dt * gravity. */
+int gb2d_apply_gravity(gb2d_ctx* ctx, double dt);
+/* Sourcing (:2082-2097): DetermineDensity (:2162-2180) into DENSITY, then the
+ * explicit viscosity if gb2d_flow_params.viscosity is set. */
+int gb2d_sourcing(gb2d_ctx* ctx, double dt);
+/* SetupBoundaryConditionForVelocity (:2227-2263): zero normal velocity on the walls. */
+int gb2d_velocity_boundary(gb2d_ctx* ctx);
+/* SolveForRK (:1857-1879): Velocity_Advection, gravity, sourcing and wall
+ * conditions (one fused pass), Projection. */
+int gb2d_solve_for_rk(gb2d_ctx* ctx, double dt, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+/* AdvanceOneTimeStepThread with order_for_time_advancing = 3 (:1694-1794): level-set
+ * and reinitialisation TVD-RK3, then the velocity TVD-RK3 over three SolveForRK
+ * stages.  stats: iterations and outer_iterations summed over the three
+ * projections, rel_residual the largest, the velocity maxima the last.  A stage
+ * that stops at the iteration cap does not end the step; the call then returns
+ * GB2D_ERR_MAX_ITERS after the step. */
+int gb2d_advance_time_step(gb2d_ctx* ctx, double dt, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
 
 /* Standalone pieces of the pressure system for parity checks and for
  * POISSON_SOLVER_2D-style use (a10, a15).  gb2d_poisson_assemble runs the
