@@ -41,7 +41,7 @@ class ParamsT(ctypes.Structure):
 
 class FlowParamsT(ctypes.Structure):
     _fields_ = [("water_viscosity", ctypes.c_double), ("air_viscosity", ctypes.c_double), ("gravity_x", ctypes.c_double),
-                ("gravity_y", ctypes.c_double), ("viscosity", ctypes.c_int)]
+                ("gravity_y", ctypes.c_double), ("cfl_number", ctypes.c_double), ("viscosity", ctypes.c_int)]
 
 
 class SolveOptsT(ctypes.Structure):
@@ -93,6 +93,8 @@ def library():
         "gb2d_velocity_boundary": [vp],
         "gb2d_solve_for_rk": [vp, d, O, S],
         "gb2d_advance_time_step": [vp, d, O, S],
+        "gb2d_cfl_time_step": [vp, ctypes.POINTER(d), vp],
+        "gb2d_advance_frame": [vp, d, ctypes.POINTER(d), O, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
         "gb2d_poisson_solve": [vp, vp, vp, O, S],
@@ -248,11 +250,29 @@ class Context:
             self._check(rc)
         return st
 
-    def set_flow_params(self, water_viscosity=1.0, air_viscosity=0.0, gravity=(0.0, -9.8), viscosity=False):
-        """Constants of SolveForRK's gravity and sourcing stages; viscosity=False is the reference's
-        air/water behaviour (no viscous term), True applies VISCOSITY_2D::ApplyViscosity's explicit term."""
-        f = FlowParamsT(water_viscosity, air_viscosity, gravity[0], gravity[1], int(bool(viscosity)))
+    def set_flow_params(self, water_viscosity=1.0, air_viscosity=0.0, gravity=(0.0, -9.8), viscosity=False, cfl_number=0.5):
+        """Constants of SolveForRK's gravity and sourcing stages and of CFLOneTimeStep; viscosity=False is
+        the reference's air/water behaviour (no viscous term), True applies VISCOSITY_2D::ApplyViscosity's
+        explicit term."""
+        f = FlowParamsT(water_viscosity, air_viscosity, gravity[0], gravity[1], cfl_number, int(bool(viscosity)))
         self._check(self.L.gb2d_set_flow_params(self.h, ctypes.byref(f)))
+
+    def cfl_time_step(self):
+        """CFLOneTimeStep from the current U, V and KAPPA: (dt, (c_f, g_f, v_f, s_f))."""
+        dt = ctypes.c_double()
+        rates = np.zeros(4)
+        self._check(self.L.gb2d_cfl_time_step(self.h, ctypes.byref(dt), _ptr(rates)))
+        return dt.value, tuple(float(r) for r in rates)
+
+    def advance_frame(self, cfl=1.0, prev_dt=0.0, opts=None, allow_max_iters=False):
+        """SIMULATION_WORLD::AdvanceOneFrame: curvature, CFL time step * cfl, one time step. Returns (dt, stats)."""
+        opts = opts or solve_opts()
+        st = SolveStatsT()
+        dt = ctypes.c_double(prev_dt)
+        rc = self.L.gb2d_advance_frame(self.h, cfl, ctypes.byref(dt), ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return dt.value, st
 
     def apply_gravity(self, dt):
         self._check(self.L.gb2d_apply_gravity(self.h, dt))

@@ -172,6 +172,7 @@ int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out
   c->flow.air_viscosity = 0.0;
   c->flow.gravity_x = 0.0;
   c->flow.gravity_y = -9.8;
+  c->flow.cfl_number = 0.5;
   c->flow.viscosity = 0;
   int ni = grid->ni, nj = grid->nj;
   c->base = make_space(ni, nj, grid->x_min, grid->y_min, grid->x_max, grid->y_max);
@@ -505,7 +506,7 @@ int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve
 
 int gb2d_set_flow_params(gb2d_ctx* c, const gb2d_flow_params* f) {
   if (!c || !f || !std::isfinite(f->water_viscosity) || !std::isfinite(f->air_viscosity) || !std::isfinite(f->gravity_x) ||
-      !std::isfinite(f->gravity_y))
+      !std::isfinite(f->gravity_y) || !std::isfinite(f->cfl_number))
     return GB2D_ERR_ARG;
   c->flow = *f;
   return GB2D_OK;
@@ -566,6 +567,30 @@ int gb2d_advance_time_step(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2
   if ((rc = check_launch(c, "advance_time_step"))) return rc;
   if (st) *st = sum;
   return capped ? GB2D_ERR_MAX_ITERS : GB2D_OK;
+}
+
+int gb2d_cfl_time_step(gb2d_ctx* c, double* dt, double* rates) {
+  if (!c || !dt) return GB2D_ERR_ARG;
+  launch_cfl(c->stream, c);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->host_stage, c->sc->cfl, sizeof(c->sc->cfl), cudaMemcpyDeviceToHost, c->stream));
+  int rc = sync_check(c, "cfl_time_step");
+  if (rc) return rc;
+  *dt = c->host_stage[0];
+  if (rates)
+    for (int k = 0; k < 4; ++k) rates[k] = c->host_stage[1 + k];
+  return GB2D_OK;
+}
+
+int gb2d_advance_frame(gb2d_ctx* c, double cfl, double* dt, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
+  if (!c || !dt || !o || !std::isfinite(cfl) || !std::isfinite(*dt)) return GB2D_ERR_ARG;
+  int rc = gb2d_curvature(c);
+  if (rc) return rc;
+  double d = 0;
+  if ((rc = gb2d_cfl_time_step(c, &d, nullptr))) return rc;
+  if (d == 0) d = *dt;  // DetermineTimeStep keeps the previous step (SIMULATION_WORLD.h:1201-1204)
+  d = d * cfl;
+  *dt = d;
+  return gb2d_advance_time_step(c, d, o, st);
 }
 
 int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {

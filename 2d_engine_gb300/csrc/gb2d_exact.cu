@@ -385,14 +385,6 @@ __global__ void k_apply_exact(const double* __restrict__ bx, const double* __res
   }
 }
 
-__device__ __forceinline__ void block_max_bits(unsigned long long b, unsigned long long* out) {
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long w = __shfl_xor_sync(0xffffffffu, b, o);
-    b = w > b ? w : b;
-  }
-  if ((threadIdx.x & 31) == 0) atomicMax(out, b);
-}
-
 // UpdateVelocityByPressureGradientVariableDensity (PROJECTION_2D.h:1297-1416):
 // same-sign faces use the node density on the + side, interface faces the
 // smeared-Heaviside density of the face-averaged phi (eps = 1.5 dx) and the
@@ -424,10 +416,8 @@ __global__ void k_velocity_update(const double* __restrict__ phi_a, const double
       else if (gtz(l0))
         *w -= dt * (dp - gam) * odh * od;
     }
-    // max(|w|, m) as (|w| > m ? |w| : m): a NaN never replaces the maximum
-    const unsigned long long ab = (unsigned long long)(__double_as_longlong(*w) & kAbsBits);
     unsigned long long& m = xc ? mx : my;
-    if (ab > m && ab <= (unsigned long long)kInfBits) m = ab;
+    m = abs_max_bits(*w, m);
   };
   GB_FOR_IJ(i, j, ni, nj) {
     face(true, i, j);

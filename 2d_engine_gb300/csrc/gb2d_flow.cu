@@ -1,7 +1,8 @@
 // The stages of SolveForRK around the projection (EULERIAN_FLUID_SOLVER_2D.h:1857-1879)
 // and the velocity TVD-RK3 blends (:1753-1794): gravity, DetermineDensity, the
 // explicit delta-function viscosity (VISCOSITY_2D.h:460-532) and the wall
-// conditions, fused into one pass over the two MAC face grids.
+// conditions, fused into one pass over the two MAC face grids; and the CFL time
+// step (:3517-3637).
 // Built with --fmad=false, in the reference's association order, like
 // gb2d_exact.cu: the results are the reference's FP64 results bit for bit, except
 // where the smeared Heaviside's sine (the only libm call) differs in the last ulp.
@@ -144,7 +145,73 @@ __global__ void k_face_blend(const double* __restrict__ ku_a, double* __restrict
   }
 }
 
+// Largest |u|, |v| over the MAC grids and |kappa| over the nodes (CFLOneTimeStep's loops).
+__global__ void k_cfl_max(const double* __restrict__ u_a, const double* __restrict__ v_a, const double* __restrict__ kappa,
+                          int ni, int nj, Scalars* sc) {
+  const DField u = dfield((double*)u_a, 2, ni + 1, nj), v = dfield((double*)v_a, 2, ni, nj + 1);
+  unsigned long long mu = 0, mv = 0, mk = 0;
+  GB_FOR_IJ(i, j, ni + 1, nj + 1) {
+    if (j < nj) mu = abs_max_bits(GB_AT(u, i, j), mu);
+    if (i < ni) mv = abs_max_bits(GB_AT(v, i, j), mv);
+    if (i < ni && j < nj) mk = abs_max_bits(kappa[i + (size_t)j * ni], mk);
+  }
+  block_max_bits(mu, &sc->cfl_bits[0]);
+  block_max_bits(mv, &sc->cfl_bits[1]);
+  block_max_bits(mk, &sc->cfl_bits[2]);
+}
+
+struct CflArgs {
+  double xs_odx, ys_ody;          // 1/dx of the x-face grid, 1/dy of the y-face grid
+  double ody, odx2, ody2, dx, dy; // base grid
+  double water_visc, air_visc, water_rho, air_rho, sigma, cfl_number;
+};
+
+// The rest of CFLOneTimeStep for air/water (EULERIAN_FLUID_SOLVER_2D.h:3562-3637),
+// in the reference's order; one thread.
+__global__ void k_cfl_final(CflArgs a, Scalars* sc) {
+  const double u_max = __longlong_as_double((long long)sc->cfl_bits[0]);
+  const double v_max = __longlong_as_double((long long)sc->cfl_bits[1]);
+  const double k_max = __longlong_as_double((long long)sc->cfl_bits[2]);
+  const double c_f = (u_max * a.xs_odx + v_max * a.ys_ody);
+  const double g_f = sqrt(9.8 * a.ody);  // the constant 9.8, as the reference writes it
+  const double rw = a.water_visc / a.water_rho, ra = a.air_visc / a.air_rho;
+  const double v_f = (rw < ra ? ra : rw) * (2 * a.odx2 + 2 * a.ody2);
+  const double rmin = a.water_rho > a.air_rho ? a.air_rho : a.water_rho;
+  const double hmin = a.dy < a.dx ? a.dy : a.dx;
+  const double s_f = sqrt(a.sigma * k_max / (rmin * (hmin * hmin)));
+  const double CFL = 0.5 * (c_f + v_f + sqrt((c_f + v_f) * (c_f + v_f) + 4 * (g_f * g_f) + 4 * (s_f * s_f)));
+  double dt = a.cfl_number / CFL;
+  if (CFL == 0) dt = 0;
+  sc->cfl[0] = dt;
+  sc->cfl[1] = c_f;
+  sc->cfl[2] = g_f;
+  sc->cfl[3] = v_f;
+  sc->cfl[4] = s_f;
+}
+
 }  // namespace
+
+void launch_cfl(cudaStream_t s, gb2d_ctx* c) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  cudaMemsetAsync(c->sc->cfl_bits, 0, sizeof(c->sc->cfl_bits), s);
+  k_cfl_max<<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(c->u, c->v, c->kappa, ni, nj, c->sc);
+  CflArgs a;
+  a.xs_odx = c->xs.odx;
+  a.ys_ody = c->ys.ody;
+  a.ody = c->base.ody;
+  a.odx2 = c->base.odx2;
+  a.ody2 = c->base.ody2;
+  a.dx = c->base.dx;
+  a.dy = c->base.dy;
+  a.water_visc = c->flow.water_viscosity;
+  a.air_visc = c->flow.air_viscosity;
+  a.water_rho = c->prm.water_density;
+  a.air_rho = c->prm.air_density;
+  a.sigma = c->prm.surface_tension;
+  a.cfl_number = c->flow.cfl_number;
+  k_cfl_final<<<1, 1, 0, s>>>(a, c->sc);
+  GB_LAUNCHED(2);
+}
 
 void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int bc, double* density) {
   const int ni = c->grid.ni, nj = c->grid.nj;

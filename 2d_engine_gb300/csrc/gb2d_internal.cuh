@@ -105,6 +105,8 @@ struct Scalars {
   int flag;        // non-finite / zero-gradient detections
   int pad;
   unsigned long long maxu_bits, maxv_bits;  // max |u|, |v| of the velocity update
+  unsigned long long cfl_bits[3];           // max |u|, |v|, |kappa| for the CFL time step
+  double cfl[5];                            // CFL dt, c_f, g_f, v_f, s_f
 };
 
 struct Solver;  // defined in gb2d_solver.cu
@@ -177,6 +179,8 @@ void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst
 void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int bc, double* density);
 // u = c0 * u_keep + c1 * u on every face of both grids (velocity TVD-RK3).
 void launch_face_blend(cudaStream_t s, gb2d_ctx* c, double c0, double c1);
+// CFLOneTimeStep into c->sc->cfl (dt, c_f, g_f, v_f, s_f).
+void launch_cfl(cudaStream_t s, gb2d_ctx* c);
 
 // ---- gb2d_solver.cu ----
 Solver* solver_create(int ni, int nj, char* err, size_t errlen);

@@ -58,6 +58,21 @@ __device__ __forceinline__ double heaviside(double phi, double eps, double oe) {
   return heaviside_band(phi, oe);
 }
 
+// Maximum of non-negative doubles by their bit patterns (which order as
+// integers): a warp's maximum, then one atomicMax into *out.
+__device__ __forceinline__ void block_max_bits(unsigned long long b, unsigned long long* out) {
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, b, o);
+    b = w > b ? w : b;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(out, b);
+}
+// max(|x|, m) as the reference's `if (m <= |x|) m = |x|`: NaN never replaces m.
+__device__ __forceinline__ unsigned long long abs_max_bits(double x, unsigned long long m) {
+  const unsigned long long ab = (unsigned long long)(__double_as_longlong(x) & kAbsBits);
+  return (ab > m && ab <= (unsigned long long)kInfBits) ? ab : m;
+}
+
 __device__ __forceinline__ bool gtz(float x) { return x > 0.0f; }
 __device__ __forceinline__ bool gez(float x) { return x >= 0.0f; }
 __device__ __forceinline__ bool lez(float x) { return x <= 0.0f; }

@@ -11,6 +11,7 @@
  *   SolveForRK(dt, tid), its gravity /   EULERIAN_FLUID_SOLVER_2D.h:1857-1879, 3249-3268,
  *   sourcing / wall stages, velocity RK3     2082-2097, 2227-2263, 1753-1794
  *   AdvanceOneTimeStepThread (order 3)    EULERIAN_FLUID_SOLVER_2D.h:1140, 1694-1794
+ *   CFLOneTimeStep, AdvanceOneFrame       EULERIAN_FLUID_SOLVER_2D.h:3517-3637, SIMULATION_WORLD.h:1094-1146
  *   LEVELSET_2D::ComputeCurvaturesThread  LEVELSET_2D.h:898-990
  *   POISSON_SOLVER::Solve + PCG_METHOD    POISSON_SOLVER.cpp:127-145, PCG_METHOD.cpp:176-264
  * Plain pointers and sizes only.  Every call returns a status (GB2D_OK = 0,
@@ -78,11 +79,13 @@ typedef struct {
 
 /* Constants of the stages SolveForRK runs around the projection (gravity, viscosity;
  * EULERIAN_FLUID_SOLVER_2D.h:180-194, 246).  A new context starts with the script
- * defaults: water_viscosity 1, air_viscosity 0, gravity (0, -9.8), viscosity 0. */
+ * defaults: water_viscosity 1, air_viscosity 0, gravity (0, -9.8), cfl_number 0.5,
+ * viscosity 0. */
 typedef struct {
   double water_viscosity;  /* phi > 0 */
   double air_viscosity;    /* phi <= 0 */
   double gravity_x, gravity_y;
+  double cfl_number;       /* CFLOneTimeStep's dt = cfl_number / CFL (script default 0.5) */
   int viscosity;           /* 1: explicit delta-function viscosity (VISCOSITY_2D::ApplyViscosity,
                               VISCOSITY_2D.h:460-532).  0: none, which is what the reference runs for
                               air/water even with is_viscosity_active: it never configures that
@@ -195,6 +198,17 @@ int gb2d_solve_for_rk(gb2d_ctx* ctx, double dt, const gb2d_solve_opts* opts, gb2
  * that stops at the iteration cap does not end the step; the call then returns
  * GB2D_ERR_MAX_ITERS after the step. */
 int gb2d_advance_time_step(gb2d_ctx* ctx, double dt, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+
+/* CFLOneTimeStep (EULERIAN_FLUID_SOLVER_2D.h:3517-3637) from U, V and KAPPA as they
+ * stand (run gb2d_curvature first, as SIMULATION_WORLD::AdvanceOneFrame does):
+ * cfl_number / CFL, or 0 where CFL is 0.  rates (may be NULL) receives the
+ * advection, gravity, viscosity and surface-tension rates c_f, g_f, v_f, s_f. */
+int gb2d_cfl_time_step(gb2d_ctx* ctx, double* dt, double* rates);
+/* SIMULATION_WORLD::AdvanceOneFrame (SIMULATION_WORLD.h:1094-1146, 1194-1207):
+ * curvature, dt = CFLOneTimeStep() * cfl (the previous dt in place of a zero
+ * CFLOneTimeStep), then gb2d_advance_time_step(dt).  *dt: the previous time step
+ * in, the step taken out. */
+int gb2d_advance_frame(gb2d_ctx* ctx, double cfl, double* dt, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
 
 /* Standalone pieces of the pressure system for parity checks and for
  * POISSON_SOLVER_2D-style use (a10, a15).  gb2d_poisson_assemble runs the

@@ -907,3 +907,43 @@ out:
   free(kv_a);
   return rc;
 }
+
+/* CFLOneTimeStep for air/water (EULERIAN_FLUID_SOLVER_2D.h:3517-3637): the
+ * advection rate from the largest |u| and |v| over the MAC grids (divided by
+ * their own spacings), gravity sqrt(9.8 / dy) (the constant, not the gravity
+ * vector), viscosity max(mu_w/rho_w, mu_a/rho_a) (2/dx^2 + 2/dy^2) (whether or not
+ * the viscous term is applied) and surface tension from the largest |kappa|;
+ * returns cfl_number / CFL, or 0 where CFL is 0.  cf/gf/vf/sf (may be null)
+ * receive the four rates as the reference prints them. */
+double or_cfl_time_step(const or_grid* gr, const or_params* pr, const or_flow* fl, const double* u_a, const double* v_a,
+                        const double* kappa, double cfl_number, double rates[4]) {
+  int ni = gr->ni, nj = gr->nj;
+  space_t b = base_space(gr), xs = xface_space(gr), ys = yface_space(gr);
+  fld u = F((double*)u_a, 2, ni + 1, nj), v = F((double*)v_a, 2, ni, nj + 1);
+  double u_max = 0, v_max = 0, k_max = 0;
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i <= ni; ++i)
+      if (u_max <= fabs(AT(u, i, j))) u_max = fabs(AT(u, i, j));
+  for (int j = 0; j <= nj; ++j)
+    for (int i = 0; i < ni; ++i)
+      if (v_max <= fabs(AT(v, i, j))) v_max = fabs(AT(v, i, j));
+  double c_f = (u_max * xs.odx + v_max * ys.ody);
+  double g_f = sqrt(9.8 * b.ody);
+  double rw = fl->water_viscosity / pr->water_density, ra = fl->air_viscosity / pr->air_density;
+  double v_f = (rw < ra ? ra : rw) * (2 * b.odx2 + 2 * b.ody2);
+  for (size_t k = 0; k < (size_t)ni * nj; ++k)
+    if (fabs(kappa[k]) >= k_max) k_max = fabs(kappa[k]);
+  double rmin = pr->water_density > pr->air_density ? pr->air_density : pr->water_density;
+  double hmin = b.dx > b.dy ? b.dy : b.dx;
+  double s_f = sqrt(pr->surface_tension * k_max / (rmin * (hmin * hmin)));
+  double CFL = 0.5 * (c_f + v_f + sqrt((c_f + v_f) * (c_f + v_f) + 4 * (g_f * g_f) + 4 * (s_f * s_f)));
+  double dt = cfl_number / CFL;
+  if (CFL == 0) dt = 0;
+  if (rates) {
+    rates[0] = c_f;
+    rates[1] = g_f;
+    rates[2] = v_f;
+    rates[3] = s_f;
+  }
+  return dt;
+}

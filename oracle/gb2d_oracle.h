@@ -97,6 +97,11 @@ int or_solve_for_rk(const or_grid* gr, const or_params* pr, const or_flow* fl, d
 int or_time_step(const or_grid* gr, const or_params* pr, const or_flow* fl, double* phi, double* u, double* v, double* ua,
                  double* va, double* p, double* kappa, double* density, double dt, or_stats* st);
 
+/* CFLOneTimeStep (EULERIAN_FLUID_SOLVER_2D.h:3517-3637) with kappa from or_curvature;
+ * rates (may be null) receives c_f, g_f, v_f, s_f. */
+double or_cfl_time_step(const or_grid* gr, const or_params* pr, const or_flow* fl, const double* u, const double* v,
+                        const double* kappa, double cfl_number, double rates[4]);
+
 /* a10 in matrix-free form.  bx: x-faces (ni+1) x nj (face i between nodes i-1 and i),
  * by: y-faces ni x (nj+1), diag, rhs: ni x nj.  phi must already hold the ghost
  * state of the projection (or_curvature fills it).  kappa: ni x nj. */

@@ -69,6 +69,8 @@ def lib():
         L.or_pcg_ic0.argtypes = [G, R, P, P, P, P, P, S]
         L.or_fill_ghost_extrapolate.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         W = ctypes.POINTER(Flow)
+        L.or_cfl_time_step.argtypes = [G, R, W, P, P, P, d, P]
+        L.or_cfl_time_step.restype = d
         L.or_apply_gravity.argtypes = [G, W, P, P, d]
         L.or_sourcing.argtypes = [G, R, W, P, P, P, P, d]
         L.or_velocity_bc.argtypes = [G, P, P]
@@ -182,3 +184,11 @@ def time_step(g, pr, fl, phi, u, v, ua, va, p, kappa, density, dt):
     _check(lib().or_time_step(ctypes.byref(g), ctypes.byref(pr), ctypes.byref(fl), _p(phi), _p(u), _p(v), _p(ua), _p(va),
                               _p(p), _p(kappa), _opt(density), dt, ctypes.byref(st)), "time_step")
     return st
+
+
+def cfl_time_step(g, pr, fl, u, v, kappa, cfl_number=0.5):
+    """CFLOneTimeStep: (dt, (c_f, g_f, v_f, s_f))."""
+    rates = np.zeros(4)
+    dt = lib().or_cfl_time_step(ctypes.byref(g), ctypes.byref(pr), ctypes.byref(fl), _p(u), _p(v), _p(kappa), cfl_number,
+                                _p(rates))
+    return dt, tuple(rates)

@@ -19,6 +19,7 @@ tests/golden/cases.py and stores inputs and outputs:
   solve_for_rk        one SolveForRK stage (viscosity configured)
   time_step           AdvanceOneTimeStepThread (order 3), without viscosity (the
                       reference's air/water setup) and with it configured
+  cfl                 CFLOneTimeStep after ComputeCurvaturesThread
 
 Usage:  python tests/golden/make_golden.py   (needs the reference sources)
 """
@@ -89,6 +90,11 @@ def make_case(name, c, dt, pcg_tolerance, flow=True):
     s.set(R.PHI, c["phi"]); s.curvature()
     out["curv_kappa"], out["curv_phi"] = s.get(R.KAPPA), s.get(R.PHI)
     s.close()
+    if flow:
+        s = R.RefSim(ni, nj, 0.0, 0.0, xm, ym, **PHYS, **FLOW)
+        s.set(R.PHI, c["phi"]); s.set(R.U, c["u"]); s.set(R.V, c["v"]); s.curvature()
+        out["cfl_dt"] = s.cfl_dt()
+        s.close()
 
     s = mk(pcg_tolerance=pcg_tolerance, pcg_max_iterations=200000)
     s.set(R.PHI, c["phi"]); s.set(R.U, c["u"]); s.set(R.V, c["v"]); s.set(R.P, c["p"])

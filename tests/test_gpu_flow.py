@@ -125,3 +125,37 @@ def test_time_step_mixed_close_to_reference(gb, name):
     for f, k in ((gb.FIELD_U, "u"), (gb.FIELD_V, "v")):
         assert rel_l2(c.get(f), g[f"step1_{k}"]) <= 1e-4, k
     c.close()
+
+
+@pytest.mark.parametrize("name", FLOW_NAMES)
+def test_cfl_time_step(gb, name):
+    g = load_golden(name)
+    c = make_ctx(gb, g, 0)
+    c.curvature()
+    dt, rates = c.cfl_time_step()
+    assert dt == float(g["cfl_dt"])
+    assert all(r > 0 for r in rates)
+    c.close()
+
+
+@pytest.mark.parametrize("name", FLOW_NAMES)
+def test_advance_frame_matches_oracle(gb, oracle, name):
+    """SIMULATION_WORLD::AdvanceOneFrame: curvature, CFL time step, one order-3 step."""
+    g = load_golden(name)
+    ni, nj = int(g["ni"]), int(g["nj"])
+    c = make_ctx(gb, g, 1)
+    opts = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=SOLVE_TOL, max_iterations=20000)
+    dt, st = c.advance_frame(cfl=1.0, prev_dt=0.0, opts=opts)
+    gr = oracle.grid(ni, nj, 0.0, 0.0, float(g["x_max"]), float(g["y_max"]))
+    pr = oracle.params(pcg_tolerance=float(g["pcg_tolerance"]), pcg_max_iterations=200000)
+    fl = oracle.flow(viscosity=True, **FLOW)
+    phi, u, v, ua, va, p = (g[k].copy() for k in ("phi", "u", "v", "ua", "va", "p"))
+    k = np.zeros((nj, ni))
+    oracle.curvature(gr, phi, k)
+    want_dt, _ = oracle.cfl_time_step(gr, pr, fl, u, v, k, 0.5)
+    assert dt == want_dt * 1.0
+    oracle.time_step(gr, pr, fl, phi, u, v, ua, va, p, k, None, dt)
+    np.testing.assert_array_equal(c.get(gb.FIELD_PHI), phi)
+    for f, want in ((gb.FIELD_P, p), (gb.FIELD_U, u), (gb.FIELD_V, v)):
+        assert rel_l2(c.get(f), want) <= STEP_TOL
+    c.close()

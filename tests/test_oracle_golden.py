@@ -141,3 +141,15 @@ def test_time_step(oracle, name, visc):
     assert st.iterations > 0
     for got, key in zip((phi, u, v, ua, va, p, density), FIELDS6 + ("density",)):
         np.testing.assert_array_equal(got, g[f"step{visc}_{key}"])
+
+
+@pytest.mark.parametrize("name", FLOW_NAMES)
+def test_cfl_time_step(oracle, name):
+    g = load_golden(name)
+    gr, ni, nj = setup(oracle, g)
+    phi = g["phi"].copy()
+    k = np.zeros((nj, ni))
+    oracle.curvature(gr, phi, k)
+    dt, rates = oracle.cfl_time_step(gr, oracle.params(), oracle.flow(), g["u"], g["v"], k, 0.5)
+    assert dt == float(g["cfl_dt"]) and dt > 0
+    assert all(r > 0 for r in rates)
