@@ -191,11 +191,17 @@ __global__ void k_blend(const double* __restrict__ keep_a, double* phi_a, int ni
 struct EnoArgs {
   int ni, nj;
   Space xs, ys;
+  double o3[2][2];  // 1/(3h) of x and y for the x-face grid [0] and the y-face grid [1], host IEEE quotients
+  // FP32 path, per face grid: 1/h, 1/(2h), 1/(3h), h for x ([0..3]) and y ([4..7])
+  float xs_f[8], ys_f[8];
 };
 
 // ENO3rd on both MAC components (ADVECTION_METHOD_2D.h:2038-2231) as called by
 // Solve_Velocity (ADVECTION_2D.cpp:83-122): both read only the advecting copies
 // UA/VA (already refreshed from U/V), so one launch updates U and V.
+// MIXED: divided differences and the ENO selection in FP32 (first differences,
+// face velocities and the update in FP64).
+template <bool MIXED>
 __global__ void k_eno3(double* __restrict__ u_a, double* __restrict__ v_a, const double* __restrict__ ua_a, const double* __restrict__ va_a,
                        EnoArgs a, double dt) {
   int ni = a.ni, nj = a.nj;
@@ -203,12 +209,27 @@ __global__ void k_eno3(double* __restrict__ u_a, double* __restrict__ v_a, const
   auto face = [&](bool xc, int i, int j) {
     const DField& g = xc ? ua : va;
     const Space& s = xc ? a.xs : a.ys;
+    const float* sf = xc ? a.xs_f : a.ys_f;
     double q[7];
-    for (int m = 0; m < 7; ++m) q[m] = __ldg(&GB_AT(g, i - 3 + m, j));
     double mx, px, my, py;
-    eno3_pair(q, s.odx, s.o2dx, s.odx / 3, s.dx, mx, px);
+    for (int m = 0; m < 7; ++m) q[m] = __ldg(&GB_AT(g, i - 3 + m, j));
+    if (MIXED) {
+      float m32, p32;
+      eno3_pair_f32(q, sf[0], sf[1], sf[2], sf[3], m32, p32);
+      mx = widen(m32);
+      px = widen(p32);
+    } else {
+      eno3_pair(q, s.odx, s.o2dx, a.o3[xc ? 0 : 1][0], s.dx, mx, px);
+    }
     for (int m = 0; m < 7; ++m) q[m] = __ldg(&GB_AT(g, i, j - 3 + m));
-    eno3_pair(q, s.ody, s.o2dy, s.ody / 3, s.dy, my, py);
+    if (MIXED) {
+      float m32, p32;
+      eno3_pair_f32(q, sf[4], sf[5], sf[6], sf[7], m32, p32);
+      my = widen(m32);
+      py = widen(p32);
+    } else {
+      eno3_pair(q, s.ody, s.o2dy, a.o3[xc ? 0 : 1][1], s.dy, my, py);
+    }
     double uu, vv;
     if (xc) {
       uu = GB_AT(ua, i, j);
@@ -544,8 +565,24 @@ void launch_blend(cudaStream_t s, const gb2d_ctx* c, const double* keep, double*
 }
 
 void launch_eno3(cudaStream_t s, const gb2d_ctx* c, double dt) {
-  EnoArgs a{c->grid.ni, c->grid.nj, c->xs, c->ys};
-  k_eno3<<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, dt);
+  EnoArgs a;
+  a.ni = c->grid.ni;
+  a.nj = c->grid.nj;
+  a.xs = c->xs;
+  a.ys = c->ys;
+  const Space* sp[2] = {&c->xs, &c->ys};
+  float* out[2] = {a.xs_f, a.ys_f};
+  for (int g = 0; g < 2; ++g) {
+    const Space& q = *sp[g];
+    const double v[8] = {q.odx, q.o2dx, q.odx / 3, q.dx, q.ody, q.o2dy, q.ody / 3, q.dy};
+    for (int k = 0; k < 8; ++k) out[g][k] = (float)v[k];
+    a.o3[g][0] = q.odx / 3;
+    a.o3[g][1] = q.ody / 3;
+  }
+  if (c->prm.advection_precision == GB2D_PRECISION_MIXED)
+    k_eno3<true><<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, dt);
+  else
+    k_eno3<false><<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, dt);
   GB_LAUNCHED(1);
 }
 

@@ -27,6 +27,10 @@ Smear make_smear(double lo, double hi) {
   return s;
 }
 
+struct SmearF {
+  float lo, d, at0, at1;
+};
+
 struct FlowArgs {
   int ni, nj;
   int grav, bc;        // add dt * gravity to every face; zero the wall faces' normal velocity
@@ -36,6 +40,9 @@ struct FlowArgs {
   Smear rho, mu;       // face density and viscosity
   double coef0, coef1; // dt * (1 / rho.at0), dt * (1 / rho.at1)
   double air, water;   // node densities of DetermineDensity
+  // FP32 viscous-flux path
+  float odx_f, ody_f, eps_f, oe_f, dt_f, coef0_f, coef1_f;
+  SmearF rho_f, mu_f;
 };
 
 __device__ __forceinline__ double smear(double l, const Smear& s, const FlowArgs& a) {
@@ -52,15 +59,33 @@ __device__ __forceinline__ double face_coef(double l, const FlowArgs& a) {
   return a.dt * (1 / (a.rho.lo + a.rho.d * heaviside_band(l, a.oe)));
 }
 
+// FP32 forms for the viscous flux of the mixed path.
+__device__ __forceinline__ float heaviside_band_f(float phi, float oe) {
+  const float PI_REF = 3.141592f, opi = 1.0f / PI_REF;
+  return 0.5f + phi * oe * 0.5f + 0.5f * opi * __sinf(PI_REF * phi * oe);
+}
+__device__ __forceinline__ float smear_f(float l, const SmearF& s, const FlowArgs& a) {
+  if (l < -a.eps_f) return s.at0;
+  if (l > a.eps_f) return s.at1;
+  return s.lo + s.d * heaviside_band_f(l, a.oe_f);
+}
+__device__ __forceinline__ float face_coef_f(float l, const FlowArgs& a) {
+  if (l < -a.eps_f) return a.coef0_f;
+  if (l > a.eps_f) return a.coef1_f;
+  return __fdividef(a.dt_f, a.rho_f.lo + a.rho_f.d * heaviside_band_f(l, a.oe_f));
+}
+
 // One pass over the (ni+1) x (nj+1) face index space: x-face (i, j), i <= ni,
 // j < nj; y-face (i, j), i < ni, j <= nj; node (i, j) for the density.
 //   VISC = false: gravity and wall conditions in place (u_out may equal u_in).
 //   VISC = true:  ApplyViscosity from the copies temp_x / temp_y of the faces after
 //                 gravity, whose values off the face grids are zero (the reference's
 //                 freshly initialised temporaries), written to u_out / v_out.
+//   MIXED (with VISC): the viscous flux in FP32 from FP64 velocity differences (the
+//                 face values and the update stay FP64).
 // density (ghost 2, may be null) receives DetermineDensity (:2162-2180): air where
 // phi <= 0, water where phi > 0, unchanged for NaN.
-template <bool VISC>
+template <bool VISC, bool MIXED>
 __global__ void k_flow(const double* __restrict__ phi_a, const double* u_in_a, const double* v_in_a, double* u_out_a,
                        double* v_out_a, double* __restrict__ dens_a, FlowArgs a) {
   const int ni = a.ni, nj = a.nj;
@@ -78,6 +103,17 @@ __global__ void k_flow(const double* __restrict__ phi_a, const double* u_in_a, c
     return a.grav ? w + a.gy : w;
   };
   auto P = [&](int i, int j) -> double { return __ldg(&GB_AT(phi, i, j)); };
+  // Face values without gravity: off the grids -gravity, so that differences of
+  // these equal differences of the temporaries.
+  auto ru = [&](int i, int j) -> double {
+    if (i < 0 || i > ni || j < 0 || j >= nj) return a.grav ? -a.gx : 0.0;
+    return GB_AT(ui, i, j);
+  };
+  auto rv = [&](int i, int j) -> double {
+    if (i < 0 || i >= ni || j < 0 || j > nj) return a.grav ? -a.gy : 0.0;
+    return GB_AT(vi, i, j);
+  };
+  auto Pf = [&](int i, int j) -> float { return narrow(__ldg(&GB_AT(phi, i, j))); };
   GB_FOR_IJ(i, j, ni + 1, nj + 1) {
     if (dens_a && i < ni && j < nj) {
       const double l = P(i, j);
@@ -89,7 +125,21 @@ __global__ void k_flow(const double* __restrict__ phi_a, const double* u_in_a, c
     }
     if (j < nj) {  // x-face between nodes (i-1, j) and (i, j)
       double w;
-      if (VISC) {
+      if (VISC && MIXED) {
+        const float pl = Pf(i - 1, j), pc = Pf(i, j);
+        const float cu = 0.25f * (pl + pc + Pf(i - 1, j + 1) + Pf(i, j + 1));
+        const float cd = 0.25f * (Pf(i - 1, j - 1) + Pf(i, j - 1) + pl + pc);
+        const float mu_cu = smear_f(cu, a.mu_f, a), mu_cd = smear_f(cd, a.mu_f, a);
+        const float mu_r = smear_f(pc, a.mu_f, a), mu_c = smear_f(pl, a.mu_f, a);
+        const float coef = face_coef_f(0.5f * (pl + pc), a);
+        const double u0 = ru(i, j);
+        const float dxp = narrow(ru(i + 1, j) - u0), dxm = narrow(u0 - ru(i - 1, j));
+        const float dyp = narrow(ru(i, j + 1) - u0), dym = narrow(u0 - ru(i, j - 1));
+        const float dvu = narrow(rv(i, j + 1) - rv(i - 1, j + 1)), dvd = narrow(rv(i, j) - rv(i - 1, j));
+        const float first = 2.0f * coef * a.odx_f * (mu_r * a.odx_f * dxp - mu_c * a.odx_f * dxm);
+        const float second = coef * a.ody_f * (mu_cu * (a.ody_f * dyp + a.odx_f * dvu) - mu_cd * (a.ody_f * dym + a.odx_f * dvd));
+        w = (a.grav ? u0 + a.gx : u0) + widen(first + second);
+      } else if (VISC) {
         const double pl = P(i - 1, j), pc = P(i, j);
         const double half = 0.5 * (pl + pc);
         const double cu = 0.25 * (pl + pc + P(i - 1, j + 1) + P(i, j + 1));
@@ -111,7 +161,21 @@ __global__ void k_flow(const double* __restrict__ phi_a, const double* u_in_a, c
     }
     if (i < ni) {  // y-face between nodes (i, j-1) and (i, j)
       double w;
-      if (VISC) {
+      if (VISC && MIXED) {
+        const float pb = Pf(i, j - 1), pc = Pf(i, j);
+        const float cu = 0.25f * (pb + Pf(i + 1, j - 1) + pc + Pf(i + 1, j));
+        const float cl = 0.25f * (Pf(i - 1, j - 1) + pb + Pf(i - 1, j) + pc);
+        const float mu_cu = smear_f(cu, a.mu_f, a), mu_cl = smear_f(cl, a.mu_f, a);
+        const float mu_u = smear_f(pc, a.mu_f, a), mu_c = smear_f(pb, a.mu_f, a);
+        const float coef = face_coef_f(0.5f * (pb + pc), a);
+        const double v0 = rv(i, j);
+        const float dyp = narrow(rv(i, j + 1) - v0), dym = narrow(v0 - rv(i, j - 1));
+        const float dur = narrow(ru(i + 1, j) - ru(i + 1, j - 1)), dul = narrow(ru(i, j) - ru(i, j - 1));
+        const float dxp = narrow(rv(i + 1, j) - v0), dxm = narrow(v0 - rv(i - 1, j));
+        const float first = 2.0f * coef * a.ody_f * (mu_u * a.ody_f * dyp - mu_c * a.ody_f * dym);
+        const float second = coef * a.odx_f * (mu_cu * (a.ody_f * dur + a.odx_f * dxp) - mu_cl * (a.ody_f * dul + a.odx_f * dxm));
+        w = (a.grav ? v0 + a.gy : v0) + widen(first + second);
+      } else if (VISC) {
         const double pb = P(i, j - 1), pc = P(i, j);
         const double half = 0.5 * (pb + pc);
         const double cu = 0.25 * (pb + P(i + 1, j - 1) + pc + P(i + 1, j));
@@ -233,9 +297,22 @@ void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int
   a.coef1 = dt * (1 / a.rho.at1);
   a.air = c->prm.air_density;
   a.water = c->prm.water_density;
+  a.odx_f = (float)a.odx;
+  a.ody_f = (float)a.ody;
+  a.eps_f = (float)a.eps;
+  a.oe_f = (float)a.oe;
+  a.dt_f = (float)dt;
+  a.coef0_f = (float)a.coef0;
+  a.coef1_f = (float)a.coef1;
+  a.rho_f = SmearF{(float)a.rho.lo, (float)a.rho.d, (float)a.rho.at0, (float)a.rho.at1};
+  a.mu_f = SmearF{(float)a.mu.lo, (float)a.mu.d, (float)a.mu.at0, (float)a.mu.at1};
   const double* phi = c->phi_buf[c->phi_cur];
+  const bool mixed = c->prm.advection_precision == GB2D_PRECISION_MIXED;
   if (visc) {
-    k_flow<true><<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(phi, c->u, c->v, c->u_alt, c->v_alt, density, a);
+    if (mixed)
+      k_flow<true, true><<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(phi, c->u, c->v, c->u_alt, c->v_alt, density, a);
+    else
+      k_flow<true, false><<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(phi, c->u, c->v, c->u_alt, c->v_alt, density, a);
     double* t = c->u;
     c->u = c->u_alt;
     c->u_alt = t;
@@ -243,7 +320,7 @@ void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int
     c->v = c->v_alt;
     c->v_alt = t;
   } else {
-    k_flow<false><<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(phi, c->u, c->v, c->u, c->v, density, a);
+    k_flow<false, false><<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(phi, c->u, c->v, c->u, c->v, density, a);
   }
   GB_LAUNCHED(1);
 }

@@ -196,35 +196,55 @@ __device__ __forceinline__ bool godunov_h(R s, R mx, R px, R my, R py, R& h) {
   return true;
 }
 
-// ENO3 one-sided derivatives by divided-difference selection (ADVECTION_METHOD_2D.h:2054-2111).
-__device__ __forceinline__ void eno3_pair(const double q[7], double o, double o2, double o3, double h, double& dm, double& dp) {
-  double d1n3 = o * (q[1] - q[0]), d1n2 = o * (q[2] - q[1]), d1n1 = o * (q[3] - q[2]);
-  double d10 = o * (q[4] - q[3]), d1p1 = o * (q[5] - q[4]), d1p2 = o * (q[6] - q[5]);
-  double d2n2 = o2 * (d1n2 - d1n3), d2n1 = o2 * (d1n1 - d1n2), d20 = o2 * (d10 - d1n1);
-  double d2p1 = o2 * (d1p1 - d10), d2p2 = o2 * (d1p2 - d1p1);
-  double d3n2 = o3 * (d2n1 - d2n2), d3n1 = o3 * (d20 - d2n1), d30 = o3 * (d2p1 - d20), d3p1 = o3 * (d2p2 - d2p1);
-  if (abs_le(d2n1, d20)) {
-    if (abs_le(d3n2, d3n1))
-      dm = d1n1 + d2n1 * h + 2 * d3n2 * h * h;
+// ENO3 one-sided derivatives by divided-difference selection (ADVECTION_METHOD_2D.h:2054-2111),
+// from the six first divided differences d[0..5] (offsets -3..+2).
+__device__ __forceinline__ bool mag_le(double a, double b) { return abs_le(a, b); }
+__device__ __forceinline__ bool mag_le(float a, float b) { return fabsf(a) <= fabsf(b); }
+template <typename R>
+__device__ __forceinline__ void eno3_select(const R d[6], R o2, R o3, R h, R& dm, R& dp) {
+  const R d1n1 = d[2], d10 = d[3];
+  R d2n2 = o2 * (d[1] - d[0]), d2n1 = o2 * (d[2] - d[1]), d20 = o2 * (d[3] - d[2]);
+  R d2p1 = o2 * (d[4] - d[3]), d2p2 = o2 * (d[5] - d[4]);
+  R d3n2 = o3 * (d2n1 - d2n2), d3n1 = o3 * (d20 - d2n1), d30 = o3 * (d2p1 - d20), d3p1 = o3 * (d2p2 - d2p1);
+  if (mag_le(d2n1, d20)) {
+    if (mag_le(d3n2, d3n1))
+      dm = d1n1 + d2n1 * h + R(2) * d3n2 * h * h;
     else
-      dm = d1n1 + d2n1 * h + 2 * d3n1 * h * h;
+      dm = d1n1 + d2n1 * h + R(2) * d3n1 * h * h;
   } else {
-    if (abs_le(d3n1, d30))
+    if (mag_le(d3n1, d30))
       dm = d1n1 + d20 * h - d3n1 * h * h;
     else
       dm = d1n1 + d20 * h - d30 * h * h;
   }
-  if (abs_le(d20, d2p1)) {
-    if (abs_le(d3n1, d30))
+  if (mag_le(d20, d2p1)) {
+    if (mag_le(d3n1, d30))
       dp = d10 - d20 * h - d3n1 * h * h;
     else
       dp = d10 - d20 * h - d30 * h * h;
   } else {
-    if (abs_le(d30, d3p1))
-      dp = d10 - d2p1 * h + 2 * d30 * h * h;
+    if (mag_le(d30, d3p1))
+      dp = d10 - d2p1 * h + R(2) * d30 * h * h;
     else
-      dp = d10 - d2p1 * h + 2 * d3p1 * h * h;
+      dp = d10 - d2p1 * h + R(2) * d3p1 * h * h;
   }
+}
+
+// Exact FP64 pair: q[0..6] are values at offsets -3..+3.
+__device__ __forceinline__ void eno3_pair(const double q[7], double o, double o2, double o3, double h, double& dm, double& dp) {
+  double d[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d[k] = o * (q[k + 1] - q[k]);
+  eno3_select<double>(d, o2, o3, h, dm, dp);
+}
+
+// Mixed pair: differences of the FP64 state formed in FP64, the divided
+// differences and the selection in FP32.
+__device__ __forceinline__ void eno3_pair_f32(const double q[7], float o, float o2, float o3, float h, float& dm, float& dp) {
+  float d[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d[k] = narrow(q[k + 1] - q[k]) * o;
+  eno3_select<float>(d, o2, o3, h, dm, dp);
 }
 
 }  // namespace gb2d

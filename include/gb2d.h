@@ -74,7 +74,10 @@ typedef struct {
   double weno_epsilon;     /* WENO weight epsilon (1e-6) */
   int reinit_iterations;   /* iteration_number_for_reinitialization */
   int reinit_scaling;      /* scaling_number_for_reinitialization: dtau = dx/scaling */
-  int advection_precision; /* GB2D_PRECISION_FP64: exact FP64 WENO; MIXED: FP32 flux evaluation, FP64 state */
+  int advection_precision; /* explicit stencils (WENO5 advection, reinitialisation, ENO3 velocity advection,
+                              viscosity): GB2D_PRECISION_FP64 reproduces the reference's FP64 results;
+                              MIXED evaluates their fluxes in FP32 from FP64 differences, state and
+                              updates FP64 */
 } gb2d_params;
 
 /* Constants of the stages SolveForRK runs around the projection (gravity, viscosity;

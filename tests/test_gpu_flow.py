@@ -159,3 +159,27 @@ def test_advance_frame_matches_oracle(gb, oracle, name):
     for f, want in ((gb.FIELD_P, p), (gb.FIELD_U, u), (gb.FIELD_V, v)):
         assert rel_l2(c.get(f), want) <= STEP_TOL
     c.close()
+
+
+@pytest.mark.parametrize("name", FLOW_NAMES)
+def test_mixed_velocity_advection_and_viscosity_close_to_fp64(gb, name):
+    """The FP32 ENO3 and viscous fluxes of the mixed path against the reference's FP64 results."""
+    g = load_golden(name)
+    dt = float(g["dt"])
+    c = make_ctx(gb, g, 1, advection_precision=gb.PRECISION_MIXED)
+    c.velocity_advection(dt)
+    for f, k in ((gb.FIELD_U, "va_u"), (gb.FIELD_V, "va_v")):
+        d = c.get(f) - g[k]
+        assert np.abs(d).max() <= 1e-6 * np.abs(g[k]).max(), k
+    c.close()
+    c = make_ctx(gb, g, 1, advection_precision=gb.PRECISION_MIXED)
+    c.apply_gravity(dt)
+    c.sourcing(dt)
+    for f, k, k0 in ((gb.FIELD_U, "src1_u", "grav_u"), (gb.FIELD_V, "src1_v", "grav_v")):
+        # Error relative to the size of the viscous update itself.  Inside the smearing
+        # band an FP32 phi (relative error 2^-23) moves H by up to ~1e-7, the face density
+        # rho_a + (rho_w - rho_a) H by ~1e-4 for a density ratio of 1000, which is a 1e-4
+        # relative change of dt / rho where rho is near rho_a.
+        d = c.get(f) - g[k]
+        assert np.abs(d).max() <= 1e-4 * np.abs(g[k] - g[k0]).max() + 1e-15 * np.abs(g[k]).max(), k
+    c.close()
