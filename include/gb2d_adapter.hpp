@@ -63,24 +63,52 @@ class GB2D_FLUID_STEP {
   }
   // EULERIAN_FLUID_SOLVER_2D::Projection(dt, thread_id) (:2359-2363)
   void Projection(const double& dt, const int& thread_id) {
-    if (thread_id == 0) {
-      int rc = gb2d_projection(ctx_, dt, &solve_, &stats_);
-      // Like PCG_METHOD::PCGMethod (PCG_METHOD.cpp:253), hitting the iteration cap is not fatal.
-      if (rc != GB2D_ERR_MAX_ITERS) Check(rc, "Projection");
-      max_velocity_x = stats_.max_velocity_x;
-      max_velocity_y = stats_.max_velocity_y;
-    }
+    if (thread_id == 0) Solved(gb2d_projection(ctx_, dt, &solve_, &stats_), "Projection");
     Sync(thread_id);
   }
+
+  // Constants of gravity, viscosity and the CFL time step (gb2d_flow_params).
+  void SetFlowParams(const gb2d_flow_params& flow) { Check(gb2d_set_flow_params(ctx_, &flow), "gb2d_set_flow_params"); }
+  // EULERIAN_FLUID_SOLVER_2D::SolveForRK(dt, thread_id) (:1857-1879)
+  void SolveForRK(const double& dt, const int& thread_id) {
+    if (thread_id == 0) Solved(gb2d_solve_for_rk(ctx_, dt, &solve_, &stats_), "SolveForRK");
+    Sync(thread_id);
+  }
+  // EULERIAN_FLUID_SOLVER_2D::AdvanceOneTimeStepThread(dt, thread_id), order 3 (:1140, 1694-1794)
+  void AdvanceOneTimeStepThread(const double& dt, const int& thread_id) {
+    if (thread_id == 0) Solved(gb2d_advance_time_step(ctx_, dt, &solve_, &stats_), "AdvanceOneTimeStepThread");
+    Sync(thread_id);
+  }
+  // EULERIAN_FLUID_SOLVER_2D::CFLOneTimeStep() (:3517-3637), with the curvature as it stands;
+  // head thread only, like SIMULATION_WORLD::DetermineTimeStep.
+  double CFLOneTimeStep() {
+    double dt = 0, rates[4];
+    Check(gb2d_cfl_time_step(ctx_, &dt, rates), "CFLOneTimeStep");
+    c_f = rates[0];
+    g_f = rates[1];
+    v_f = rates[2];
+    s_f = rates[3];
+    return dt;
+  }
+  // SIMULATION_WORLD::AdvanceOneFrame (SIMULATION_WORLD.h:1094-1146): curvature, dt = CFL step * cfl,
+  // one time step.  dt: the previous step in, the step taken out.
+  void AdvanceOneFrame(const double& cfl, double& dt) { Solved(gb2d_advance_frame(ctx_, cfl, &dt, &solve_, &stats_), "AdvanceOneFrame"); }
 
   const gb2d_solve_stats& LastSolveStats() const { return stats_; }
   gb2d_ctx* Context() const { return ctx_; }
 
   double max_velocity_x = 0, max_velocity_y = 0;  // PROJECTION_2D::max_velocity_x/_y
+  double c_f = 0, g_f = 0, v_f = 0, s_f = 0;       // rates of the last CFLOneTimeStep
 
  private:
   void Sync(int thread_id) {
     if (sync_) sync_(thread_id);
+  }
+  // A solve stopped at its iteration cap is not fatal (PCG_METHOD.cpp:253).
+  void Solved(int rc, const char* what) {
+    if (rc != GB2D_ERR_MAX_ITERS) Check(rc, what);
+    max_velocity_x = stats_.max_velocity_x;
+    max_velocity_y = stats_.max_velocity_y;
   }
   void Check(int rc, const char* what) {
     if (rc != GB2D_OK) {

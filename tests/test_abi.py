@@ -51,3 +51,31 @@ def test_create_rejects_bad_arguments(gb):
     assert lib.gb2d_create(ctypes.byref(gb.GridT(10, 10, 1, 0, 1, 1)), ctypes.byref(p), ctypes.byref(h)) == -1
     bad = gb.ParamsT(1000.0, 1.0, 0.07, 1e-6, 25, 0, 0)
     assert lib.gb2d_create(ctypes.byref(gb.GridT(10, 10, 0, 0, 1, 1)), ctypes.byref(bad), ctypes.byref(h)) == -1
+
+
+def test_cpp_adapter_compiles(tmp_path):
+    """include/gb2d_adapter.hpp (the C++ mirror a reference maintainer includes) compiles
+    against the header with the reference's C++ dialect."""
+    import shutil
+    import subprocess
+    import pytest
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "use_adapter.cpp"
+    src.write_text('#include "gb2d_adapter.hpp"\n'
+                   'void step(GB2D_FLUID_STEP& s, double dt) {\n'
+                   '  s.Levelset_RK3(dt, 0); s.SolveForRK(dt, 0); s.AdvanceOneTimeStepThread(dt, 0);\n'
+                   '  double d = s.CFLOneTimeStep(); s.AdvanceOneFrame(1.0, d); s.Projection(dt, 0);\n'
+                   '  gb2d_flow_params f = {1.0, 0.01, 0.0, -9.8, 0.5, 0}; s.SetFlowParams(f);\n'
+                   '}\n')
+    r = subprocess.run([cxx, "-std=c++14", "-fsyntax-only", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_field_density_extent(gb):
+    g = gb.GridT(33, 17, 0.0, 0.0, 1.0, 1.0)
+    a, b = ctypes.c_int(), ctypes.c_int()
+    assert gb.library().gb2d_field_extent(ctypes.byref(g), gb.FIELD_DENSITY, ctypes.byref(a), ctypes.byref(b)) == 0
+    assert (a.value, b.value) == (37, 21)
