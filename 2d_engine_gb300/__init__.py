@@ -95,6 +95,8 @@ def library():
         "gb2d_advance_time_step": [vp, d, O, S],
         "gb2d_cfl_time_step": [vp, ctypes.POINTER(d), vp],
         "gb2d_advance_frame": [vp, d, ctypes.POINTER(d), O, S],
+        "gb2d_weno5_adjoint": [vp, d, vp, vp, vp, vp],
+        "gb2d_projection_adjoint": [vp, d, vp, vp, vp, vp, vp, O, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
         "gb2d_poisson_solve": [vp, vp, vp, O, S],
@@ -299,6 +301,31 @@ class Context:
         if rc != 0 and not (allow_max_iters and rc == -4):
             self._check(rc)
         return st
+
+    # Adjoints (vector-Jacobian products)
+    def weno5_adjoint(self, dt, lam_phi, velocity=True):
+        """VJP of one levelset_advection at the current PHI, UA, VA: (mu_phi, mu_ua, mu_va)."""
+        lam = np.ascontiguousarray(lam_phi, dtype=np.float64)
+        mu = np.empty(self.shape(FIELD_PHI))
+        mua = np.empty(self.shape(FIELD_UA)) if velocity else None
+        mva = np.empty(self.shape(FIELD_VA)) if velocity else None
+        self._check(self.L.gb2d_weno5_adjoint(self.h, dt, _ptr(lam), _ptr(mu), _ptr(mua) if velocity else None,
+                                              _ptr(mva) if velocity else None))
+        return mu, mua, mva
+
+    def projection_adjoint(self, dt, lam_u, lam_v, lam_p=None, opts=None, allow_max_iters=False):
+        """VJP of the last projection with respect to its intermediate velocity: (mu_u, mu_v, stats)."""
+        lu = np.ascontiguousarray(lam_u, dtype=np.float64)
+        lv = np.ascontiguousarray(lam_v, dtype=np.float64)
+        lp = None if lam_p is None else np.ascontiguousarray(lam_p, dtype=np.float64)
+        mu, mv = np.empty(self.shape(FIELD_U)), np.empty(self.shape(FIELD_V))
+        opts = opts or solve_opts(tolerance=1e-12)
+        st = SolveStatsT()
+        rc = self.L.gb2d_projection_adjoint(self.h, dt, _ptr(lu), _ptr(lv), None if lp is None else _ptr(lp), _ptr(mu), _ptr(mv),
+                                            ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return mu, mv, st
 
     # Pressure system (a10/a15)
     def poisson_assemble(self, dt):

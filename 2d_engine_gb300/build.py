@@ -24,6 +24,7 @@ UNITS = {
     "gb2d_solver.cu": [],
     "gb2d_api.cu": [],
     "gb2d_noalloc.cu": [],
+    "gb2d_adjoint.cu": [],
 }
 
 

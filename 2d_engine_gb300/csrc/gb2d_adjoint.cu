@@ -1,0 +1,338 @@
+// Adjoints (vector-Jacobian products) of the level-set WENO5 advection sweep and of
+// the projection's velocity map, for gradients of a scalar loss through the step.
+// The reference has no derivative code; these differentiate the reference's own
+// forward maps as the FP64 kernels compute them:
+//   * Levelset_Advection (ADVECTION_METHOD_2D.h:508-663 with the ghost copy of
+//     FIELD_STRUCTURE_2D.h:374-449 and the extrapolation of :641-716): WENO5 weights
+//     included; the upwind switch on the sign of the face-averaged velocity is held.
+//   * PROJECTION_2D::Solve (PROJECTION_2D.h:244-257): u' = u* - dt M p, A p = b(u*),
+//     so dL/du* = lam + D^T z with A z = M^T-applied cotangent (A symmetric): the
+//     transposed gradient, the same solve, the transposed divergence.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "gb2d_internal.cuh"
+#include "gb2d_schemes.cuh"
+
+namespace gb2d {
+
+namespace {
+
+// d f / d a_m of one WENO5 side f(a1..a5) = sum_k w_k P_k (ADVECTION_METHOD_2D.h:545-619):
+//   df/da = sum_k w_k dP_k/da + sum_k (P_k - f) / S * dalpha_k/da,
+//   alpha_k = c_k / (eps + beta_k)^2, S = sum alpha_k, w_k = alpha_k / S.
+__device__ void weno5_side_grad(const double a[5], double eps, double& f, double g[5]) {
+  const double A[3] = {a[0] - 2 * a[1] + a[2], a[1] - 2 * a[2] + a[3], a[2] - 2 * a[3] + a[4]};
+  const double B[3] = {a[0] - 4 * a[1] + 3 * a[2], a[1] - a[3], 3 * a[2] - 4 * a[3] + a[4]};
+  const double dA[3][5] = {{1, -2, 1, 0, 0}, {0, 1, -2, 1, 0}, {0, 0, 1, -2, 1}};
+  const double dB[3][5] = {{1, -4, 3, 0, 0}, {0, 1, 0, -1, 0}, {0, 0, 3, -4, 1}};
+  const double dP[3][5] = {{1.0 / 3, -7.0 / 6, 11.0 / 6, 0, 0}, {0, -1.0 / 6, 5.0 / 6, 1.0 / 3, 0}, {0, 0, 1.0 / 3, 5.0 / 6, -1.0 / 6}};
+  const double c[3] = {0.1, 0.6, 0.3};
+  double beta[3], al[3], P[3], S = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    beta[k] = 13.0 / 12.0 * A[k] * A[k] + 0.25 * B[k] * B[k];
+    al[k] = c[k] / ((eps + beta[k]) * (eps + beta[k]));
+    S += al[k];
+    P[k] = 0;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) P[k] += dP[k][m] * a[m];
+  }
+  f = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) f += al[k] / S * P[k];
+#pragma unroll
+  for (int m = 0; m < 5; ++m) g[m] = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double w = al[k] / S, r = (P[k] - f) / S * (-2 * al[k] / (eps + beta[k]));
+#pragma unroll
+    for (int m = 0; m < 5; ++m) g[m] += w * dP[k][m] + r * (13.0 / 6.0 * A[k] * dA[k][m] + 0.5 * B[k] * dB[k][m]);
+  }
+}
+
+// Derivative of the upwind WENO5 derivative along one line with respect to its seven
+// stencil values q[0..6] (offsets -3..+3): minus side (d0..d4) when up, else plus side
+// (d5..d1); d_k = o (q[k+1] - q[k]).  f receives the derivative itself.
+__device__ void weno5_line_grad(const double q[7], double o, double eps, bool up, double& f, double J[7]) {
+  double d[6], gd[6] = {0, 0, 0, 0, 0, 0}, a[5], g[5];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d[k] = o * (q[k + 1] - q[k]);
+  if (up) {
+#pragma unroll
+    for (int t = 0; t < 5; ++t) a[t] = d[t];
+    weno5_side_grad(a, eps, f, g);
+#pragma unroll
+    for (int t = 0; t < 5; ++t) gd[t] = g[t];
+  } else {
+#pragma unroll
+    for (int t = 0; t < 5; ++t) a[t] = d[5 - t];
+    weno5_side_grad(a, eps, f, g);
+#pragma unroll
+    for (int t = 0; t < 5; ++t) gd[5 - t] = g[t];
+  }
+#pragma unroll
+  for (int m = 0; m < 7; ++m) J[m] = o * ((m > 0 ? gd[m - 1] : 0.0) - (m < 6 ? gd[m] : 0.0));
+}
+
+// The seven stencil positions of the ghost-filled copy read clamped positions of the
+// interior (FillGhostCellsFrom copies the second interior line into every ghost layer).
+__device__ __forceinline__ int clamp_line(int k, int n) { return k < 0 ? 1 : (k >= n ? n - 2 : k); }
+
+struct AdjArgs {
+  int ni, nj;
+  double odx, ody, eps, dt;
+};
+
+// Per interior node n: C[m] = -dt u_n lam_n dfx/dq_m (m = 0..6) and the same for y
+// (m = 7..13); gv = -dt lam f / 2 per direction (the face-averaged velocity's share).
+__global__ void k_weno5_adj_coef(const double* __restrict__ phi_a, const double* __restrict__ ua_a, const double* __restrict__ va_a,
+                                 const double* __restrict__ lam_a, double* __restrict__ coef, double* __restrict__ gvel, AdjArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const DField phi = dfield((double*)phi_a, 2, ni, nj), lam = dfield((double*)lam_a, 2, ni, nj);
+  const DField ua = dfield((double*)ua_a, 3, ni + 1, nj), va = dfield((double*)va_a, 3, ni, nj + 1);
+  const size_t n = (size_t)ni * nj;
+  GB_FOR_IJ(i, j, ni, nj) {
+    const size_t t = (size_t)j * ni + i;
+    const double u = (GB_AT(ua, i + 1, j) + GB_AT(ua, i, j)) * 0.5;
+    const double v = (GB_AT(va, i, j + 1) + GB_AT(va, i, j)) * 0.5;
+    const double l = GB_AT(lam, i, j);
+    double q[7], J[7], fx, fy;
+#pragma unroll
+    for (int m = 0; m < 7; ++m) q[m] = GB_AT(phi, clamp_line(i - 3 + m, ni), j);
+    weno5_line_grad(q, a.odx, a.eps, gtz(u), fx, J);
+#pragma unroll
+    for (int m = 0; m < 7; ++m) coef[m * n + t] = -a.dt * u * l * J[m];
+#pragma unroll
+    for (int m = 0; m < 7; ++m) q[m] = GB_AT(phi, i, clamp_line(j - 3 + m, nj));
+    weno5_line_grad(q, a.ody, a.eps, gtz(v), fy, J);
+#pragma unroll
+    for (int m = 0; m < 7; ++m) coef[(7 + m) * n + t] = -a.dt * v * l * J[m];
+    gvel[t] = -a.dt * l * fx * 0.5;
+    gvel[n + t] = -a.dt * l * fy * 0.5;
+  }
+}
+
+// Sum of the stencil coefficients that land on interior position k of one line:
+// position p of the ghost-filled copy feeds nodes within 3 of it; k = 1 also owns the
+// low ghost positions -1..-3, k = n-2 the high ones n..n+2.
+__device__ __forceinline__ double line_gather(const double* __restrict__ coef, size_t n, size_t stride, size_t base, int k, int nk,
+                                              int mbase) {
+  double acc = 0;
+  int ps[4] = {k, 0, 0, 0}, np = 1;
+  if (k == 1) {
+    ps[1] = -1;
+    ps[2] = -2;
+    ps[3] = -3;
+    np = 4;
+  } else if (k == nk - 2) {
+    ps[1] = nk;
+    ps[2] = nk + 1;
+    ps[3] = nk + 2;
+    np = 4;
+  }
+  for (int s = 0; s < np; ++s) {
+    const int p = ps[s];
+    const int lo = p - 3 < 0 ? 0 : p - 3, hi = p + 3 > nk - 1 ? nk - 1 : p + 3;
+    for (int c = lo; c <= hi; ++c) acc += coef[(size_t)(mbase + p - c + 3) * n + base + (size_t)c * stride];
+  }
+  return acc;
+}
+
+// mu = lam (identity part) + the stencil coefficients gathered onto each interior
+// node; ghost positions pass lam through (the sweep copies the input's ghost ring).
+__global__ void k_weno5_adj_gather(const double* __restrict__ lam_a, const double* __restrict__ coef, double* __restrict__ mu_a, AdjArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const DField lam = dfield((double*)lam_a, 2, ni, nj), mu = dfield(mu_a, 2, ni, nj);
+  const size_t n = (size_t)ni * nj;
+  GB_FOR_IJ(ii, jj, ni + 4, nj + 4) {
+    const int i = ii - 2, j = jj - 2;
+    double v = GB_AT(lam, i, j);
+    if (i >= 0 && i < ni && j >= 0 && j < nj) {
+      v += line_gather(coef, n, 1, (size_t)j * ni, i, ni, 0);
+      v += line_gather(coef, n, (size_t)ni, (size_t)i, j, nj, 7);
+    }
+    GB_AT(mu, i, j) = v;
+  }
+}
+
+// dL/dUA, dL/dVA: each node's velocity share goes to the two faces it averages.
+__global__ void k_weno5_adj_vel(const double* __restrict__ gvel, double* __restrict__ mu_ua_a, double* __restrict__ mu_va_a, int ni, int nj) {
+  const DField mu_ua = dfield(mu_ua_a, 3, ni + 1, nj), mu_va = dfield(mu_va_a, 3, ni, nj + 1);
+  const size_t n = (size_t)ni * nj;
+  GB_FOR_IJ(i, j, ni + 1, nj + 1) {
+    if (mu_ua_a && j < nj) GB_AT(mu_ua, i, j) = (i > 0 ? gvel[(size_t)j * ni + i - 1] : 0.0) + (i < ni ? gvel[(size_t)j * ni + i] : 0.0);
+    if (mu_va_a && i < ni) GB_AT(mu_va, i, j) = (j > 0 ? gvel[n + (size_t)(j - 1) * ni + i] : 0.0) + (j < nj ? gvel[n + (size_t)j * ni + i] : 0.0);
+  }
+}
+
+// Reverse of the ghost extrapolation (FillGhostCellsContinuousDerivativesFrom, ghost 2):
+// each overwrite t <- 2 a - b becomes lam_a += 2 lam_t, lam_b -= lam_t, lam_t = 0, in
+// the reverse order of the forward assignments.  What remains on a ghost cell is the
+// cotangent of the value it held before the extrapolation.  Rows: left and right sides.
+__global__ void k_extrap_adj_rows(double* lam_a, int ni, int nj) {
+  const DField L = dfield(lam_a, 2, ni, nj);
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nj; j += gridDim.x * blockDim.x) {
+    // right: forward i = ni then ni+1
+    double t = GB_AT(L, ni + 1, j);
+    GB_AT(L, ni, j) += 2 * t, GB_AT(L, ni - 1, j) -= t, GB_AT(L, ni + 1, j) = 0;
+    t = GB_AT(L, ni, j);
+    GB_AT(L, ni - 1, j) += 2 * t, GB_AT(L, ni - 2, j) -= t, GB_AT(L, ni, j) = 0;
+    // left: forward i = -2 (reading the old -1) then i = -1
+    t = GB_AT(L, -1, j);
+    GB_AT(L, 0, j) += 2 * t, GB_AT(L, 1, j) -= t, GB_AT(L, -1, j) = 0;
+    t = GB_AT(L, -2, j);
+    GB_AT(L, -1, j) += 2 * t, GB_AT(L, 0, j) -= t, GB_AT(L, -2, j) = 0;
+  }
+}
+// Columns: top and bottom sides.
+__global__ void k_extrap_adj_cols(double* lam_a, int ni, int nj) {
+  const DField L = dfield(lam_a, 2, ni, nj);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
+    double t = GB_AT(L, i, -1);  // bottom: forward j = -2 then j = -1
+    GB_AT(L, i, 0) += 2 * t, GB_AT(L, i, 1) -= t, GB_AT(L, i, -1) = 0;
+    t = GB_AT(L, i, -2);
+    GB_AT(L, i, -1) += 2 * t, GB_AT(L, i, 0) -= t, GB_AT(L, i, -2) = 0;
+    t = GB_AT(L, i, nj + 1);  // top: forward j = nj then nj+1
+    GB_AT(L, i, nj) += 2 * t, GB_AT(L, i, nj - 1) -= t, GB_AT(L, i, nj + 1) = 0;
+    t = GB_AT(L, i, nj);
+    GB_AT(L, i, nj - 1) += 2 * t, GB_AT(L, i, nj - 2) -= t, GB_AT(L, i, nj) = 0;
+  }
+}
+
+struct ProjAdjArgs {
+  int ni, nj;
+  double dt, odx, ody, odt;
+  double inv_water, inv_air, water, air, eps_h, eps_v, oeh, oev;
+};
+
+// 1/rho of a velocity-update face (UpdateVelocityByPressureGradientVariableDensity,
+// PROJECTION_2D.h:1297-1416): the + side's node density on same-sign faces, the
+// smeared density of the face-averaged phi on interface faces, 0 where the forward
+// leaves the face alone (NaN).
+__device__ __forceinline__ double face_inv_rho(double l0, double ln, bool xc, const ProjAdjArgs& a) {
+  if (l0 * ln >= 0) return lez(l0) ? a.inv_air : a.inv_water;
+  if (!(ltz(l0) || gtz(l0))) return 0;
+  const double dh = a.air + (a.water - a.air) * heaviside(0.5 * (l0 + ln), xc ? a.eps_h : a.eps_v, xc ? a.oeh : a.oev);
+  return 1 / dh;
+}
+
+// r = dL/dp = (d u'/d p)^T lam + lam_p for u'_f = u*_f - dt c_f od (p_+ - p_-), on the
+// faces the forward updates (x-faces i < ni, y-faces j < nj; the pressure ghost is 0).
+__global__ void k_proj_adj_rhs(const double* __restrict__ phi_a, const double* __restrict__ lu_a, const double* __restrict__ lv_a,
+                               const double* __restrict__ lp_a, double* __restrict__ r, ProjAdjArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const DField phi = dfield((double*)phi_a, 2, ni, nj);
+  const DField lu = dfield((double*)lu_a, 2, ni + 1, nj), lv = dfield((double*)lv_a, 2, ni, nj + 1);
+  const DField lp = dfield((double*)lp_a, 1, ni, nj);
+  GB_FOR_IJ(i, j, ni, nj) {
+    const double pc = GB_AT(phi, i, j);
+    double acc = lp_a ? GB_AT(lp, i, j) : 0.0;
+    acc -= a.dt * face_inv_rho(pc, GB_AT(phi, i - 1, j), true, a) * a.odx * GB_AT(lu, i, j);
+    acc -= a.dt * face_inv_rho(pc, GB_AT(phi, i, j - 1), false, a) * a.ody * GB_AT(lv, i, j);
+    if (i + 1 < ni) acc += a.dt * face_inv_rho(GB_AT(phi, i + 1, j), pc, true, a) * a.odx * GB_AT(lu, i + 1, j);
+    if (j + 1 < nj) acc += a.dt * face_inv_rho(GB_AT(phi, i, j + 1), pc, false, a) * a.ody * GB_AT(lv, i, j + 1);
+    r[(size_t)j * ni + i] = acc;
+  }
+}
+
+// mu = lam + (db/du*)^T z with b = -(odx dU + ody dV) / dt - F: z is the padded adjoint
+// pressure (zero ghost ring), so wall faces see only their one interior node.
+__global__ void k_proj_adj_vel(const double* __restrict__ lu_a, const double* __restrict__ lv_a, const double* __restrict__ z_a,
+                               double* __restrict__ mu_u_a, double* __restrict__ mu_v_a, ProjAdjArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const DField lu = dfield((double*)lu_a, 2, ni + 1, nj), lv = dfield((double*)lv_a, 2, ni, nj + 1);
+  const DField mu = dfield(mu_u_a, 2, ni + 1, nj), mv = dfield(mu_v_a, 2, ni, nj + 1);
+  const DField z = dfield((double*)z_a, 1, ni, nj);
+  GB_FOR_IJ(ii, jj, ni + 5, nj + 5) {
+    const int i = ii - 2, j = jj - 2;
+    if (i <= ni + 2 && j <= nj + 1) {
+      double w = GB_AT(lu, i, j);
+      if (i >= 0 && i <= ni && j >= 0 && j < nj) w += a.odx * a.odt * (GB_AT(z, i, j) - GB_AT(z, i - 1, j));
+      GB_AT(mu, i, j) = w;
+    }
+    if (i <= ni + 1 && j <= nj + 2) {
+      double w = GB_AT(lv, i, j);
+      if (i >= 0 && i < ni && j >= 0 && j <= nj) w += a.ody * a.odt * (GB_AT(z, i, j) - GB_AT(z, i, j - 1));
+      GB_AT(mv, i, j) = w;
+    }
+  }
+}
+
+}  // namespace
+
+int adjoint_buffers(gb2d_ctx* c) {
+  if (c->adj_coef) return GB2D_OK;
+  const size_t ni = c->grid.ni, nj = c->grid.nj;
+  struct A {
+    double** p;
+    size_t n;
+  } allocs[] = {
+      {&c->adj_coef, 14 * ni * nj},           {&c->adj_gvel, 2 * ni * nj},
+      {&c->adj_lam_phi, (ni + 4) * (nj + 4)}, {&c->adj_mu_phi, (ni + 4) * (nj + 4)},
+      {&c->adj_lam_u, (ni + 5) * (nj + 4)},   {&c->adj_lam_v, (ni + 4) * (nj + 5)},
+      {&c->adj_mu_u, (ni + 7) * (nj + 6)},    {&c->adj_mu_v, (ni + 6) * (nj + 7)},
+      {&c->adj_lam_p, (ni + 2) * (nj + 2)},
+  };
+  for (auto& a : allocs) {
+    cudaError_t e = cudaMalloc(a.p, a.n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(*a.p, 0, a.n * sizeof(double));
+    if (e != cudaSuccess) {
+      snprintf(c->err, sizeof(c->err), "adjoint buffers: %s", cudaGetErrorString(e));
+      return GB2D_ERR_CUDA;
+    }
+  }
+  return GB2D_OK;
+}
+
+void launch_weno5_adjoint(cudaStream_t s, gb2d_ctx* c, double dt, double* mu_ua, double* mu_va) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  AdjArgs a{ni, nj, c->base.odx, c->base.ody, c->prm.weno_epsilon, dt};
+  k_extrap_adj_cols<<<(ni + 127) / 128, 128, 0, s>>>(c->adj_lam_phi, ni, nj);
+  k_extrap_adj_rows<<<(nj + 127) / 128, 128, 0, s>>>(c->adj_lam_phi, ni, nj);
+  k_weno5_adj_coef<<<grid_ij(ni, nj), kThreads, 0, s>>>(c->phi_buf[c->phi_cur], c->ua, c->va, c->adj_lam_phi, c->adj_coef, c->adj_gvel, a);
+  k_weno5_adj_gather<<<grid_ij(ni + 4, nj + 4), kThreads, 0, s>>>(c->adj_lam_phi, c->adj_coef, c->adj_mu_phi, a);
+  GB_LAUNCHED(4);
+  if (mu_ua || mu_va) {
+    k_weno5_adj_vel<<<grid_ij(ni + 1, nj + 1), kThreads, 0, s>>>(c->adj_gvel, mu_ua, mu_va, ni, nj);
+    GB_LAUNCHED(1);
+  }
+}
+
+void launch_projection_adjoint_rhs(cudaStream_t s, gb2d_ctx* c, double dt, int with_lam_p) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  ProjAdjArgs a;
+  a.ni = ni;
+  a.nj = nj;
+  a.dt = dt;
+  a.odx = c->base.odx;
+  a.ody = c->base.ody;
+  a.odt = 1.0 / dt;
+  a.water = c->prm.water_density;
+  a.air = c->prm.air_density;
+  a.inv_water = 1.0 / a.water;
+  a.inv_air = 1.0 / a.air;
+  a.eps_h = 1.5 * c->base.dx;
+  a.eps_v = 1.5 * c->base.dy;
+  a.oeh = 1.0 / a.eps_h;
+  a.oev = 1.0 / a.eps_v;
+  k_proj_adj_rhs<<<grid_ij(ni, nj), kThreads, 0, s>>>(c->phi_buf[c->phi_cur], c->adj_lam_u, c->adj_lam_v,
+                                                      with_lam_p ? c->adj_lam_p : nullptr, c->rhs, a);
+  GB_LAUNCHED(1);
+}
+
+void launch_projection_adjoint_vel(cudaStream_t s, gb2d_ctx* c, double dt, const double* z) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  ProjAdjArgs a;
+  memset(&a, 0, sizeof a);
+  a.ni = ni;
+  a.nj = nj;
+  a.odx = c->base.odx;
+  a.ody = c->base.ody;
+  a.odt = 1.0 / dt;
+  k_proj_adj_vel<<<grid_ij(ni + 5, nj + 5), kThreads, 0, s>>>(c->adj_lam_u, c->adj_lam_v, z, c->adj_mu_u, c->adj_mu_v, a);
+  GB_LAUNCHED(1);
+}
+
+}  // namespace gb2d

@@ -121,7 +121,8 @@ void free_ctx(gb2d_ctx* c) {
   if (c->solver) solver_destroy(c->solver);
   double* bufs[] = {c->phi_buf[0], c->phi_buf[1], c->phi_buf[2], c->phi_buf[3], c->u, c->v, c->ua, c->va, c->p,
                     c->kappa, c->sign, c->bx, c->by, c->diag, c->rhs, c->tmp_a, c->tmp_b, c->xw, c->u_alt, c->v_alt,
-                    c->u_keep, c->v_keep, c->density};
+                    c->u_keep, c->v_keep, c->density, c->adj_coef, c->adj_gvel, c->adj_lam_phi, c->adj_mu_phi,
+                    c->adj_lam_u, c->adj_lam_v, c->adj_mu_u, c->adj_mu_v, c->adj_lam_p};
   for (auto b : bufs)
     if (b) cudaFree(b);
   for (auto b : c->ckpt)
@@ -591,6 +592,48 @@ int gb2d_advance_frame(gb2d_ctx* c, double cfl, double* dt, const gb2d_solve_opt
   d = d * cfl;
   *dt = d;
   return gb2d_advance_time_step(c, d, o, st);
+}
+
+int gb2d_weno5_adjoint(gb2d_ctx* c, double dt, const double* lam_phi, double* mu_phi, double* mu_ua, double* mu_va) {
+  if (!c || !lam_phi || !mu_phi || !std::isfinite(dt)) return GB2D_ERR_ARG;
+  int rc = adjoint_buffers(c);
+  if (rc) return rc;
+  const size_t ni = c->grid.ni, nj = c->grid.nj;
+  const size_t nphi = (ni + 4) * (nj + 4), nua = (ni + 7) * (nj + 6), nva = (ni + 6) * (nj + 7);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_phi, lam_phi, nphi * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (mu_ua) GB2D_CUDA_TRY(c, cudaMemsetAsync(c->adj_mu_u, 0, nua * sizeof(double), c->stream));
+  if (mu_va) GB2D_CUDA_TRY(c, cudaMemsetAsync(c->adj_mu_v, 0, nva * sizeof(double), c->stream));
+  launch_weno5_adjoint(c->stream, c, dt, mu_ua ? c->adj_mu_u : nullptr, mu_va ? c->adj_mu_v : nullptr);
+  if ((rc = check_launch(c, "weno5_adjoint"))) return rc;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_phi, c->adj_mu_phi, nphi * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (mu_ua) GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_ua, c->adj_mu_u, nua * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (mu_va) GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_va, c->adj_mu_v, nva * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return sync_check(c, "weno5_adjoint");
+}
+
+int gb2d_projection_adjoint(gb2d_ctx* c, double dt, const double* lam_u, const double* lam_v, const double* lam_p, double* mu_u,
+                            double* mu_v, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
+  if (!c || !lam_u || !lam_v || !mu_u || !mu_v || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
+  int rc = adjoint_buffers(c);
+  if (rc) return rc;
+  const size_t ni = c->grid.ni, nj = c->grid.nj;
+  const size_t nu = (ni + 5) * (nj + 4), nv = (ni + 4) * (nj + 5), np = (ni + 2) * (nj + 2);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_u, lam_u, nu * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_v, lam_v, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (lam_p) GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_p, lam_p, np * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_projection_adjoint_rhs(c->stream, c, dt, lam_p != nullptr);
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(c->xw, 0, np * sizeof(double), c->stream));
+  gb2d_solve_stats local;
+  memset(&local, 0, sizeof local);
+  int src = solver_solve(c, c->rhs, c->xw, o, &local);
+  if (src != GB2D_OK && src != GB2D_ERR_MAX_ITERS) return src;
+  launch_projection_adjoint_vel(c->stream, c, dt, c->xw);
+  if ((rc = check_launch(c, "projection_adjoint"))) return rc;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_u, c->adj_mu_u, nu * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_v, c->adj_mu_v, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = sync_check(c, "projection_adjoint"))) return rc;
+  if (st) *st = local;
+  return src;
 }
 
 int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {

@@ -141,6 +141,12 @@ struct gb2d_ctx {
   double *u_alt, *v_alt;    // second face buffers: the viscosity pass writes them, then they swap with u, v
   double *u_keep, *v_keep;  // velocity TVD-RK3 stage-0 copies (water_velocity_field_*_rk_3rd)
   double* density;          // DetermineDensity's node density, ghost 2
+  // Adjoint work buffers (allocated by the first adjoint call)
+  double *adj_coef, *adj_gvel;        // WENO5 stencil coefficients (14 per node), velocity shares (2 per node)
+  double *adj_lam_phi, *adj_mu_phi;   // cotangents of phi (ghost 2)
+  double *adj_lam_u, *adj_lam_v;      // cotangents of U, V (ghost 2)
+  double *adj_mu_u, *adj_mu_v;        // results for U/V (ghost 2) or UA/VA (ghost 3)
+  double* adj_lam_p;                  // cotangent of p (ghost 1)
   double* sign;  // reinit S (interior)
   // Assembled pressure system (FP64): faces bx ((ni+1) x nj), by (ni x (nj+1)), diag/rhs (ni x nj).
   double *bx, *by, *diag, *rhs;
@@ -181,6 +187,16 @@ void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int
 void launch_face_blend(cudaStream_t s, gb2d_ctx* c, double c0, double c1);
 // CFLOneTimeStep into c->sc->cfl (dt, c_f, g_f, v_f, s_f).
 void launch_cfl(cudaStream_t s, gb2d_ctx* c);
+
+// ---- gb2d_adjoint.cu ----
+int adjoint_buffers(gb2d_ctx* c);
+// VJP of one level-set advection sweep at the current PHI, UA, VA: adj_lam_phi (consumed)
+// -> adj_mu_phi; velocity cotangents into mu_ua / mu_va (UA/VA layout) when non-null.
+void launch_weno5_adjoint(cudaStream_t s, gb2d_ctx* c, double dt, double* mu_ua, double* mu_va);
+// Projection adjoint: c->rhs = dL/dp from adj_lam_u/v (and adj_lam_p); then, after the
+// solve into the padded z, adj_mu_u/v = lam + D^T z.
+void launch_projection_adjoint_rhs(cudaStream_t s, gb2d_ctx* c, double dt, int with_lam_p);
+void launch_projection_adjoint_vel(cudaStream_t s, gb2d_ctx* c, double dt, const double* z);
 
 // ---- gb2d_solver.cu ----
 Solver* solver_create(int ni, int nj, char* err, size_t errlen);

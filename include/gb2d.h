@@ -213,6 +213,25 @@ int gb2d_cfl_time_step(gb2d_ctx* ctx, double* dt, double* rates);
  * in, the step taken out. */
 int gb2d_advance_frame(gb2d_ctx* ctx, double cfl, double* dt, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
 
+/* Adjoints (vector-Jacobian products) for gradients of a scalar loss L; no counterpart in
+ * the reference, which has no derivative code.  Host arrays in the field layouts; FP64.
+ *
+ * gb2d_weno5_adjoint: one gb2d_levelset_advection (WENO5 sweep, its ghost copy and the
+ * ghost extrapolation) linearised at the current PHI, UA, VA, i.e. at the step's input.
+ * lam_phi = dL/dphi' of the step's output (PHI layout); writes mu_phi = dL/dphi (PHI
+ * layout) and, if non-NULL, mu_ua / mu_va = dL/dUA, dL/dVA (UA / VA layouts).  The WENO5
+ * weights are differentiated; the upwind switch on the sign of the face-averaged
+ * velocity is held at its current side.  Allocates about 16 doubles per node on the
+ * first call. */
+int gb2d_weno5_adjoint(gb2d_ctx* ctx, double dt, const double* lam_phi, double* mu_phi, double* mu_ua, double* mu_va);
+/* gb2d_projection_adjoint: the last gb2d_projection, linearised at its level set and
+ * assembled system (PHI unchanged since), with respect to its intermediate velocity.
+ * lam_u, lam_v = dL/dU', dL/dV' of the projected velocity, lam_p = dL/dp (P layout, may be
+ * NULL); writes mu_u, mu_v = dL/dU*, dL/dV*.  Applies the transposed pressure gradient,
+ * solves the same symmetric system with opts, applies the transposed divergence. */
+int gb2d_projection_adjoint(gb2d_ctx* ctx, double dt, const double* lam_u, const double* lam_v, const double* lam_p, double* mu_u,
+                            double* mu_v, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+
 /* Standalone pieces of the pressure system for parity checks and for
  * POISSON_SOLVER_2D-style use (a10, a15).  gb2d_poisson_assemble runs the
  * curvature step (which extrapolates phi's ghosts) and builds the system of the

@@ -1,0 +1,187 @@
+"""Adjoints through the C ABI: the WENO5 advection adjoint and the projection
+adjoint against central finite differences of the GPU forward maps, against an
+FP64 reference gradient (central differences of the CPU oracle, component by
+component), and a rising-bubble differentiation window (centroid height after K
+level-set RK3 steps, reinitialisation off) through the torch.autograd wrappers
+with checkpointed segments."""
+import importlib
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from tests.golden.cases import rising_bubble_case
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+EPS_FD = 1e-6
+GRAD_TOL = 1e-5  # spec bound: adjoint gradients against finite differences
+
+
+def central(f, x, d, eps=EPS_FD):
+    """Central difference of f at x along d, with step eps and one Richardson step at
+    eps/2.  Where the level set is locally linear the WENO5 smoothness indicators are
+    near their 1e-6 floor and the weights vary on that scale, so the plain quotient at
+    eps = 1e-6 carries O(eps^2) errors near 1e-5 relative; the extrapolation removes most
+    of them.  The single-sweep checks below, whose difference quotients sum over every
+    component of a random direction, step at 1e-7."""
+    q = lambda h: (f(x + h * d) - f(x - h * d)) / (2 * h)
+    return (4 * q(eps / 2) - q(eps)) / 3
+
+
+def make_ctx(gb, g):
+    return gb.Context(int(g["ni"]), int(g["nj"]), 0.0, 0.0, float(g["x_max"]), float(g["y_max"]))
+
+
+def advect(gb, c, phi, ua, va, dt):
+    c.set(gb.FIELD_PHI, phi)
+    c.set(gb.FIELD_UA, ua)
+    c.set(gb.FIELD_VA, va)
+    c.levelset_advection(dt)
+    return c.get(gb.FIELD_PHI)
+
+
+@pytest.mark.parametrize("name", ["bubbles_17", "bubbles_33", "rising_bubble_40x24"])
+def test_weno5_adjoint_matches_finite_differences(gb, name):
+    g = load_golden(name)
+    dt = float(g["dt"])
+    c = make_ctx(gb, g)
+    rng = np.random.default_rng(7)
+    lam = rng.standard_normal(g["phi"].shape)
+    phi, ua, va = g["phi"], g["ua"], g["va"]
+    advect(gb, c, phi, ua, va, dt)
+    c.set(gb.FIELD_PHI, phi)  # linearise at the input
+    mu, mua, mva = c.weno5_adjoint(dt, lam)
+    L = lambda p, a, b: float(np.sum(lam * advect(gb, c, p, a, b, dt)))
+    nu = ua.size
+    Lv = lambda w: L(phi, w[:nu].reshape(ua.shape), w[nu:].reshape(va.shape))
+    for k in range(4):
+        d = rng.standard_normal(phi.shape)
+        fd = central(lambda p: L(p, ua, va), phi, d, eps=1e-7)
+        ad = float(np.sum(mu * d))
+        assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-12), (k, ad, fd)
+        dw = rng.standard_normal(nu + va.size)
+        fd = central(Lv, np.concatenate([ua.ravel(), va.ravel()]), dw, eps=1e-7)
+        ad = float(np.sum(mua.ravel() * dw[:nu]) + np.sum(mva.ravel() * dw[nu:]))
+        assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-12), (k, ad, fd)
+    c.close()
+
+
+def test_weno5_adjoint_matches_oracle_reference_gradient(gb, oracle):
+    """Every component of d<lam, phi'>/dphi from central differences of the FP64 oracle."""
+    g = load_golden("bubbles_17")
+    ni, nj, dt = int(g["ni"]), int(g["nj"]), float(g["dt"])
+    gr = oracle.grid(ni, nj, 0.0, 0.0, float(g["x_max"]), float(g["y_max"]))
+    pr = oracle.params()
+    lam = np.random.default_rng(8).standard_normal(g["phi"].shape)
+
+    def L(p):
+        q = p.copy()
+        oracle.levelset_advection(gr, pr, q, g["ua"].copy(), g["va"].copy(), dt)
+        return float(np.sum(lam * q))
+
+    ref = np.zeros_like(lam)
+    base = g["phi"].copy()
+    for idx in np.ndindex(base.shape):
+        e = np.zeros_like(base)
+        e[idx] = 1.0
+        ref[idx] = central(L, base, e)
+    c = make_ctx(gb, g)
+    c.set(gb.FIELD_PHI, base); c.set(gb.FIELD_UA, g["ua"]); c.set(gb.FIELD_VA, g["va"])
+    mu, _, _ = c.weno5_adjoint(dt, lam, velocity=False)
+    assert np.abs(mu - ref).max() <= 1e-6 * np.abs(ref).max()
+    c.close()
+
+
+@pytest.mark.parametrize("name", ["bubbles_17", "bubbles_33", "tall_24x40"])
+def test_projection_adjoint_matches_finite_differences(gb, name):
+    g = load_golden(name)
+    dt = float(g["dt"])
+    c = make_ctx(gb, g)
+    # 1e-11: the FP64 MG-PCG's attainable relative residual on these systems lies near 2e-12
+    opts = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=1e-11, max_iterations=20000)
+    c.set(gb.FIELD_PHI, g["phi"])
+    rng = np.random.default_rng(9)
+    lu, lv, lp = rng.standard_normal(g["u"].shape), rng.standard_normal(g["v"].shape), rng.standard_normal(g["p"].shape)
+    lp[0, :] = lp[-1, :] = lp[:, 0] = lp[:, -1] = 0  # the pressure ghosts are not unknowns
+
+    def L(u, v):
+        c.set(gb.FIELD_U, u); c.set(gb.FIELD_V, v); c.set(gb.FIELD_P, g["p"])
+        c.projection(dt, opts, allow_max_iters=True)
+        return float(np.sum(lu * c.get(gb.FIELD_U)) + np.sum(lv * c.get(gb.FIELD_V)) + np.sum(lp * c.get(gb.FIELD_P)))
+
+    L(g["u"], g["v"])
+    mu, mv, st = c.projection_adjoint(dt, lu, lv, lp, opts)
+    assert st.rel_residual <= 1e-11
+    eps = 1e-3  # the map is affine in the velocity: only the solver tolerance limits the difference quotient
+    for k in range(4):
+        du, dv = rng.standard_normal(g["u"].shape), rng.standard_normal(g["v"].shape)
+        fd = (L(g["u"] + eps * du, g["v"] + eps * dv) - L(g["u"] - eps * du, g["v"] - eps * dv)) / (2 * eps)
+        ad = float(np.sum(mu * du) + np.sum(mv * dv))
+        assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-12), (k, ad, fd)
+    c.close()
+
+
+def window_case():
+    c = rising_bubble_case(33, 33, seed=11)
+    return c, 0.25 / 32
+
+
+def test_window_gradient_against_finite_differences(gb):
+    """Centroid height after 20 level-set RK3 steps, checkpoints every 10 steps: 16 seeded
+    unit directions, central differences with eps = 1e-6 (Richardson-extrapolated)."""
+    ag = importlib.import_module("2d_engine_gb300.autograd")
+    case, dt = window_case()
+    c = gb.Context(33, 33)
+    ua, va = torch.from_numpy(case["ua"]), torch.from_numpy(case["va"])
+    phi0 = torch.from_numpy(case["phi"].copy()).requires_grad_(True)
+    loss = ag.window_loss(c, phi0, ua, va, dt, steps=20, checkpoint_every=10)
+    loss.backward()
+    grad = phi0.grad.numpy().copy()
+    rng = np.random.default_rng(12)
+    with torch.no_grad():
+        f = lambda p: float(ag.window_loss(c, torch.from_numpy(p), ua, va, dt, steps=20))
+        for k in range(16):
+            d = rng.standard_normal(case["phi"].shape)
+            d /= np.linalg.norm(d)
+            fd = central(f, case["phi"], d)
+            ad = float(np.sum(grad * d))
+            assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-3 * np.linalg.norm(grad)), (k, ad, fd)
+    c.close()
+
+
+def test_window_gradient_against_oracle_reference(gb, oracle):
+    """The same window at 17^2 over 10 steps against the FP64 oracle's component-wise central differences."""
+    ag = importlib.import_module("2d_engine_gb300.autograd")
+    case = rising_bubble_case(17, 17, seed=13)
+    dt, steps = 0.25 / 16, 10
+    ni = nj = 17
+    gr = oracle.grid(ni, nj)
+    pr = oracle.params()
+    it = (slice(2, 2 + nj), slice(2, 2 + ni))
+
+    def loss_np(p0):
+        p = p0.copy()
+        for _ in range(steps):
+            keep = p[it].copy()
+            oracle.levelset_advection(gr, pr, p, case["ua"].copy(), case["va"].copy(), dt)
+            oracle.levelset_advection(gr, pr, p, case["ua"].copy(), case["va"].copy(), dt)
+            p[it] = 0.75 * keep + 0.25 * p[it]
+            oracle.levelset_advection(gr, pr, p, case["ua"].copy(), case["va"].copy(), dt)
+            p[it] = (1 / 3.0) * keep + (2 / 3.0) * p[it]
+        return float(ag.centroid_height(torch.from_numpy(p), ni, nj))
+
+    base = case["phi"].copy()
+    ref = np.zeros_like(base)
+    for idx in np.ndindex(base.shape):
+        e = np.zeros_like(base)
+        e[idx] = 1.0
+        ref[idx] = central(loss_np, base, e)
+    c = gb.Context(ni, nj)
+    phi0 = torch.from_numpy(base.copy()).requires_grad_(True)
+    ag.window_loss(c, phi0, torch.from_numpy(case["ua"]), torch.from_numpy(case["va"]), dt, steps=steps,
+                   checkpoint_every=5).backward()
+    got = phi0.grad.numpy()
+    assert np.abs(got - ref).max() <= GRAD_TOL * np.abs(ref).max()
+    c.close()
