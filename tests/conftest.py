@@ -33,7 +33,15 @@ def gb():
 
 
 def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    """The per-case fixtures (inputs and single-call outputs); multi-frame runs are separate."""
+    import numpy as np
+    names = []
+    for f in sorted(os.listdir(GOLDEN)):
+        if f.endswith(".npz"):
+            with np.load(os.path.join(GOLDEN, f)) as z:
+                if "ni" in z.files:
+                    names.append(f[:-4])
+    return names
 
 
 def load_golden(name):

@@ -20,6 +20,8 @@ tests/golden/cases.py and stores inputs and outputs:
   time_step           AdvanceOneTimeStepThread (order 3), without viscosity (the
                       reference's air/water setup) and with it configured
   cfl                 CFLOneTimeStep after ComputeCurvaturesThread
+and, in rising_bubble_128_frames.npz, 100 frames of the 128^2 rising bubble
+(SIMULATION_WORLD::AdvanceOneFrame: curvature, CFL time step, time step).
 
 Usage:  python tests/golden/make_golden.py   (needs the reference sources)
 """
@@ -150,6 +152,40 @@ def make_flow(out, c, dt, pcg_tolerance):
         s.close()
 
 
+def make_rising_bubble_run(name, n=128, steps=100, keep=(10,)):
+    """The rising bubble on [0,1]^2 run by the reference itself, frame by frame as
+    SIMULATION_WORLD::AdvanceOneFrame does (curvature, dt = CFLOneTimeStep() * CFL with
+    CFL = 1, AdvanceOneTimeStepThread): bubble of radius 0.15 at (0.5, 0.3), rho 1 / 1000,
+    sigma 0.0728, gravity -9.8, cfl_number 0.5, reinitialisation every step.  The initial
+    level set is built as SIMULATION_WORLD.h:408-415 builds its bubbles: interior values,
+    ghosts copied from the second interior line, corners left at the solver's init."""
+    s = R.RefSim(n, n, 0.0, 0.0, 1.0, 1.0, **PHYS, **FLOW, pcg_tolerance=1e-13, pcg_max_iterations=200000, cfl_number=0.5)
+    phi = s.get(R.PHI)
+    x = np.arange(n) / (n - 1.0)
+    X, Y = np.meshgrid(x, x)
+    phi[2:2 + n, 2:2 + n] = np.sqrt((X - 0.5) ** 2 + (Y - 0.3) ** 2) - 0.15
+    phi[2:2 + n, 0:2] = phi[2:2 + n, 3:4]            # FillGhostCellsFrom: second interior line
+    phi[2:2 + n, 2 + n:] = phi[2:2 + n, n:n + 1]
+    phi[0:2, 2:2 + n] = phi[3:4, 2:2 + n]
+    phi[2 + n:, 2:2 + n] = phi[n:n + 1, 2:2 + n]
+    s.set(R.PHI, phi)
+    out = dict(phi0=phi.copy(), n=n, steps=steps, pcg_tolerance=1e-13)
+    dts = []
+    for k in range(1, steps + 1):
+        s.curvature()
+        dt = s.cfl_dt() * 1.0
+        dts.append(dt)
+        s.step(dt)
+        if k in keep or k == steps:
+            for f, key in ((R.PHI, "phi"), (R.U, "u"), (R.V, "v"), (R.P, "p")):
+                out[f"{key}{k}"] = s.get(f)
+    out["dts"] = np.array(dts)
+    s.close()
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB, dt {dts[0]:.3e} .. {dts[-1]:.3e}")
+
+
 def main():
     if not R.available():
         sys.exit("oracle/_ref/libref2d.so missing: run `make -C oracle/ref` where the reference sources are present")
@@ -158,6 +194,7 @@ def main():
     make_case("rising_bubble_40x24", rising_bubble_case(40, 24, seed=3), 0.01, 1e-13)
     make_case("tall_24x40", bubbles_case(24, 40, seed=4, x_max=1.0, y_max=2.0), 0.02, 1e-13)
     make_case("bubbles_65", bubbles_case(65, seed=5), 0.5 / 64, 1e-12, flow=False)
+    make_rising_bubble_run("rising_bubble_128_frames")
 
 
 if __name__ == "__main__":

@@ -153,3 +153,24 @@ def test_cfl_time_step(oracle, name):
     dt, rates = oracle.cfl_time_step(gr, oracle.params(), oracle.flow(), g["u"], g["v"], k, 0.5)
     assert dt == float(g["cfl_dt"]) and dt > 0
     assert all(r > 0 for r in rates)
+
+
+def test_rising_bubble_frames(oracle):
+    """Ten frames of the 128^2 rising bubble (curvature, CFL time step, order-3 step) equal
+    the reference's own frames bit for bit, time steps included."""
+    g = load_golden("rising_bubble_128_frames")
+    n = int(g["n"])
+    gr = oracle.grid(n, n)
+    pr = oracle.params(pcg_tolerance=float(g["pcg_tolerance"]), pcg_max_iterations=200000)
+    fl = oracle.flow(water_viscosity=1.0, air_viscosity=0.01, gravity=(0.0, -9.8), viscosity=False)
+    phi = g["phi0"].copy()
+    u, v = np.zeros((n + 4, n + 5)), np.zeros((n + 5, n + 4))
+    ua, va = np.zeros((n + 6, n + 7)), np.zeros((n + 7, n + 6))
+    p, k = np.zeros((n + 2, n + 2)), np.zeros((n, n))
+    for frame in range(10):
+        oracle.curvature(gr, phi, k)
+        dt, _ = oracle.cfl_time_step(gr, pr, fl, u, v, k, 0.5)
+        assert dt == float(g["dts"][frame])
+        oracle.time_step(gr, pr, fl, phi, u, v, ua, va, p, k, None, dt)
+    for got, key in ((phi, "phi10"), (u, "u10"), (v, "v10"), (p, "p10")):
+        np.testing.assert_array_equal(got, g[key])
