@@ -1,7 +1,8 @@
 """Build recipe of the in-tree CUDA library (libgb2d.so) for sm_103a.
 
 Compiles the csrc/ translation units in parallel with nvcc and links them into
-2d_engine_gb300/_build/libgb2d.so (static CUDA runtime, C ABI of include/gb2d.h).
+2d_engine_gb300/_build/libgb2d.so (static CUDA runtime, C ABI of include/gb2d.h),
+then the headless .sim driver 2d_engine_gb300/_build/gb2d_sim (driver/, C++).
 gb2d_exact.cu and gb2d_flow.cu are built with --fmad=false: their FP64 kernels
 must round every multiply and add separately, exactly as the reference's CPU
 arithmetic.
@@ -75,7 +76,29 @@ def build(verbose=False, ptxas_info=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")
+    build_driver()
     return LIB
+
+
+DRIVER_DIR = os.path.join(HERE, "driver")
+SIM = os.path.join(OUT, "gb2d_sim")
+
+
+def build_driver():
+    """The headless .sim driver (C++, host compiler only), linked to libgb2d.so."""
+    src = os.path.join(DRIVER_DIR, "gb2d_sim.cpp")
+    deps = [src, os.path.join(DRIVER_DIR, "script.hpp"), os.path.join(ROOT, "include", "gb2d.h"), LIB]
+    if not _stale(SIM, deps):
+        return SIM
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("no C++ compiler for the .sim driver")
+    cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"), "-I", DRIVER_DIR, src, "-o", SIM,
+           "-L", OUT, "-lgb2d", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"gb2d_sim build failed:\n{r.stderr}")
+    return SIM
 
 
 if __name__ == "__main__":
