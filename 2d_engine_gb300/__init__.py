@@ -54,6 +54,11 @@ class SolveStatsT(ctypes.Structure):
                 ("max_velocity_x", ctypes.c_double), ("max_velocity_y", ctypes.c_double)]
 
 
+class BatchStatsT(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_int), ("instances", ctypes.c_int), ("cg_iterations", ctypes.c_longlong),
+                ("max_rel_residual", ctypes.c_double), ("wall_ms", ctypes.c_double), ("cell_frames_per_s", ctypes.c_double)]
+
+
 class GB2DError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"gb2d error {code} ({ERRORS.get(code, '?')}): {msg}")
@@ -97,6 +102,12 @@ def library():
         "gb2d_advance_frame": [vp, d, ctypes.POINTER(d), O, S],
         "gb2d_weno5_adjoint": [vp, d, vp, vp, vp, vp],
         "gb2d_projection_adjoint": [vp, d, vp, vp, vp, vp, vp, O, S],
+        "gb2d_batch_create": [i, G, P, ctypes.POINTER(FlowParamsT), i, ctypes.POINTER(vp)],
+        "gb2d_batch_destroy": [vp],
+        "gb2d_batch_size": [vp, ctypes.POINTER(i), ctypes.POINTER(i)],
+        "gb2d_batch_context": [vp, i, ctypes.POINTER(vp)],
+        "gb2d_batch_autotune": [vp, d, O, vp],
+        "gb2d_batch_advance": [vp, i, d, vp, O, ctypes.POINTER(BatchStatsT)],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
         "gb2d_poisson_solve": [vp, vp, vp, O, S],
@@ -116,6 +127,8 @@ def library():
         f.restype = i
     L.gb2d_last_error.argtypes = [vp]
     L.gb2d_last_error.restype = ctypes.c_char_p
+    L.gb2d_batch_last_error.argtypes = [vp]
+    L.gb2d_batch_last_error.restype = ctypes.c_char_p
     _lib = L
     return L
 
@@ -350,3 +363,84 @@ class Context:
         if rc != 0 and not (allow_max_iters and rc == -4):
             self._check(rc)
         return x, st
+
+
+class _View(Context):
+    """A context owned by a Batch (not destroyed by Python)."""
+
+    def __init__(self, L, h, ni, nj, grid):
+        self.L, self.h, self.ni, self.nj, self.grid = L, h, ni, nj, grid
+
+    def close(self):
+        self.h = None
+
+
+class Batch:
+    """Independent simulations of uneven sizes advanced together (gb2d_batch_*)."""
+
+    def __init__(self, sizes, params=None, flows=None, workers=0):
+        """sizes: list of (ni, nj, x_max, y_max) on [0, x_max] x [0, y_max]; params / flows: per-instance
+        dicts for Context's keyword arguments / set_flow_params (or one dict for all)."""
+        self.L = library()
+        n = len(sizes)
+        G = (GridT * n)(*[GridT(ni, nj, 0.0, 0.0, xm, ym) for ni, nj, xm, ym in sizes])
+
+        def each(x, k):
+            return (x[k] if isinstance(x, (list, tuple)) else x) or {}
+
+        P = (ParamsT * n)()
+        F = (FlowParamsT * n)()
+        for k in range(n):
+            p = dict(water_density=1000.0, air_density=1.0, surface_tension=0.0728, weno_epsilon=1e-6,
+                     reinit_iterations=25, reinit_scaling=5, advection_precision=PRECISION_MIXED)
+            p.update(each(params, k))
+            P[k] = ParamsT(p["water_density"], p["air_density"], p["surface_tension"], p["weno_epsilon"],
+                           p["reinit_iterations"], p["reinit_scaling"], p["advection_precision"])
+            f = dict(water_viscosity=1.0, air_viscosity=0.0, gravity=(0.0, -9.8), cfl_number=0.5, viscosity=False)
+            f.update(each(flows, k))
+            F[k] = FlowParamsT(f["water_viscosity"], f["air_viscosity"], f["gravity"][0], f["gravity"][1], f["cfl_number"],
+                               int(bool(f["viscosity"])))
+        h = ctypes.c_void_p()
+        rc = self.L.gb2d_batch_create(n, G, P, F, workers, ctypes.byref(h))
+        if rc != 0:
+            raise GB2DError(rc, "gb2d_batch_create failed")
+        self.h, self.n, self.sizes, self.grids = h, n, sizes, G
+        nn, w = ctypes.c_int(), ctypes.c_int()
+        self.L.gb2d_batch_size(self.h, ctypes.byref(nn), ctypes.byref(w))
+        self.workers = w.value
+
+    def _check(self, rc):
+        if rc != 0:
+            raise GB2DError(rc, self.L.gb2d_batch_last_error(self.h).decode(errors="replace"))
+
+    def context(self, k):
+        c = ctypes.c_void_p()
+        self._check(self.L.gb2d_batch_context(self.h, k, ctypes.byref(c)))
+        ni, nj = self.sizes[k][0], self.sizes[k][1]
+        return _View(self.L, c, ni, nj, self.grids[k])
+
+    def autotune(self, cfl=1.0, opts=None):
+        opts = opts or solve_opts(precision=PRECISION_MIXED)
+        out = (ctypes.c_int * self.n)()
+        self._check(self.L.gb2d_batch_autotune(self.h, cfl, ctypes.byref(opts), out))
+        return list(out)
+
+    def advance(self, frames, cfl=1.0, dts=None, opts=None, allow_max_iters=False):
+        opts = opts or solve_opts(precision=PRECISION_MIXED)
+        dts = np.zeros(self.n) if dts is None else np.ascontiguousarray(dts, dtype=np.float64)
+        st = BatchStatsT()
+        rc = self.L.gb2d_batch_advance(self.h, frames, cfl, _ptr(dts), ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return dts, st
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gb2d_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -26,6 +26,7 @@ UNITS = {
     "gb2d_api.cu": [],
     "gb2d_noalloc.cu": [],
     "gb2d_adjoint.cu": [],
+    "gb2d_batch.cu": [],
 }
 
 

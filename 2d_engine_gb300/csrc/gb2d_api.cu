@@ -9,7 +9,8 @@
 
 namespace gb2d {
 
-unsigned long long g_launches = 0;
+std::atomic<unsigned long long> g_launches{0};
+thread_local unsigned long long* t_capture_count = nullptr;
 
 Space make_space(int ires, int jres, double x_min, double y_min, double x_max, double y_max) {
   Space s;
@@ -349,7 +350,7 @@ int gb2d_check_exact_division(unsigned long long n, unsigned long long seed, uns
 
 int gb2d_kernel_launches(unsigned long long* count) {
   if (!count) return GB2D_ERR_ARG;
-  *count = gb2d::g_launches;
+  *count = gb2d::g_launches.load();
   return GB2D_OK;
 }
 

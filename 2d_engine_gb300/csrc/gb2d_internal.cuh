@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "gb2d.h"
 
 namespace gb2d {
@@ -112,8 +114,12 @@ struct Scalars {
 struct Solver;  // defined in gb2d_solver.cu
 
 // Kernels launched by this library (process-wide), reported by gb2d_kernel_launches.
-extern unsigned long long g_launches;
-#define GB_LAUNCHED(n) (::gb2d::g_launches += (n))
+// Launches made while this thread captures a graph count into t_capture_count instead
+// (they run, and are counted, when the graph is launched).
+extern std::atomic<unsigned long long> g_launches;
+extern thread_local unsigned long long* t_capture_count;
+#define GB_LAUNCHED(n) \
+  (::gb2d::t_capture_count ? (void)(*::gb2d::t_capture_count += (n)) : (void)(::gb2d::g_launches += (n)))
 
 // Event brackets around one kernel's launches (roofline measurement).
 struct Probe {

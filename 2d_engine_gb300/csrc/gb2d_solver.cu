@@ -35,6 +35,7 @@
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <utility>
 
 #include "gb2d_internal.cuh"
@@ -1246,16 +1247,17 @@ void enqueue_iter(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv
 template <typename F>
 bool capture_graph(gb2d_ctx* c, cudaGraphExec_t* exec, unsigned long long* nodes, F fn) {
   cudaStream_t cs = c->own_stream;
-  unsigned long long before = g_launches;
   if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
+  unsigned long long captured = 0;
+  t_capture_count = &captured;  // captured launches are counted when the graph runs
   fn(cs);
+  t_capture_count = nullptr;
   cudaGraph_t g = nullptr;
   cudaError_t e = cudaStreamEndCapture(cs, &g);
-  *nodes = g_launches - before;
-  g_launches = before;  // captured launches are counted when the graph runs
+  *nodes = captured;
   if (e != cudaSuccess || !g) {
     cudaGetLastError();
     return false;
@@ -1350,6 +1352,9 @@ cudaError_t set_smooth_smem() {
 }  // namespace
 
 Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
+  // Kernel attributes and the cluster-size probe are process-wide: one creation at a time.
+  static std::mutex create_lock;
+  std::lock_guard<std::mutex> hold(create_lock);
   Solver* S = new Solver();
   S->ni = ni;
   S->nj = nj;

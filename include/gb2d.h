@@ -232,6 +232,37 @@ int gb2d_weno5_adjoint(gb2d_ctx* ctx, double dt, const double* lam_phi, double* 
 int gb2d_projection_adjoint(gb2d_ctx* ctx, double dt, const double* lam_u, const double* lam_v, const double* lam_p, double* mu_u,
                             double* mu_v, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
 
+/* Batches: many independent simulations of uneven grid sizes on one GPU (no counterpart
+ * in the reference, which runs one simulation per process).  Each instance is a full
+ * context with its own stream; host worker threads drive disjoint sets of instances frame
+ * by frame so that small grids overlap on the GPU.  Instances are placed on workers
+ * longest-first by cost per frame (cells until gb2d_batch_autotune has measured them).
+ * Set each instance's fields through gb2d_batch_context; the contexts belong to the batch.
+ * workers <= 0 picks min(host threads, 16). */
+typedef struct gb2d_batch gb2d_batch;
+typedef struct {
+  int frames;                /* frames advanced per instance */
+  int instances;
+  long long cg_iterations;   /* summed over every projection of every instance */
+  double max_rel_residual;   /* largest final relative residual of any projection */
+  double wall_ms;            /* host wall time of the call (all work finished) */
+  double cell_frames_per_s;  /* sum of instance cells x frames / wall time */
+} gb2d_batch_stats;
+int gb2d_batch_create(int n, const gb2d_grid* grids, const gb2d_params* params, const gb2d_flow_params* flows, int workers,
+                      gb2d_batch** out);
+int gb2d_batch_destroy(gb2d_batch* batch);
+const char* gb2d_batch_last_error(const gb2d_batch* batch);
+int gb2d_batch_size(const gb2d_batch* batch, int* n, int* workers);
+int gb2d_batch_context(gb2d_batch* batch, int k, gb2d_ctx** ctx);
+/* Autotuner: for each distinct grid size, time one frame (gb2d_advance_frame with cfl)
+ * with 1, 2 and 3 red-black sweeps per V-cycle side from the instance's current state
+ * (restored afterwards), keep the fastest for every instance of that size (smooth_out[k],
+ * may be NULL) and re-place the instances on the workers by the measured times. */
+int gb2d_batch_autotune(gb2d_batch* batch, double cfl, const gb2d_solve_opts* opts, int* smooth_out);
+/* gb2d_advance_frame for every instance, frames times.  dts[k]: instance k's previous time
+ * step in, its last step out.  opts' mg_smooth is replaced per instance by the tuned value. */
+int gb2d_batch_advance(gb2d_batch* batch, int frames, double cfl, double* dts, const gb2d_solve_opts* opts, gb2d_batch_stats* stats);
+
 /* Standalone pieces of the pressure system for parity checks and for
  * POISSON_SOLVER_2D-style use (a10, a15).  gb2d_poisson_assemble runs the
  * curvature step (which extrapolates phi's ghosts) and builds the system of the
