@@ -166,6 +166,81 @@ def cpu_baseline(case, sample_iterations, full_iterations):
     return total_ms, per_iter * 1e3, st.iterations
 
 
+BATCH_INSTANCES, BATCH_FRAMES, BATCH_SEED = 256, 10, 3
+
+
+def run_batch(gb, n, frames, cpu=True):
+    """Independent rising bubbles of uneven sizes (64^2 to 512^2) advanced together by the
+    batched runtime (mixed precision, relative residual 1e-8, autotuned V-cycles), with
+    the same instances on one worker thread for comparison and the reference's solver
+    (the oracle) timed on a bounded sample and extrapolated."""
+    import numpy as np
+    from tests.golden.cases import batched_bubbles
+    grids, phis, params, flows = batched_bubbles(n, seed=BATCH_SEED)
+    for p in params:
+        p["advection_precision"] = gb.PRECISION_MIXED
+    opts = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=TOL)
+    out = {"instances": n, "frames": frames, "sizes": {str(N): sum(1 for g in grids if g[0] == N) for N in (64, 128, 256, 512)}}
+    walls = {}
+    for workers in (0, 1):
+        t0 = time.perf_counter()
+        b = gb.Batch(grids, params=params, flows=flows, workers=workers)
+        for k in range(n):
+            b.context(k).set(gb.FIELD_PHI, phis[k])
+        t1 = time.perf_counter()
+        smooth = b.autotune(cfl=1.0, opts=opts)
+        t2 = time.perf_counter()
+        f = frames if workers == 0 else max(1, frames // 5)
+        dts, st = b.advance(f, cfl=1.0, opts=opts, allow_max_iters=True)
+        walls[workers] = st.wall_ms / f
+        if workers == 0:
+            cells = sum(g[0] * g[1] for g in grids)
+            out.update({"workers": b.workers, "create_s": t1 - t0, "autotune_s": t2 - t1, "wall_ms": st.wall_ms,
+                        "ms_per_frame_all_instances": st.wall_ms / f, "instance_frames_per_s": n * f / (st.wall_ms * 1e-3),
+                        "cell_frames_per_s": st.cell_frames_per_s, "cells": cells,
+                        "cg_iterations_per_projection": st.cg_iterations / (3.0 * n * f), "max_rel_residual": st.max_rel_residual,
+                        "mg_smooth_by_size": {str(g[0]): smooth[k] for k, g in enumerate(grids)}})
+        b.close()
+    out["one_worker_ms_per_frame_all_instances"] = walls[1]
+    out["speedup_vs_one_worker"] = walls[1] / walls[0]
+    if cpu:
+        out["cpu_reference"] = batch_cpu_estimate(grids, params, flows, frames)
+    return out
+
+
+def batch_cpu_estimate(grids, params, flows, frames):
+    """The reference's solver (the oracle: IC(0)-PCG to the same relative residual,
+    single-threaded) timed for one frame of a 64^2 and a 128^2 instance of the batch;
+    the per-frame cost is fitted as c N^a and summed over the batch."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle2d
+    from tests.golden.cases import bubble_level_set
+    oracle2d.build()
+    ms = {}
+    for N in (64, 128):
+        k = next(i for i, g in enumerate(grids) if g[0] == N)
+        gr = oracle2d.grid(N, N)
+        pr = oracle2d.params(water_density=params[k]["water_density"], air_density=1.0, pcg_tolerance=0.0,
+                             pcg_max_iterations=100000, pcg_rel_residual=TOL)
+        fl = oracle2d.flow(water_viscosity=flows[k]["water_viscosity"], air_viscosity=0.01, viscosity=True)
+        phi = bubble_level_set(N, N, 1.0, 0.5, 0.3, 0.15)
+        u, v = np.zeros((N + 4, N + 5)), np.zeros((N + 5, N + 4))
+        ua, va = np.zeros((N + 6, N + 7)), np.zeros((N + 7, N + 6))
+        p, kap = np.zeros((N + 2, N + 2)), np.zeros((N, N))
+        t0 = time.perf_counter()
+        oracle2d.curvature(gr, phi, kap)
+        dt, _ = oracle2d.cfl_time_step(gr, pr, fl, u, v, kap, 0.5)
+        oracle2d.time_step(gr, pr, fl, phi, u, v, ua, va, p, kap, None, dt)
+        ms[N] = (time.perf_counter() - t0) * 1e3
+    a = np.log(ms[128] / ms[64]) / np.log(2.0)
+    total_ms = sum(ms[64] * (g[0] / 64.0) ** a for g in grids) * frames
+    return {"kind": "port", "cores": 1, "ms_per_frame_64": ms[64], "ms_per_frame_128": ms[128], "exponent": a,
+            "estimated_s_for_batch": total_ms * 1e-3,
+            "sample": "oracle frame (level-set RK3, reinit, 3 SolveForRK with IC(0)-PCG to 1e-8) at 64^2 and 128^2, "
+                      "fitted c N^a and summed over the batch's instances and frames"}
+
+
 def ref_full_iterations():
     path = os.path.join(ROOT, "profiles", "cpu_reference_1024.json")
     try:
@@ -346,6 +421,8 @@ def run_gb300(args):
         time_step[name + "_projection_iterations"] = statistics.mean(its)
         cs.close()
 
+    batch = run_batch(gb, BATCH_INSTANCES, BATCH_FRAMES, cpu=not args.no_cpu)
+
     ms_step = max_over_ranks(dist, statistics.mean(ms_m))
     value = ms_step / ws
     e2e_ms = max_over_ranks(dist, statistics.mean(e2e)) / ws
@@ -372,7 +449,7 @@ def run_gb300(args):
                    "rel_residual_mixed": st_m.rel_residual,
                    "fp64_mgpcg_ms": statistics.mean(ms_64), "iterations_fp64": statistics.mean(it_64), "rel_residual_fp64": st_64.rel_residual,
                    "mixed_vs_fp64_rel_l2_p": diff, "replicas": ws,
-                   "levelset_rk3_1024": levelset, "time_step_1024": time_step},
+                   "levelset_rk3_1024": levelset, "time_step_1024": time_step, "batched_rising_bubbles": batch},
         "clocks": clk,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

@@ -97,3 +97,36 @@ def rising_bubble_case(ni, nj=None, seed=0):
     return dict(phi=np.ascontiguousarray(phi), u=embed(u_int, 2), v=embed(v_int, 2),
                 ua=copy_ghosts(u_int, 3), va=copy_ghosts(v_int, 3), p=np.zeros((nj + 2, ni + 2)),
                 ni=ni, nj=nj, x_max=1.0, y_max=1.0)
+
+
+def bubble_level_set(ni, nj, y_max, cx, cy, r):
+    """Signed distance to a circle at (cx, cy) on [0,1] x [0,y_max] (dx = dy when
+    y_max = (nj-1)/(ni-1)), built as the reference builds its bubbles: interior values,
+    ghosts copied from the second interior line, corners at dx."""
+    dx = 1.0 / (ni - 1)
+    phi = np.full((nj + 4, ni + 4), dx)
+    X, Y = np.meshgrid(np.arange(ni) * dx, np.arange(nj) * (y_max / (nj - 1)))
+    phi[2:2 + nj, 2:2 + ni] = np.sqrt((X - cx) ** 2 + (Y - cy) ** 2) - r
+    phi[2:2 + nj, 0:2] = phi[2:2 + nj, 3:4]
+    phi[2:2 + nj, 2 + ni:] = phi[2:2 + nj, ni:ni + 1]
+    phi[0:2, 2:2 + ni] = phi[3:4, 2:2 + ni]
+    phi[2 + nj:, 2:2 + ni] = phi[nj:nj + 1, 2:2 + ni]
+    return phi
+
+
+def batched_bubbles(n, seed=0, sizes=(64, 128, 256, 512)):
+    """Independent rising bubbles: grid N^2 with N uniform over `sizes`, radius U[0.1,0.2],
+    centre (0.5, U[0.2,0.4]), density ratio log-uniform in [10,1000] (air 1), viscosity
+    ratio log-uniform in [1,100] (air 0.01).  Returns (grid sizes, level sets, params, flows)."""
+    rng = np.random.default_rng(seed)
+    grids, phis, params, flows = [], [], [], []
+    for _ in range(n):
+        N = int(rng.choice(sizes))
+        r, cy = rng.uniform(0.1, 0.2), rng.uniform(0.2, 0.4)
+        rho = float(np.exp(rng.uniform(np.log(10), np.log(1000))))
+        mu = float(np.exp(rng.uniform(np.log(1), np.log(100))))
+        grids.append((N, N, 1.0, 1.0))
+        phis.append(bubble_level_set(N, N, 1.0, 0.5, cy, r))
+        params.append(dict(water_density=rho, air_density=1.0))
+        flows.append(dict(water_viscosity=0.01 * mu, air_viscosity=0.01, viscosity=True))
+    return grids, phis, params, flows

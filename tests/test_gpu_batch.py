@@ -4,25 +4,11 @@ one by one, and the autotuner's choices are valid sweep counts."""
 import numpy as np
 import pytest
 
+from tests.golden.cases import bubble_level_set
+
 pytestmark = pytest.mark.gpu
 
 SIZES = [(32, 32), (48, 48), (64, 64), (40, 56), (64, 96), (33, 33)]
-
-
-def bubble_phi(ni, nj, y_max, cy, r):
-    """Signed distance to a circle at (0.5, cy) on [0,1] x [0,y_max] with dx = dy, ghosts copied
-    from the second interior line and corners at dx, as the .sim driver builds it."""
-    dx = 1.0 / (ni - 1)
-    phi = np.full((nj + 4, ni + 4), dx)
-    x = np.arange(ni) * dx
-    y = np.arange(nj) * (y_max / (nj - 1))
-    X, Y = np.meshgrid(x, y)
-    phi[2:2 + nj, 2:2 + ni] = np.sqrt((X - 0.5) ** 2 + (Y - cy) ** 2) - r
-    phi[2:2 + nj, 0:2] = phi[2:2 + nj, 3:4]
-    phi[2:2 + nj, 2 + ni:] = phi[2:2 + nj, ni:ni + 1]
-    phi[0:2, 2:2 + ni] = phi[3:4, 2:2 + ni]
-    phi[2 + nj:, 2:2 + ni] = phi[nj:nj + 1, 2:2 + ni]
-    return phi
 
 
 def setup():
@@ -31,7 +17,7 @@ def setup():
     for ni, nj in SIZES:
         y_max = (nj - 1) / (ni - 1)
         sizes.append((ni, nj, 1.0, y_max))
-        phis.append(bubble_phi(ni, nj, y_max, rng.uniform(0.2, 0.4), rng.uniform(0.1, 0.2)))
+        phis.append(bubble_level_set(ni, nj, y_max, 0.5, rng.uniform(0.2, 0.4), rng.uniform(0.1, 0.2)))
         params.append(dict(water_density=float(np.exp(rng.uniform(np.log(10), np.log(1000))))))
     return sizes, phis, params
 
