@@ -174,6 +174,35 @@ def cpu_baseline(case, sample_iterations, full_iterations):
 BATCH_INSTANCES, BATCH_FRAMES, BATCH_SEED = 256, 10, 3
 
 
+def run_rayleigh_taylor(gb, stream, n=2048, frames=4):
+    """Rayleigh-Taylor on 2048 x 2048 nodes over [0,1] x [0,2] (dy = 2 dx, the reference's
+    dx-only diagonal): interface y = 1 + 0.05 cos(2 pi x), densities 3 over 1, viscosity 1e-3,
+    no surface tension; mixed precision (FP32 WENO5 / reinit / ENO3 fluxes, FP32 V-cycles),
+    CFL time steps.  One untimed frame, then `frames` timed with CUDA events."""
+    import torch
+    from tests.golden.cases import rayleigh_taylor_level_set
+    c = gb.Context(n, n, 0.0, 0.0, 1.0, 2.0, water_density=3.0, air_density=1.0, surface_tension=0.0,
+                   advection_precision=gb.PRECISION_MIXED)
+    c.set_stream(stream.cuda_stream)
+    c.set_flow_params(water_viscosity=1e-3, air_viscosity=1e-3, gravity=(0.0, -9.8), viscosity=True, cfl_number=0.5)
+    c.set(gb.FIELD_PHI, rayleigh_taylor_level_set(n, n))
+    opts = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=TOL)
+    dt, _ = c.advance_frame(cfl=1.0, prev_dt=0.0, opts=opts, allow_max_iters=True)
+    ms, its = [], []
+    for _ in range(frames):
+        with torch.cuda.stream(stream):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dt, st = c.advance_frame(cfl=1.0, prev_dt=dt, opts=opts, allow_max_iters=True)
+            e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        its.append(st.iterations / 3.0)
+    c.close()
+    return {"nodes": [n, n], "domain": [1.0, 2.0], "frames_timed": frames, "ms_per_frame": statistics.mean(ms),
+            "cg_iterations_per_projection": statistics.mean(its), "last_dt": dt, "precision": "mixed"}
+
+
 def run_batch(gb, n, frames, cpu=True, dist=None, rank=0, ws=1):
     """Independent rising bubbles of uneven sizes (64^2 to 512^2) advanced together by the
     batched runtime (mixed precision, relative residual 1e-8, autotuned V-cycles), with
@@ -434,6 +463,7 @@ def run_gb300(args):
         cs.close()
 
     batch = run_batch(gb, BATCH_INSTANCES, BATCH_FRAMES, cpu=not args.no_cpu and rank == 0, dist=dist, rank=rank, ws=ws)
+    rt = run_rayleigh_taylor(gb, stream)
 
     ms_step = max_over_ranks(dist, statistics.mean(ms_m))
     value = ms_step / ws
@@ -461,7 +491,8 @@ def run_gb300(args):
                    "rel_residual_mixed": st_m.rel_residual,
                    "fp64_mgpcg_ms": statistics.mean(ms_64), "iterations_fp64": statistics.mean(it_64), "rel_residual_fp64": st_64.rel_residual,
                    "mixed_vs_fp64_rel_l2_p": diff, "replicas": ws,
-                   "levelset_rk3_1024": levelset, "time_step_1024": time_step, "batched_rising_bubbles": batch},
+                   "levelset_rk3_1024": levelset, "time_step_1024": time_step, "batched_rising_bubbles": batch,
+                   "rayleigh_taylor_2048": rt},
         "clocks": clk,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

@@ -130,3 +130,17 @@ def batched_bubbles(n, seed=0, sizes=(64, 128, 256, 512)):
         params.append(dict(water_density=rho, air_density=1.0))
         flows.append(dict(water_viscosity=0.01 * mu, air_viscosity=0.01, viscosity=True))
     return grids, phis, params, flows
+
+
+def rayleigh_taylor_level_set(ni, nj, y_max=2.0, amplitude=0.05):
+    """phi = y - y_max/2 - amplitude cos(2 pi x) on [0,1] x [0,y_max] (heavy fluid where
+    phi > 0, above the interface), ghosts copied from the second interior line, corners at dx."""
+    dx = 1.0 / (ni - 1)
+    phi = np.full((nj + 4, ni + 4), dx)
+    X, Y = np.meshgrid(np.arange(ni) * dx, np.arange(nj) * (y_max / (nj - 1)))
+    phi[2:2 + nj, 2:2 + ni] = Y - 0.5 * y_max - amplitude * np.cos(2 * np.pi * X)
+    phi[2:2 + nj, 0:2] = phi[2:2 + nj, 3:4]
+    phi[2:2 + nj, 2 + ni:] = phi[2:2 + nj, ni:ni + 1]
+    phi[0:2, 2:2 + ni] = phi[3:4, 2:2 + ni]
+    phi[2 + nj:, 2:2 + ni] = phi[nj:nj + 1, 2:2 + ni]
+    return phi
