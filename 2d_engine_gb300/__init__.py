@@ -108,6 +108,7 @@ def library():
         "gb2d_batch_context": [vp, i, ctypes.POINTER(vp)],
         "gb2d_batch_autotune": [vp, d, O, vp],
         "gb2d_batch_advance": [vp, i, d, vp, O, ctypes.POINTER(BatchStatsT)],
+        "gb2d_jump_poisson_solve": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, O, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
         "gb2d_poisson_solve": [vp, vp, vp, O, S],
@@ -339,6 +340,23 @@ class Context:
         if rc != 0 and not (allow_max_iters and rc == -4):
             self._check(rc)
         return mu, mv, st
+
+    def jump_poisson_solve(self, density, bc, div, levelset, jc_solution, jc_derivative, pressure, opts=None,
+                           allow_max_iters=False):
+        """General jump-condition Poisson problem (POISSON_SOLVER::Solve with jumps): returns
+        (solution, normal_x, normal_y, stats); pressure carries the Dirichlet values and warm start."""
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        d, dv, ls, js, jd = f(density), f(div), f(levelset), f(jc_solution), f(jc_derivative)
+        bci = np.ascontiguousarray(bc, dtype=np.int32)
+        p = f(pressure).copy()
+        nx, ny = np.zeros_like(p), np.zeros_like(p)
+        opts = opts or solve_opts(tolerance=1e-10)
+        st = SolveStatsT()
+        rc = self.L.gb2d_jump_poisson_solve(self.h, _ptr(d), bci.ctypes.data, _ptr(dv), _ptr(ls), _ptr(js), _ptr(jd), _ptr(p),
+                                            _ptr(nx), _ptr(ny), ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return p, nx, ny, st
 
     # Pressure system (a10/a15)
     def poisson_assemble(self, dt):

@@ -22,6 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = {
     "gb2d_exact.cu": ["--fmad=false"],
     "gb2d_flow.cu": ["--fmad=false"],
+    "gb2d_jump.cu": ["--fmad=false"],
     "gb2d_solver.cu": [],
     "gb2d_api.cu": [],
     "gb2d_noalloc.cu": [],

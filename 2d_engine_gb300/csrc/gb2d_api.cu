@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "gb2d_internal.cuh"
 
@@ -123,11 +124,13 @@ void free_ctx(gb2d_ctx* c) {
   double* bufs[] = {c->phi_buf[0], c->phi_buf[1], c->phi_buf[2], c->phi_buf[3], c->u, c->v, c->ua, c->va, c->p,
                     c->kappa, c->sign, c->bx, c->by, c->diag, c->rhs, c->tmp_a, c->tmp_b, c->xw, c->u_alt, c->v_alt,
                     c->u_keep, c->v_keep, c->density, c->adj_coef, c->adj_gvel, c->adj_lam_phi, c->adj_mu_phi,
-                    c->adj_lam_u, c->adj_lam_v, c->adj_mu_u, c->adj_mu_v, c->adj_lam_p};
+                    c->adj_lam_u, c->adj_lam_v, c->adj_mu_u, c->adj_mu_v, c->adj_lam_p, c->jmp_dens, c->jmp_div,
+                    c->jmp_js, c->jmp_jd, c->jmp_nx, c->jmp_ny, c->jmp_phi};
   for (auto b : bufs)
     if (b) cudaFree(b);
   for (auto b : c->ckpt)
     if (b) cudaFree(b);
+  if (c->jmp_bc) cudaFree(c->jmp_bc);
   if (c->sc) cudaFree(c->sc);
   if (c->host_stage) cudaFreeHost(c->host_stage);
   if (c->probe.ev) {
@@ -637,6 +640,49 @@ int gb2d_projection_adjoint(gb2d_ctx* c, double dt, const double* lam_u, const d
   return src;
 }
 
+int gb2d_jump_poisson_solve(gb2d_ctx* c, const double* density, const int* bc, const double* div, const double* levelset,
+                            const double* jc_solution, const double* jc_derivative, double* pressure, double* normal_x,
+                            double* normal_y, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
+  if (!c || !density || !bc || !div || !levelset || !jc_solution || !jc_derivative || !pressure || !o) return GB2D_ERR_ARG;
+  int rc = jump_buffers(c);
+  if (rc) {
+    snprintf(c->err, sizeof(c->err), "jump_poisson_solve: device allocation failed");
+    return rc;
+  }
+  const size_t ni = c->grid.ni, nj = c->grid.nj, np = (ni + 2) * (nj + 2), nphi = (ni + 4) * (nj + 4);
+  const cudaMemcpyKind h2d = cudaMemcpyHostToDevice;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->jmp_dens, density, np * sizeof(double), h2d, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->jmp_bc, bc, np * sizeof(int), h2d, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->jmp_div, div, np * sizeof(double), h2d, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->jmp_phi, levelset, nphi * sizeof(double), h2d, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->jmp_js, jc_solution, np * sizeof(double), h2d, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->jmp_jd, jc_derivative, np * sizeof(double), h2d, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->xw, pressure, np * sizeof(double), h2d, c->stream));
+  launch_jump_assemble(c->stream, c);
+  if ((rc = check_launch(c, "jump_poisson_assemble"))) return rc;
+  gb2d_solve_stats local;
+  memset(&local, 0, sizeof local);
+  c->sys_shift = c->tmp_b;  // the solver's levels take this system's diagonal shift
+  int src = solver_solve(c, c->rhs, c->xw, o, &local);
+  c->sys_shift = nullptr;
+  if (src != GB2D_OK && src != GB2D_ERR_MAX_ITERS) return src;
+  // The solver writes the interior; the ghost ring keeps the caller's values.
+  launch_copy_interior(c->stream, c->xw, 1, c->tmp_a, 0, (int)ni, (int)nj);
+  std::vector<double> host(ni * nj);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(host.data(), c->tmp_a, ni * nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (normal_x) GB2D_CUDA_TRY(c, cudaMemcpyAsync(normal_x, c->jmp_nx, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (normal_y) GB2D_CUDA_TRY(c, cudaMemcpyAsync(normal_y, c->jmp_ny, np * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if ((rc = sync_check(c, "jump_poisson_solve"))) return rc;
+  // VectorToGrid (POISSON_SOLVER.cpp:1593-1603): only the unknowns take the solution.
+  for (size_t j = 0; j < nj; ++j)
+    for (size_t i = 0; i < ni; ++i) {
+      const size_t k = (i + 1) + (j + 1) * (ni + 2);
+      if (bc[k] >= 0) pressure[k] = host[i + j * ni];
+    }
+  if (st) *st = local;
+  return src;
+}
+
 int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {
   if (!c || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
   int rc = curvature_and_assemble(c, dt);
@@ -665,6 +711,7 @@ int gb2d_poisson_solve(gb2d_ctx* c, const double* rhs, double* x, const gb2d_sol
   size_t n = (size_t)ni * nj;
   GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->rhs, rhs, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->tmp_a, x, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(c->xw, 0, (size_t)(ni + 2) * (nj + 2) * sizeof(double), c->stream));
   launch_copy_interior(c->stream, c->tmp_a, 0, c->xw, 1, ni, nj);
   gb2d_solve_stats local;
   memset(&local, 0, sizeof local);

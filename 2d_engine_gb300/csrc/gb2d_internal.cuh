@@ -153,9 +153,13 @@ struct gb2d_ctx {
   double *adj_lam_u, *adj_lam_v;      // cotangents of U, V (ghost 2)
   double *adj_mu_u, *adj_mu_v;        // results for U/V (ghost 2) or UA/VA (ghost 3)
   double* adj_lam_p;                  // cotangent of p (ghost 1)
+  // General jump-Poisson inputs (allocated by the first gb2d_jump_poisson_solve)
+  double *jmp_dens, *jmp_div, *jmp_js, *jmp_jd, *jmp_nx, *jmp_ny, *jmp_phi;
+  int* jmp_bc;
   double* sign;  // reinit S (interior)
   // Assembled pressure system (FP64): faces bx ((ni+1) x nj), by (ni x (nj+1)), diag/rhs (ni x nj).
   double *bx, *by, *diag, *rhs;
+  const double* sys_shift;  // diagonal beyond the face conductances (ni x nj), or null: the projection's structure
   double *tmp_a, *tmp_b;  // compact scratch for the standalone Poisson calls
   double* xw;             // padded solution buffer for gb2d_poisson_solve
   double* ckpt[6];        // checkpoint copies of phi, u, v, ua, va, p (allocated on first save)
@@ -203,6 +207,12 @@ void launch_weno5_adjoint(cudaStream_t s, gb2d_ctx* c, double dt, double* mu_ua,
 // solve into the padded z, adj_mu_u/v = lam + D^T z.
 void launch_projection_adjoint_rhs(cudaStream_t s, gb2d_ctx* c, double dt, int with_lam_p);
 void launch_projection_adjoint_vel(cudaStream_t s, gb2d_ctx* c, double dt, const double* z);
+
+// ---- gb2d_jump.cu (FP64, compiled without FMA contraction) ----
+int jump_buffers(gb2d_ctx* c);
+// Normals of jmp_phi, then the jump system (xw holds the pressure with its boundary values)
+// into c->bx, by, diag, rhs, and its diagonal shift into c->tmp_b.
+void launch_jump_assemble(cudaStream_t s, gb2d_ctx* c);
 
 // ---- gb2d_solver.cu ----
 Solver* solver_create(int ni, int nj, char* err, size_t errlen);

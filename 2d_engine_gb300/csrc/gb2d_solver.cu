@@ -104,7 +104,8 @@ __device__ __forceinline__ double in_prec(double v, double) { return v; }
 // faces, zero on walls; diagonal as assembled; shift = pin + (dx != dy) terms.
 template <typename T>
 __global__ void k_build_level0(const double* __restrict__ bx, const double* __restrict__ by, const double* __restrict__ diag,
-                               const double* __restrict__ rhs, Level<T> L, double* __restrict__ b64, double idx2_, double idy2_) {
+                               const double* __restrict__ rhs, const double* __restrict__ shift, Level<T> L, double* __restrict__ b64,
+                               double idx2_, double idy2_) {
   int ni = L.nI, nj = L.nJ;
   const T idx2 = in_prec(idx2_, T()), idy2 = in_prec(idy2_, T()), zero = 0;
   GB_FOR_IJ(i, j, ni, nj) {
@@ -119,9 +120,13 @@ __global__ void k_build_level0(const double* __restrict__ bx, const double* __re
     const T d = in_prec(diag[t], T());
     L.dg[k] = d;
     L.idg[k] = (T)1 / d;
-    const T ybeta = (j > 0 ? bb : zero) + (j < nj - 1 ? bt : zero);
-    const T pin = (i == 0 && j == 0) ? (bl + bb) : zero;
-    L.sh[k] = pin * idx2 + ybeta * (idx2 - idy2);
+    if (shift) {  // a system that states its diagonal beyond the face conductances itself
+      L.sh[k] = in_prec(shift[t], T());
+    } else {  // the projection's: the corner pin and the dx-only diagonal's y-face excess
+      const T ybeta = (j > 0 ? bb : zero) + (j < nj - 1 ? bt : zero);
+      const T pin = (i == 0 && j == 0) ? (bl + bb) : zero;
+      L.sh[k] = pin * idx2 + ybeta * (idx2 - idy2);
+    }
     if (b64) b64[k] = rhs[t];
   }
 }
@@ -1084,7 +1089,7 @@ template <typename T>
 void build_hierarchy(cudaStream_t s, Hierarchy<T>& H, const gb2d_ctx* c, double* b64, double* ainv) {
   double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
   Level<T>& L0 = H.L[0];
-  k_build_level0<T><<<grid_ij(L0.nI, L0.nJ), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, L0, b64, idx2, idy2);
+  k_build_level0<T><<<grid_ij(L0.nI, L0.nJ), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, c->sys_shift, L0, b64, idx2, idy2);
   GB_LAUNCHED(1);
   for (int l = 1; l < H.nlev; ++l) {
     k_coarsen<T><<<grid_ij(H.L[l].nI, H.L[l].nJ), kThreads, 0, s>>>(H.L[l - 1], H.L[l]);
@@ -1098,7 +1103,8 @@ void build_hierarchy(cudaStream_t s, Hierarchy<T>& H, const gb2d_ctx* c, double*
 void build_level0_f64(cudaStream_t s, Hierarchy<double>& H, const gb2d_ctx* c, double* b64) {
   double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
   Level<double>& L0 = H.L[0];
-  k_build_level0<double><<<grid_ij(L0.nI, L0.nJ), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, L0, b64, idx2, idy2);
+  k_build_level0<double><<<grid_ij(L0.nI, L0.nJ), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, c->sys_shift, L0, b64, idx2,
+                                                                     idy2);
   GB_LAUNCHED(1);
 }
 
@@ -1474,8 +1480,8 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
   bool joined = !(prec && use_mg);
   if (prec && !use_mg) {
     double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
-    k_build_level0<float><<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, S->h32.L[0], nullptr,
-                                                                                                idx2, idy2);
+    k_build_level0<float><<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, c->sys_shift,
+                                                                                                S->h32.L[0], nullptr, idx2, idy2);
     GB_LAUNCHED(1);
   }
   int total = 0, outer = 0;

@@ -263,6 +263,20 @@ int gb2d_batch_autotune(gb2d_batch* batch, double cfl, const gb2d_solve_opts* op
  * step in, its last step out.  opts' mg_smooth is replaced per instance by the tuned value. */
 int gb2d_batch_advance(gb2d_batch* batch, int frames, double cfl, double* dts, const gb2d_solve_opts* opts, gb2d_batch_stats* stats);
 
+/* The general jump-condition Poisson problem (a15; POISSON_SOLVER::Solve with density, bc,
+ * div, levelset, jc_on_solution, jc_on_derivative, POISSON_SOLVER.cpp:127-145, and its
+ * builder :714-976, as POISSON_EQUATION_TEST uses it): on the context's grid, with the
+ * coefficient 1/density, boundary codes bc (>= 0 unknown, -1 Dirichlet, -4 Neumann),
+ * right-hand side -div, jumps [u] = jc_solution and [beta du/dn] = jc_derivative across
+ * levelset = 0 (normals from the level set as LEVELSET_2D::ComputeNormals forms them).
+ * density, bc (int), div, jc_solution, jc_derivative, pressure: P layout (ghost 1);
+ * levelset: PHI layout (ghost 2).  pressure holds the Dirichlet values and the warm start
+ * and receives the solution; normal_x / normal_y (P layout, may be NULL) receive the
+ * normals.  Uses the context's system buffers (a later gb2d_projection rebuilds them). */
+int gb2d_jump_poisson_solve(gb2d_ctx* ctx, const double* density, const int* bc, const double* div, const double* levelset,
+                            const double* jc_solution, const double* jc_derivative, double* pressure, double* normal_x,
+                            double* normal_y, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+
 /* Standalone pieces of the pressure system for parity checks and for
  * POISSON_SOLVER_2D-style use (a10, a15).  gb2d_poisson_assemble runs the
  * curvature step (which extrapolates phi's ghosts) and builds the system of the

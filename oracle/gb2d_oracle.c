@@ -947,3 +947,130 @@ double or_cfl_time_step(const or_grid* gr, const or_params* pr, const or_flow* f
   }
   return dt;
 }
+
+/* ------------------------------------------------------------------------- */
+/* General jump-condition Poisson problem: POISSON_SOLVER::Solve(pressure, density, bc,
+ * div, levelset, jc_on_solution, jc_on_derivative) (POISSON_SOLVER.cpp:127-145) with
+ * BuildLinearSystemNodeJumpConditionVaribleCoefficient (:714-976), as POISSON_EQUATION_TEST
+ * calls it (POISSON_EQUATION_TEST.h:352-396). */
+
+/* LEVELSET_2D::ComputeNormals(thread_id) (LEVELSET_2D.h:640-662): phi's ghosts refreshed by
+ * the copy fill first, then unit central-difference normals (one-sided where the central
+ * ones vanish) on the interior nodes; nx, ny have ghost 1 (left untouched there). */
+void or_normals(const or_grid* gr, double* phi_a, double* nx_a, double* ny_a) {
+  int ni = gr->ni, nj = gr->nj;
+  space_t s = base_space(gr);
+  fld phi = F(phi_a, 2, ni, nj), nx = F(nx_a, 1, ni, nj), ny = F(ny_a, 1, ni, nj);
+  or_fill_ghost_copy(phi_a, 2, phi_a, 2, ni, nj, 2);
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i < ni; ++i) {
+      double x = (AT(phi, i + 1, j) - AT(phi, i - 1, j)) * s.o2dx, y = (AT(phi, i, j + 1) - AT(phi, i, j - 1)) * s.o2dy;
+      double m = sqrt(x * x + y * y);
+      if (!(m != 0)) {
+        x = (AT(phi, i + 1, j) - AT(phi, i, j)) * s.odx;
+        y = (AT(phi, i, j + 1) - AT(phi, i, j)) * s.ody;
+      }
+      double mag = sqrt(x * x + y * y), om = 1 / mag; /* VECTOR_2D::MakeThisUnit */
+      if (mag != 0) {
+        x *= om;
+        y *= om;
+      }
+      AT(nx, i, j) = x;
+      AT(ny, i, j) = y;
+    }
+}
+
+#define OR_BC_DIR (-1)
+#define OR_BC_NEUM (-4)
+
+/* The system in the grid layout: rows of full cells (bc >= 0) as the builder writes them,
+ * rows of every other node the identity scaled by 1/dx^2 with the node's pressure as its
+ * value; faces touching a non-full node carry no coupling.  All node fields have ghost 1
+ * (phi ghost 2; normals from or_normals).  bx: (ni+1) x nj, by: ni x (nj+1). */
+int or_jump_poisson_assemble(const or_grid* gr, const double* pressure_a, const double* density_a, const int* bc_a,
+                             const double* div_a, const double* phi_a, const double* nx_a, const double* ny_a,
+                             const double* jcs_a, const double* jcd_a, double* bx, double* by, double* diag, double* rhs) {
+  if (!gr || gr->ni < 4 || gr->nj < 4) return OR_BAD_ARG;
+  int ni = gr->ni, nj = gr->nj, ld = ni + 2;
+  space_t s = base_space(gr);
+  const double inv_dxdx = 1 / (s.dx * s.dx), inv_dydy = 1 / (s.dy * s.dy);
+  fld P = F((double*)pressure_a, 1, ni, nj), D = F((double*)div_a, 1, ni, nj), phi = F((double*)phi_a, 2, ni, nj);
+  fld NX = F((double*)nx_a, 1, ni, nj), NY = F((double*)ny_a, 1, ni, nj);
+  fld JS = F((double*)jcs_a, 1, ni, nj), JD = F((double*)jcd_a, 1, ni, nj);
+  /* variable = 1/density on the interior, ghosts copied from the second interior line (:131-138) */
+  double* v_a = zalloc((size_t)(ni + 4) * (nj + 4));
+  if (!v_a) return OR_NO_MEMORY;
+  fld V = F(v_a, 2, ni, nj), Dn = F((double*)density_a, 1, ni, nj);
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i < ni; ++i) AT(V, i, j) = 1 / AT(Dn, i, j);
+  or_fill_ghost_copy(v_a, 2, v_a, 2, ni, nj, 2);
+#define BC(i, j) (bc_a[((i) + 1) + (size_t)((j) + 1) * ld])
+  for (size_t k = 0; k < (size_t)(ni + 1) * nj; ++k) bx[k] = 0;
+  for (size_t k = 0; k < (size_t)ni * (nj + 1); ++k) by[k] = 0;
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i < ni; ++i) {
+      size_t t = i + (size_t)j * ni;
+      if (BC(i, j) < 0) {
+        diag[t] = inv_dxdx;
+        rhs[t] = inv_dxdx * AT(P, i, j);
+        continue;
+      }
+      double lc = AT(phi, i, j), ll = AT(phi, i - 1, j), lr = AT(phi, i + 1, j), lb = AT(phi, i, j - 1), lt = AT(phi, i, j + 1);
+      double vc = AT(V, i, j), vl = AT(V, i - 1, j), vr = AT(V, i + 1, j), vb = AT(V, i, j - 1), vt = AT(V, i, j + 1);
+      double beta_l = vc * vl * (fabs(ll) + fabs(lc)) / (vc * fabs(ll) + vl * fabs(lc));
+      double beta_r = vc * vr * (fabs(lr) + fabs(lc)) / (vr * fabs(lc) + vc * fabs(lr));
+      double beta_b = vc * vb * (fabs(lb) + fabs(lc)) / (vc * fabs(lb) + vb * fabs(lc));
+      double beta_t = vc * vt * (fabs(lt) + fabs(lc)) / (vt * fabs(lc) + vc * fabs(lt));
+      int cl = BC(i - 1, j), cr = BC(i + 1, j), cb = BC(i, j - 1), ct = BC(i, j + 1);
+      double coef = 0;
+      if (cl > -1) coef += beta_l, bx[i + (size_t)j * (ni + 1)] = beta_l;
+      if (cr > -1) coef += beta_r, bx[i + 1 + (size_t)j * (ni + 1)] = beta_r;
+      if (cb > -1) coef += beta_b, by[i + (size_t)j * ni] = beta_b;
+      if (ct > -1) coef += beta_t, by[i + (size_t)(j + 1) * ni] = beta_t;
+      if (cl == OR_BC_DIR) coef += beta_l;
+      if (cr == OR_BC_DIR) coef += beta_r;
+      if (cb == OR_BC_DIR) coef += beta_b;
+      if (ct == OR_BC_DIR) coef += beta_t;
+      if (i == 0 && j == 0) {
+        if (cl == OR_BC_NEUM) coef += beta_l;
+        if (cr == OR_BC_NEUM) coef += beta_r;
+        if (cb == OR_BC_NEUM) coef += beta_b;
+        if (ct == OR_BC_NEUM) coef += beta_t;
+      }
+      if (coef == 0) coef = 1;
+      diag[t] = inv_dxdx * coef;
+      double jc = AT(JS, i, j), jd = AT(JD, i, j), nxc = AT(NX, i, j), nyc = AT(NY, i, j);
+#define ARM(ln, jsn, jdn, nn, nc, beta, vn, o, o2, side)                                       \
+  do {                                                                                          \
+    double sub = fabs(ln) / (fabs(lc) + fabs(ln));                                              \
+    double a = (jc * fabs(ln) + (jsn) * fabs(lc)) / (fabs(lc) + fabs(ln));                      \
+    double b = (jd * (nc) * fabs(ln) + (jdn) * (nn) * fabs(lc)) / (fabs(lc) + fabs(ln));        \
+    if ((lc <= 0 && (ln) <= 0) || (lc > 0 && (ln) > 0))                                         \
+      side = 0;                                                                                 \
+    else if (lc <= 0 && (ln) > 0)                                                               \
+      side = (o2) * a * (beta) + SGN * ((o) * (beta) * b * sub / (vn));                         \
+    else if (lc > 0 && (ln) <= 0)                                                               \
+      side = -(o2) * a * (beta) - SGN * ((o) * (beta) * b * sub / (vn));                        \
+  } while (0)
+      double FL = 0, FR = 0, FB = 0, FT = 0;
+#define SGN (-1)
+      ARM(ll, AT(JS, i - 1, j), AT(JD, i - 1, j), AT(NX, i - 1, j), nxc, beta_l, vl, s.odx, s.odx2, FL);
+      ARM(lb, AT(JS, i, j - 1), AT(JD, i, j - 1), AT(NY, i, j - 1), nyc, beta_b, vb, s.ody, s.ody2, FB);
+#undef SGN
+#define SGN (+1)
+      ARM(lr, AT(JS, i + 1, j), AT(JD, i + 1, j), AT(NX, i + 1, j), nxc, beta_r, vr, s.odx, s.odx2, FR);
+      ARM(lt, AT(JS, i, j + 1), AT(JD, i, j + 1), AT(NY, i, j + 1), nyc, beta_t, vt, s.ody, s.ody2, FT);
+#undef SGN
+#undef ARM
+      double FX = FL + FR, FY = FB + FT;
+      double r = -AT(D, i, j) - FX - FY;
+      if (cl == OR_BC_DIR) r += beta_l * inv_dxdx * AT(P, i - 1, j);
+      if (cr == OR_BC_DIR) r += beta_r * inv_dxdx * AT(P, i + 1, j);
+      if (cb == OR_BC_DIR) r += beta_b * inv_dydy * AT(P, i, j - 1);
+      if (ct == OR_BC_DIR) r += beta_t * inv_dydy * AT(P, i, j + 1);
+      rhs[t] = r;
+    }
+#undef BC
+  free(v_a);
+  return OR_OK;
+}

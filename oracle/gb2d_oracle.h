@@ -102,6 +102,17 @@ int or_time_step(const or_grid* gr, const or_params* pr, const or_flow* fl, doub
 double or_cfl_time_step(const or_grid* gr, const or_params* pr, const or_flow* fl, const double* u, const double* v,
                         const double* kappa, double cfl_number, double rates[4]);
 
+/* General jump-condition Poisson problem (POISSON_SOLVER::Solve with density, bc, div,
+ * levelset, jc_on_solution, jc_on_derivative; POISSON_SOLVER.cpp:127-145, 714-976).
+ * or_normals: LEVELSET_2D::ComputeNormals(thread_id) (copy-fills phi's ghosts, writes unit
+ * normals nx, ny on the nodes; ghost 1).  or_jump_poisson_assemble: the system in the grid
+ * layout, full cells (bc >= 0) as the builder writes them, every other node an identity
+ * row scaled by 1/dx^2 holding its pressure; bc codes: >= 0 full, -1 Dirichlet, -4 Neumann. */
+void or_normals(const or_grid* gr, double* phi, double* nx, double* ny);
+int or_jump_poisson_assemble(const or_grid* gr, const double* pressure, const double* density, const int* bc, const double* div,
+                             const double* phi, const double* nx, const double* ny, const double* jc_solution,
+                             const double* jc_derivative, double* bx, double* by, double* diag, double* rhs);
+
 /* a10 in matrix-free form.  bx: x-faces (ni+1) x nj (face i between nodes i-1 and i),
  * by: y-faces ni x (nj+1), diag, rhs: ni x nj.  phi must already hold the ghost
  * state of the projection (or_curvature fills it).  kappa: ni x nj. */

@@ -70,6 +70,9 @@ def lib():
         L.or_fill_ghost_extrapolate.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         W = ctypes.POINTER(Flow)
         L.or_cfl_time_step.argtypes = [G, R, W, P, P, P, d, P]
+        L.or_normals.argtypes = [G, P, P, P]
+        L.or_jump_poisson_assemble.argtypes = [G, P, P, P, P, P, P, P, P, P, P, P, P, P]
+        L.or_jump_poisson_assemble.restype = ctypes.c_int
         L.or_cfl_time_step.restype = d
         L.or_apply_gravity.argtypes = [G, W, P, P, d]
         L.or_sourcing.argtypes = [G, R, W, P, P, P, P, d]
@@ -192,3 +195,20 @@ def cfl_time_step(g, pr, fl, u, v, kappa, cfl_number=0.5):
     dt = lib().or_cfl_time_step(ctypes.byref(g), ctypes.byref(pr), ctypes.byref(fl), _p(u), _p(v), _p(kappa), cfl_number,
                                 _p(rates))
     return dt, tuple(rates)
+
+
+def normals(g, phi):
+    """ComputeNormals: fills phi's ghosts (copy) and returns (nx, ny) with ghost 1."""
+    nx, ny = np.zeros((g.nj + 2, g.ni + 2)), np.zeros((g.nj + 2, g.ni + 2))
+    lib().or_normals(ctypes.byref(g), _p(phi), _p(nx), _p(ny))
+    return nx, ny
+
+
+def jump_poisson_assemble(g, pressure, density, bc, div, phi, nx, ny, jc_solution, jc_derivative):
+    ni, nj = g.ni, g.nj
+    bc = np.ascontiguousarray(bc, dtype=np.int32)
+    bx = np.zeros((nj, ni + 1)); by = np.zeros((nj + 1, ni)); dg = np.zeros((nj, ni)); rhs = np.zeros((nj, ni))
+    _check(lib().or_jump_poisson_assemble(ctypes.byref(g), _p(pressure), _p(density), bc.ctypes.data, _p(div), _p(phi), _p(nx),
+                                          _p(ny), _p(jc_solution), _p(jc_derivative), _p(bx), _p(by), _p(dg), _p(rhs)),
+           "jump_poisson_assemble")
+    return bx, by, dg, rhs

@@ -26,6 +26,7 @@
 #include <string>
 
 #include "EULERIAN_FLUID_SOLVER_2D.h"
+#include "POISSON_EQUATION_TEST.h"
 
 /* ---- SCRIPT_BLOCK accessors (declared in SCRIPT_READER.h:112-160) ----------
  * The reference implements these with a regex parser (SCRIPT_READER.cpp); the
@@ -258,6 +259,114 @@ void ref_velocity_bc(void* h) { static_cast<RefSim*>(h)->solver.SetupBoundaryCon
 void ref_solve_for_rk(void* h, double dt) { static_cast<RefSim*>(h)->solver.SolveForRK(dt, 0); }
 void ref_step(void* h, double dt) { static_cast<RefSim*>(h)->solver.AdvanceOneTimeStepThread(dt, 0); }
 double ref_cfl_dt(void* h) { return static_cast<RefSim*>(h)->solver.CFLOneTimeStep(); }
+
+/* ---- POISSON_EQUATION_TEST (POISSON_EQUATION_TEST.h) -------------------------
+ * The jump-condition Poisson tests 3 and 5 on [-1,1]^2 with n x n nodes, Dirichlet
+ * boundaries and PCG, set up as SIMULATION_WORLD does for
+ * poisson_equation_with_jump_condition (SIMULATION_WORLD.h:379-384 and the interface
+ * level sets at :913-943), then solved by POISSON_EQUATION_TEST::Solve (:288-311). */
+struct RefPoisson {
+  MULTITHREADING mt;
+  WORLD_DISCRETIZATION_2D world;
+  POISSON_EQUATION_TEST test;
+};
+
+void* ref_poisson_create(int test_number, int n, double tolerance, int max_iteration) {
+  std::cout.rdbuf(&g_null);
+  if (test_number != 3 && test_number != 5) return 0;
+  RefPoisson* r = new RefPoisson;
+  r->mt.Initialize(1);
+  r->world.poisson_equation_with_jump_condition_test = true;
+  r->world.grid_1d = false;
+  r->world.grid_2d = true;
+  r->world.world_grid.Initialize(n, n, 0, 0, -1, -1, 1, 1);
+  r->test.world_discretization = &r->world;
+  r->test.test_number = test_number;
+  r->test.grid_1d = false;
+  r->test.grid_2d = true;
+  SCRIPT_BLOCK b;
+  put(b, "tolerance", num(tolerance));
+  put(b, "max_iteration", num(max_iteration));
+  put(b, "poisson_solver_type", "PCG");
+  put(b, "Dirichlet_Boundary_Condition", "true");
+  put(b, "Neumann_Boundary_Condition", "false");
+  r->test.InitializeFromBlock(b, &r->mt);
+  LEVELSET_2D& ls = *r->test.interface_levelset_2d;
+  GRID_STRUCTURE_2D& g = ls.grid;
+  for (int j = g.j_start; j <= g.j_end; ++j)
+    for (int i = g.i_start; i <= g.i_end; ++i) {
+      T x = g.x_min + i * g.dx, y = g.y_min + j * g.dy;
+      if (test_number == 3)
+        ls(i, j) = sqrt(POW2(x - (T)0.5) + POW2(y - (T)0.5)) - (T)0.25;
+      else
+        ls(i, j) = sqrt(POW2(x) + POW2(y)) - (T)0.5;
+    }
+  ls.FillGhostCellsFromThreaded(&(ls.phi), false);
+  return r;
+}
+
+void ref_poisson_destroy(void* h) { delete static_cast<RefPoisson*>(h); }
+
+double ref_poisson_solve(void* h) {
+  RefPoisson* r = static_cast<RefPoisson*>(h);
+  r->test.Solve(0);
+  return r->test.l2_norm;
+}
+
+/* Fields after ref_poisson_solve, ghost-inclusive: 0 solution (ghost 1), 1 true solution,
+ * 2 beta, 3 rhs, 4 jc_on_solution, 5 jc_on_derivative, 6 boundary condition (as double),
+ * 7 interface level set (ghost 2), 8 / 9 normal x / y (ghost 1). */
+int ref_poisson_field(void* h, int id, int* i_res, int* j_res, double* out) {
+  RefPoisson* r = static_cast<RefPoisson*>(h);
+  POISSON_EQUATION_TEST& t = r->test;
+  const ARRAY_2D<T>* a = 0;
+  switch (id) {
+    case 0: a = &t.solution_2d.array_for_this; break;
+    case 1: a = &t.true_solution_2d.array_for_this; break;
+    case 2: a = &t.beta_2d.array_for_this; break;
+    case 3: a = &t.rhs_2d.array_for_this; break;
+    case 4: a = &t.jc_on_solution_2d.array_for_this; break;
+    case 5: a = &t.jc_on_derivative_2d.array_for_this; break;
+    case 7: a = &t.interface_levelset_2d->signed_distance_field.array_for_this; break;
+    default: break;
+  }
+  if (a) {
+    *i_res = a->i_res;
+    *j_res = a->j_res;
+    if (out)
+      for (int k = 0; k < a->ij_res; ++k) out[k] = a->values[k];
+    return 0;
+  }
+  if (id == 6) {
+    const ARRAY_2D<int>& bc = t.boundary_condition_2d.array_for_this;
+    *i_res = bc.i_res;
+    *j_res = bc.j_res;
+    if (out)
+      for (int k = 0; k < bc.ij_res; ++k) out[k] = bc.values[k];
+    return 0;
+  }
+  if (id == 8 || id == 9) {
+    const ARRAY_2D<VT>& nv = t.interface_levelset_2d->normal.array_for_this;
+    *i_res = nv.i_res;
+    *j_res = nv.j_res;
+    if (out)
+      for (int k = 0; k < nv.ij_res; ++k) out[k] = id == 8 ? nv.values[k].x : nv.values[k].y;
+    return 0;
+  }
+  return -1;
+}
+
+int ref_poisson_test_system(void* h, int* n, int* nnz, int* row_ptr, int* col, double* val, double* b, int* iterations) {
+  POISSON_SOLVER& ps = static_cast<RefPoisson*>(h)->test.poisson_solver;
+  *n = ps.A.N;
+  *nnz = ps.A.nz;
+  if (row_ptr) for (int k = 0; k <= ps.A.N; ++k) row_ptr[k] = ps.A.row_ptr[k];
+  if (col) for (int k = 0; k < ps.A.nz; ++k) col[k] = ps.A.column_index[k];
+  if (val) for (int k = 0; k < ps.A.nz; ++k) val[k] = ps.A.values[k];
+  if (b) for (int k = 0; k < ps.b.num_dimension; ++k) b[k] = ps.b[k];
+  if (iterations) *iterations = ps.linear_solver->num_iteration;
+  return 0;
+}
 
 /* Linear system of the most recent projection (POISSON_SOLVER.cpp:714-976):
  * call with null arrays to get n and nnz, then again to copy. */

@@ -123,3 +123,50 @@ class RefSim:
         self.L.ref_poisson_system(self.h, ctypes.byref(n), ctypes.byref(nnz), rp.ctypes.data, col.ctypes.data,
                                   val.ctypes.data, b.ctypes.data, x.ctypes.data)
         return rp, col, val, b, x
+
+
+class RefPoissonTest:
+    """POISSON_EQUATION_TEST of the reference (tests 3 and 5: jump-condition Poisson on
+    [-1,1]^2 with n x n nodes, Dirichlet boundaries, PCG)."""
+
+    FIELDS = dict(solution=0, true_solution=1, beta=2, rhs=3, jc_on_solution=4, jc_on_derivative=5, bc=6, levelset=7,
+                  normal_x=8, normal_y=9)
+
+    def __init__(self, test_number, n, tolerance=1e-13, max_iteration=200000):
+        L = ctypes.CDLL(LIB_PATH)
+        vp, d, i = ctypes.c_void_p, ctypes.c_double, ctypes.c_int
+        L.ref_poisson_create.restype = vp
+        L.ref_poisson_create.argtypes = [i, i, d, i]
+        L.ref_poisson_destroy.argtypes = [vp]
+        L.ref_poisson_solve.restype = d
+        L.ref_poisson_solve.argtypes = [vp]
+        L.ref_poisson_field.argtypes = [vp, i, ctypes.POINTER(i), ctypes.POINTER(i), vp]
+        L.ref_poisson_test_system.argtypes = [vp, ctypes.POINTER(i), ctypes.POINTER(i), vp, vp, vp, vp, ctypes.POINTER(i)]
+        self.L = L
+        self.h = L.ref_poisson_create(test_number, n, tolerance, max_iteration)
+        if not self.h:
+            raise ValueError("test number must be 3 or 5")
+
+    def solve(self):
+        return self.L.ref_poisson_solve(self.h)
+
+    def get(self, name):
+        ir, jr = ctypes.c_int(), ctypes.c_int()
+        self.L.ref_poisson_field(self.h, self.FIELDS[name], ctypes.byref(ir), ctypes.byref(jr), None)
+        a = np.zeros((jr.value, ir.value))
+        self.L.ref_poisson_field(self.h, self.FIELDS[name], ctypes.byref(ir), ctypes.byref(jr), a.ctypes.data)
+        return a
+
+    def system(self):
+        n, nnz, it = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self.L.ref_poisson_test_system(self.h, ctypes.byref(n), ctypes.byref(nnz), None, None, None, None, ctypes.byref(it))
+        rp = np.zeros(n.value + 1, dtype=np.int32); col = np.zeros(nnz.value, dtype=np.int32)
+        val = np.zeros(nnz.value); b = np.zeros(n.value)
+        self.L.ref_poisson_test_system(self.h, ctypes.byref(n), ctypes.byref(nnz), rp.ctypes.data, col.ctypes.data,
+                                       val.ctypes.data, b.ctypes.data, ctypes.byref(it))
+        return rp, col, val, b, it.value
+
+    def close(self):
+        if self.h:
+            self.L.ref_poisson_destroy(self.h)
+            self.h = None

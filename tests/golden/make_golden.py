@@ -21,7 +21,8 @@ tests/golden/cases.py and stores inputs and outputs:
                       reference's air/water setup) and with it configured
   cfl                 CFLOneTimeStep after ComputeCurvaturesThread
 and, in rising_bubble_128_frames.npz, 100 frames of the 128^2 rising bubble
-(SIMULATION_WORLD::AdvanceOneFrame: curvature, CFL time step, time step).
+(SIMULATION_WORLD::AdvanceOneFrame: curvature, CFL time step, time step); in
+poisson_test{3,5}_61.npz, POISSON_EQUATION_TEST's jump-condition problems 3 and 5.
 
 Usage:  python tests/golden/make_golden.py   (needs the reference sources)
 """
@@ -186,6 +187,25 @@ def make_rising_bubble_run(name, n=128, steps=100, keep=(10,)):
     print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB, dt {dts[0]:.3e} .. {dts[-1]:.3e}")
 
 
+def make_poisson_test(name, test_number, n):
+    """POISSON_EQUATION_TEST of the reference (test 3: circle of radius 0.25 at (0.5, 0.5),
+    beta 0.5 / 1, both jumps; test 5: circle of radius 0.5, flux jump 2) on [-1,1]^2 with
+    n x n nodes and Dirichlet boundaries: inputs as the solver sees them, its system (b,
+    A x for a seeded x), the solution and, for test 3, its L2 error against the exact one."""
+    p = R.RefPoissonTest(test_number, n)
+    l2 = p.solve()
+    out = {k: p.get(k) for k in R.RefPoissonTest.FIELDS}
+    rp, col, val, b, its = p.system()
+    x = np.random.default_rng(777).standard_normal(len(b))
+    out.update(n=n, test_number=test_number, l2_norm=l2, iterations=its, sys_b=b, sys_x=x, sys_ax=csr_apply(rp, col, val, x))
+    # the solver's input pressure: Dirichlet values on the non-unknown nodes, zero elsewhere
+    out["pressure_in"] = np.where(out["bc"] >= 0, 0.0, out["solution"])
+    p.close()
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez_compressed(path, **out)
+    print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB, CG {its} iterations, L2 error {l2:.3e}")
+
+
 def main():
     if not R.available():
         sys.exit("oracle/_ref/libref2d.so missing: run `make -C oracle/ref` where the reference sources are present")
@@ -195,6 +215,8 @@ def main():
     make_case("tall_24x40", bubbles_case(24, 40, seed=4, x_max=1.0, y_max=2.0), 0.02, 1e-13)
     make_case("bubbles_65", bubbles_case(65, seed=5), 0.5 / 64, 1e-12, flow=False)
     make_rising_bubble_run("rising_bubble_128_frames")
+    make_poisson_test("poisson_test3_61", 3, 61)
+    make_poisson_test("poisson_test5_61", 5, 61)
 
 
 if __name__ == "__main__":

@@ -174,3 +174,30 @@ def test_rising_bubble_frames(oracle):
         oracle.time_step(gr, pr, fl, phi, u, v, ua, va, p, k, None, dt)
     for got, key in ((phi, "phi10"), (u, "u10"), (v, "v10"), (p, "p10")):
         np.testing.assert_array_equal(got, g[key])
+
+
+@pytest.mark.parametrize("name", ["poisson_test3_61", "poisson_test5_61"])
+def test_jump_poisson_system(oracle, name):
+    """POISSON_EQUATION_TEST's jump problems: the oracle's normals, right-hand side and
+    operator equal the reference's system bit for bit; its IC(0)-PCG solution agrees with
+    the reference's (which runs plain CG: the test's missing coarsest-level solver key
+    resets its solver type, POISSON_EQUATION_TEST.h:127-140) to the solve tolerance."""
+    g = load_golden(name)
+    n = int(g["n"])
+    gr = oracle.grid(n, n, -1.0, -1.0, 1.0, 1.0)
+    phi = g["levelset"].copy()
+    nx, ny = oracle.normals(gr, phi)
+    np.testing.assert_array_equal(nx[1:-1, 1:-1], g["normal_x"][1:-1, 1:-1])
+    np.testing.assert_array_equal(ny[1:-1, 1:-1], g["normal_y"][1:-1, 1:-1])
+    bc = np.where(g["bc"] >= 0, 0, g["bc"]).astype(np.int32)
+    bx, by, dg, rhs = oracle.jump_poisson_assemble(gr, g["pressure_in"], g["beta"], bc, g["rhs"], phi, nx, ny,
+                                                   g["jc_on_solution"], g["jc_on_derivative"])
+    full = g["bc"][1:-1, 1:-1] >= 0
+    np.testing.assert_array_equal(rhs[full], g["sys_b"])
+    xg = np.zeros((n, n))
+    xg[full] = g["sys_x"]
+    np.testing.assert_array_equal(oracle.poisson_apply(gr, bx, by, dg, xg)[full], g["sys_ax"])
+    x = g["pressure_in"][1:-1, 1:-1].copy()
+    oracle.pcg_ic0(gr, oracle.params(pcg_tolerance=1e-13, pcg_max_iterations=100000), bx, by, dg, rhs, x)
+    want = g["solution"][1:-1, 1:-1]
+    assert np.linalg.norm(x - want) <= 1e-10 * np.linalg.norm(want)
