@@ -89,6 +89,7 @@ def library():
         "gb2d_levelset_advection": [vp, d],
         "gb2d_reinitialization": [vp],
         "gb2d_levelset_rk3": [vp, d],
+        "gb2d_fast_sweeping": [vp, i],
         "gb2d_velocity_advection": [vp, d],
         "gb2d_curvature": [vp],
         "gb2d_projection": [vp, d, O, S],
@@ -248,6 +249,10 @@ class Context:
 
     def reinitialization(self):
         self._check(self.L.gb2d_reinitialization(self.h))
+
+    def fast_sweeping(self, sweeps=4):
+        """LEVELSET_2D::FastSweepingMethodOriginal(sweeps)."""
+        self._check(self.L.gb2d_fast_sweeping(self.h, sweeps))
 
     def levelset_rk3(self, dt):
         self._check(self.L.gb2d_levelset_rk3(self.h, dt))

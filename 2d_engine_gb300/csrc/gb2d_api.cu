@@ -412,6 +412,12 @@ int gb2d_reinitialization(gb2d_ctx* c) {
   return check_launch(c, "reinitialization");
 }
 
+int gb2d_fast_sweeping(gb2d_ctx* c, int sweeps) {
+  if (!c || sweeps < 0) return GB2D_ERR_ARG;
+  launch_fast_sweeping(c->stream, c, sweeps);
+  return check_launch(c, "fast_sweeping");
+}
+
 int gb2d_levelset_rk3(gb2d_ctx* c, double dt) {
   if (!c || !std::isfinite(dt)) return GB2D_ERR_ARG;
   cudaStream_t s = c->stream;

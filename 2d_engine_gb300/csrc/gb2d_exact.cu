@@ -455,6 +455,67 @@ __global__ void k_copy_interior(const double* __restrict__ src_a, int gs, double
   }
 }
 
+// FastSweepingMethodOriginal (LEVELSET_2D.h:281-384): the fixed band |phi| < 2 dx.
+__global__ void k_fsm_fixed(const double* __restrict__ phi_a, double* __restrict__ fixed, int ni, int nj, double nb) {
+  const DField phi = dfield((double*)phi_a, 2, ni, nj);
+  GB_FOR_IJ(i, j, ni, nj) { fixed[(size_t)j * ni + i] = fabs(GB_AT(phi, i, j)) < nb ? 1.0 : 0.0; }
+}
+
+// The single-threaded FillGhostCellsContinuousDerivativesFrom (FIELD_STRUCTURE_2D.h:584-639):
+// each side innermost layer first.  Thread k extrapolates row k's left and right ghosts and
+// column k's top and bottom ghosts (disjoint ghost cells, interior reads only).
+__global__ void k_extrapolate_inner_first(double* a, int g, int nI, int nJ) {
+  const DField f = dfield(a, g, nI, nJ);
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < (nI > nJ ? nI : nJ); k += gridDim.x * blockDim.x) {
+    if (k < nJ) {
+      for (int i = -1; i >= -g; --i) GB_AT(f, i, k) = 2.0 * GB_AT(f, i + 1, k) - GB_AT(f, i + 2, k);
+      for (int i = nI; i <= nI - 1 + g; ++i) GB_AT(f, i, k) = 2.0 * GB_AT(f, i - 1, k) - GB_AT(f, i - 2, k);
+    }
+    if (k < nI) {
+      for (int j = nJ; j <= nJ - 1 + g; ++j) GB_AT(f, k, j) = 2.0 * GB_AT(f, k, j - 1) - GB_AT(f, k, j - 2);
+      for (int j = -1; j >= -g; --j) GB_AT(f, k, j) = 2.0 * GB_AT(f, k, j + 1) - GB_AT(f, k, j + 2);
+    }
+  }
+}
+
+// One Gauss-Seidel sweep of LEVELSET_2D::Sweep (LEVELSET_2D.h:507-589) in direction dir
+// (0: i+ j+, 1: i- j+, 2: i- j-, 3: i+ j-).  The reference visits rows in order and
+// nodes within a row in order; a node reads its two predecessors along i and j (already
+// updated) and its two successors (not yet).  Anti-diagonal wavefronts in sweep
+// coordinates have the same dependencies, so one block walks them in turn, one barrier
+// per wavefront, and produces the reference's values bit for bit.
+__global__ void k_fsm_sweep(double* phi_a, const double* __restrict__ fixed, int ni, int nj, double h, int dir) {
+  const DField phi = dfield(phi_a, 2, ni, nj);
+  const double one_over_two = 1.0 / 2.0, hh = h * h, hh2 = hh * 2.0;
+  const bool irev = dir == 1 || dir == 2, jrev = dir == 2 || dir == 3;
+  for (int d = 0; d <= ni + nj - 2; ++d) {
+    const int lo = d - (nj - 1) > 0 ? d - (nj - 1) : 0, hi = d < ni - 1 ? d : ni - 1;
+    for (int a = lo + (int)threadIdx.x; a <= hi; a += blockDim.x) {
+      const int i = irev ? ni - 1 - a : a, jj = d - a, j = jrev ? nj - 1 - jj : jj;
+      if (fixed[(size_t)j * ni + i] != 0.0) continue;
+      double* pc = &GB_AT(phi, i, j);
+      const double c = *pc, l = GB_AT(phi, i - 1, j), r = GB_AT(phi, i + 1, j), dn = GB_AT(phi, i, j - 1), up = GB_AT(phi, i, j + 1);
+      double av, bv, a1, a2, update;
+      if (c > 0) {
+        av = l > r ? r : l;
+        bv = dn > up ? up : dn;
+        if (av <= bv) a1 = av, a2 = bv;
+        else a1 = bv, a2 = av;
+        update = fabs(a1 - a2) >= h ? a1 + h : one_over_two * (a1 + a2 + sqrt(hh2 - (a1 - a2) * (a1 - a2)));
+        *pc = update > c ? c : update;
+      } else if (c <= 0) {
+        av = l > r ? l : r;
+        bv = dn > up ? dn : up;
+        if (av <= bv) a1 = av, a2 = bv;
+        else a1 = bv, a2 = av;
+        update = fabs(a1 - a2) >= h ? a2 - h : one_over_two * (a2 + a1 - sqrt(hh2 - (a2 - a1) * (a2 - a1)));
+        *pc = update > c ? update : c;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 inline dim3 grid2d(int W, int H, dim3 blk) { return dim3((W + blk.x - 1) / blk.x, (H + blk.y - 1) / blk.y); }
 
 LSArgs ls_args(const gb2d_ctx* c) {
@@ -614,6 +675,16 @@ void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi
   AsmArgs a = asm_args(c, dt);
   k_velocity_update<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, c->p, c->kappa, c->u, c->v, a, dt, sc);
   GB_LAUNCHED(1);
+}
+
+void launch_fast_sweeping(cudaStream_t s, gb2d_ctx* c, int sweeps) {
+  const int ni = c->grid.ni, nj = c->grid.nj, n = ni > nj ? ni : nj;
+  double* phi = c->phi_buf[c->phi_cur];
+  k_fsm_fixed<<<grid_ij(ni, nj), kThreads, 0, s>>>(phi, c->tmp_a, ni, nj, 2.0 * c->base.dx);
+  k_extrapolate_inner_first<<<(n + 127) / 128, 128, 0, s>>>(phi, 2, ni, nj);
+  for (int k = 0; k < sweeps; ++k) k_fsm_sweep<<<1, 1024, 0, s>>>(phi, c->tmp_a, ni, nj, c->base.dx, k % 4);
+  k_extrapolate_inner_first<<<(n + 127) / 128, 128, 0, s>>>(phi, 2, ni, nj);
+  GB_LAUNCHED(3 + sweeps);
 }
 
 void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst, int gd, int nI, int nJ) {

@@ -187,6 +187,8 @@ void launch_rhs_diag(cudaStream_t s, const gb2d_ctx* c, const double* phi, doubl
 void launch_poisson_apply_exact(cudaStream_t s, const gb2d_ctx* c, const double* x, double* y);
 void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt, Scalars* sc);
 void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst, int gd, int nI, int nJ);
+// FastSweepingMethodOriginal on the current level set (c->tmp_a holds the fixed band).
+void launch_fast_sweeping(cudaStream_t s, gb2d_ctx* c, int sweeps);
 
 // ---- gb2d_flow.cu (FP64, compiled without FMA contraction) ----
 // Gravity (grav), viscosity (visc) and wall conditions (bc) over the face grids, and

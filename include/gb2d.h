@@ -171,6 +171,12 @@ int gb2d_checkpoint_restore(gb2d_ctx* ctx);
 int gb2d_levelset_advection(gb2d_ctx* ctx, double dt);
 /* One Reinitialization: S = phi/sqrt(phi^2+dx^2), reinit_iterations WENO5-Godunov sweeps (a2, a6). */
 int gb2d_reinitialization(gb2d_ctx* ctx);
+/* LEVELSET_2D::FastSweepingMethodOriginal(sweeps) (LEVELSET_2D.h:281-384), the
+ * reinitialisation of scripts with fastsweeping_reinitialization (EULERIAN_FLUID_SOLVER_2D.h:2404-2408,
+ * called there with 4): nodes with |phi| < 2 dx stay fixed, the others take sweeps
+ * Gauss-Seidel sweeps of Zhao's upwind distance update (directions ++, -+, --, +- in turn),
+ * with phi's ghosts extrapolated before and after. */
+int gb2d_fast_sweeping(gb2d_ctx* ctx, int sweeps);
 /* Level-set TVD-RK3 followed by reinit TVD-RK3, as one step of the reference (a4). */
 int gb2d_levelset_rk3(gb2d_ctx* ctx, double dt);
 /* One Velocity_Advection: refresh UA/VA from U/V, ENO3 on both MAC components (a3). */

@@ -1074,3 +1074,75 @@ int or_jump_poisson_assemble(const or_grid* gr, const double* pressure_a, const 
   free(v_a);
   return OR_OK;
 }
+
+/* ------------------------------------------------------------------------- */
+/* LEVELSET_2D::FastSweepingMethodOriginal(sweep_number) (LEVELSET_2D.h:281-384) with
+ * Sweep (:507-589): nodes with |phi| < 2 dx stay fixed; phi's ghosts are extrapolated,
+ * then sweep_number Gauss-Seidel sweeps (directions ++, -+, --, +- in turn) of Zhao's
+ * upwind update, then the ghosts are extrapolated again (the single-threaded fill). */
+static void fsm_sweep(fld* phi, const unsigned char* fixed, int ni, int nj, double h, int dir) {
+  const double one_over_two = 1.0 / 2.0, hh = h * h, hh2 = hh * 2.0;
+  const int ip = (dir == 1 || dir == 2) ? -1 : 1, jp = (dir == 2 || dir == 3) ? -1 : 1;
+  for (int jj = 0; jj < nj; ++jj) {
+    const int j = jp > 0 ? jj : nj - 1 - jj;
+    for (int ii = 0; ii < ni; ++ii) {
+      const int i = ip > 0 ? ii : ni - 1 - ii;
+      if (fixed[i + (size_t)j * ni]) continue;
+      double* pc = &AT(*phi, i, j);
+      double a, b, a1, a2, update;
+      double l = AT(*phi, i - 1, j), r = AT(*phi, i + 1, j), d = AT(*phi, i, j - 1), u = AT(*phi, i, j + 1);
+      if (*pc > 0) {
+        a = l > r ? r : l;
+        b = d > u ? u : d;
+        if (a <= b) a1 = a, a2 = b;
+        else a1 = b, a2 = a;
+        if (fabs(a1 - a2) >= h)
+          update = a1 + h;
+        else
+          update = one_over_two * (a1 + a2 + sqrt(hh2 - (a1 - a2) * (a1 - a2)));
+        *pc = update > *pc ? *pc : update;
+      } else if (*pc <= 0) {
+        a = l > r ? l : r;
+        b = d > u ? d : u;
+        if (a <= b) a1 = a, a2 = b;
+        else a1 = b, a2 = a;
+        if (fabs(a1 - a2) >= h)
+          update = a2 - h;
+        else
+          update = one_over_two * (a2 + a1 - sqrt(hh2 - (a2 - a1) * (a2 - a1)));
+        *pc = update > *pc ? update : *pc;
+      }
+    }
+  }
+}
+
+/* The single-threaded FillGhostCellsContinuousDerivativesFrom (FIELD_STRUCTURE_2D.h:584-639):
+ * every side innermost layer first, so outer layers read the freshly extrapolated inner one. */
+static void extrapolate_inner_first(double* a, int g, int nI, int nJ) {
+  fld f = F(a, g, nI, nJ);
+  for (int j = 0; j < nJ; ++j)
+    for (int i = -1; i >= -g; --i) AT(f, i, j) = 2.0 * AT(f, i + 1, j) - AT(f, i + 2, j);
+  for (int j = 0; j < nJ; ++j)
+    for (int i = nI; i <= nI - 1 + g; ++i) AT(f, i, j) = 2.0 * AT(f, i - 1, j) - AT(f, i - 2, j);
+  for (int i = 0; i < nI; ++i)
+    for (int j = nJ; j <= nJ - 1 + g; ++j) AT(f, i, j) = 2.0 * AT(f, i, j - 1) - AT(f, i, j - 2);
+  for (int i = 0; i < nI; ++i)
+    for (int j = -1; j >= -g; --j) AT(f, i, j) = 2.0 * AT(f, i, j + 1) - AT(f, i, j + 2);
+}
+
+int or_fast_sweeping(const or_grid* gr, double* phi_a, int sweeps) {
+  if (!gr || !phi_a || sweeps < 0) return OR_BAD_ARG;
+  int ni = gr->ni, nj = gr->nj;
+  space_t s = base_space(gr);
+  fld phi = F(phi_a, 2, ni, nj);
+  unsigned char* fixed = (unsigned char*)calloc((size_t)ni * nj, 1);
+  if (!fixed) return OR_NO_MEMORY;
+  const double nb = 2.0 * s.dx;
+  for (int j = 0; j < nj; ++j)
+    for (int i = 0; i < ni; ++i) fixed[i + (size_t)j * ni] = fabs(AT(phi, i, j)) < nb;
+  extrapolate_inner_first(phi_a, 2, ni, nj);
+  for (int k = 0; k < sweeps; ++k) fsm_sweep(&phi, fixed, ni, nj, s.dx, k % 4);
+  extrapolate_inner_first(phi_a, 2, ni, nj);
+  free(fixed);
+  return OR_OK;
+}

@@ -113,6 +113,9 @@ int or_jump_poisson_assemble(const or_grid* gr, const double* pressure, const do
                              const double* phi, const double* nx, const double* ny, const double* jc_solution,
                              const double* jc_derivative, double* bx, double* by, double* diag, double* rhs);
 
+/* LEVELSET_2D::FastSweepingMethodOriginal(sweeps) (LEVELSET_2D.h:281-384, 507-589). */
+int or_fast_sweeping(const or_grid* gr, double* phi, int sweeps);
+
 /* a10 in matrix-free form.  bx: x-faces (ni+1) x nj (face i between nodes i-1 and i),
  * by: y-faces ni x (nj+1), diag, rhs: ni x nj.  phi must already hold the ghost
  * state of the projection (or_curvature fills it).  kappa: ni x nj. */

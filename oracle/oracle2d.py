@@ -71,6 +71,8 @@ def lib():
         W = ctypes.POINTER(Flow)
         L.or_cfl_time_step.argtypes = [G, R, W, P, P, P, d, P]
         L.or_normals.argtypes = [G, P, P, P]
+        L.or_fast_sweeping.argtypes = [G, P, ctypes.c_int]
+        L.or_fast_sweeping.restype = ctypes.c_int
         L.or_jump_poisson_assemble.argtypes = [G, P, P, P, P, P, P, P, P, P, P, P, P, P]
         L.or_jump_poisson_assemble.restype = ctypes.c_int
         L.or_cfl_time_step.restype = d
@@ -212,3 +214,7 @@ def jump_poisson_assemble(g, pressure, density, bc, div, phi, nx, ny, jc_solutio
                                           _p(ny), _p(jc_solution), _p(jc_derivative), _p(bx), _p(by), _p(dg), _p(rhs)),
            "jump_poisson_assemble")
     return bx, by, dg, rhs
+
+
+def fast_sweeping(g, phi, sweeps=4):
+    _check(lib().or_fast_sweeping(ctypes.byref(g), _p(phi), sweeps), "fast_sweeping")

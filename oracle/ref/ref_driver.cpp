@@ -253,6 +253,7 @@ void ref_reinitialization(void* h, double dt) { static_cast<RefSim*>(h)->solver.
 void ref_velocity_advection(void* h, double dt) { static_cast<RefSim*>(h)->solver.Velocity_Advection(dt, 0); }
 void ref_projection(void* h, double dt) { static_cast<RefSim*>(h)->solver.Projection(dt, 0); }
 void ref_curvature(void* h) { static_cast<RefSim*>(h)->solver.water_levelset->ComputeCurvaturesThread(0); }
+void ref_fast_sweeping(void* h, int sweeps) { static_cast<RefSim*>(h)->solver.water_levelset->FastSweepingMethodOriginal(sweeps); }
 void ref_apply_gravity(void* h, double dt) { static_cast<RefSim*>(h)->solver.ApplyGraivity(dt, 0); }
 void ref_sourcing(void* h, double dt) { static_cast<RefSim*>(h)->solver.Sourcing(dt, 0); }
 void ref_velocity_bc(void* h) { static_cast<RefSim*>(h)->solver.SetupBoundaryConditionForVelocity(); }

@@ -36,6 +36,7 @@ class RefSim:
             getattr(L, f).argtypes = [vp, d]
         L.ref_curvature.argtypes = [vp]
         L.ref_velocity_bc.argtypes = [vp]
+        L.ref_fast_sweeping.argtypes = [vp, i]
         L.ref_configure_viscosity.argtypes = [vp, i]
         L.ref_cfl_dt.argtypes = [vp]
         L.ref_cfl_dt.restype = d
@@ -89,6 +90,9 @@ class RefSim:
 
     def step(self, dt):
         self.L.ref_step(self.h, dt)
+
+    def fast_sweeping(self, sweeps=4):
+        self.L.ref_fast_sweeping(self.h, sweeps)
 
     def apply_gravity(self, dt):
         self.L.ref_apply_gravity(self.h, dt)

@@ -20,6 +20,7 @@ tests/golden/cases.py and stores inputs and outputs:
   time_step           AdvanceOneTimeStepThread (order 3), without viscosity (the
                       reference's air/water setup) and with it configured
   cfl                 CFLOneTimeStep after ComputeCurvaturesThread
+  fast sweeping       FastSweepingMethodOriginal with 1 and 4 sweeps
 and, in rising_bubble_128_frames.npz, 100 frames of the 128^2 rising bubble
 (SIMULATION_WORLD::AdvanceOneFrame: curvature, CFL time step, time step); in
 poisson_test{3,5}_61.npz, POISSON_EQUATION_TEST's jump-condition problems 3 and 5.
@@ -66,6 +67,13 @@ def make_case(name, c, dt, pcg_tolerance, flow=True):
     s.reinitialization(dt)
     out["reinit_phi"] = s.get(R.PHI)
     s.close()
+
+    for sweeps in (1, 4):
+        s = mk()
+        s.set(R.PHI, c["phi"])
+        s.fast_sweeping(sweeps)
+        out[f"fsm{sweeps}_phi"] = s.get(R.PHI)
+        s.close()
 
     s = mk()
     s.set(R.PHI, c["phi"]); s.set(R.UA, c["ua"]); s.set(R.VA, c["va"])

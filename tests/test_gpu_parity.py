@@ -115,3 +115,14 @@ def test_mixed_advection_close_to_fp64(gb, name):
     got = c.get(gb.FIELD_PHI)[2:2 + nj, 2:2 + ni]
     want = g["rk3_phi"][2:2 + nj, 2:2 + ni]
     assert rel_l2(got, want) <= 1e-5
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("sweeps", [1, 4])
+def test_fast_sweeping_bitexact(gb, name, sweeps):
+    """FastSweepingMethodOriginal: wavefront Gauss-Seidel sweeps equal the reference's row-order sweeps."""
+    g = load_golden(name)
+    c = make_ctx(gb, g)
+    c.set(gb.FIELD_PHI, g["phi"])
+    c.fast_sweeping(sweeps)
+    np.testing.assert_array_equal(c.get(gb.FIELD_PHI), g[f"fsm{sweeps}_phi"])

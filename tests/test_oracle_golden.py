@@ -201,3 +201,13 @@ def test_jump_poisson_system(oracle, name):
     oracle.pcg_ic0(gr, oracle.params(pcg_tolerance=1e-13, pcg_max_iterations=100000), bx, by, dg, rhs, x)
     want = g["solution"][1:-1, 1:-1]
     assert np.linalg.norm(x - want) <= 1e-10 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("sweeps", [1, 4])
+def test_fast_sweeping(oracle, name, sweeps):
+    g = load_golden(name)
+    gr, ni, nj = setup(oracle, g)
+    phi = g["phi"].copy()
+    oracle.fast_sweeping(gr, phi, sweeps)
+    np.testing.assert_array_equal(phi, g[f"fsm{sweeps}_phi"])
