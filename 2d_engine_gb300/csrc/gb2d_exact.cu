@@ -7,6 +7,7 @@
 // The "mixed" advection variants (FP32 flux evaluation, FP64 state) live here
 // too so that they share the loaders.
 #include <cstdio>
+#include <cstdlib>
 
 #include "gb2d_internal.cuh"
 #include "gb2d_schemes.cuh"
@@ -177,6 +178,60 @@ __global__ void k_reinit_sweep(const double* __restrict__ src_a, double* __restr
     double s = __ldg(&S[i + (size_t)j * ni]);
     if (godunov_h<double>(s, mx, px, my, py, h)) out = old - dtau * s * h;
   }
+  GB_AT(dst, i, j) = out;
+}
+
+// The mixed reinit sweep, tiled: the WENO first differences of a node and of its
+// neighbours overlap, so one 32 x 8 tile stages phi with a 3-node halo (positions mapped
+// as the ghost-filled copy maps them) and forms every FP64 difference once (2.8 per node
+// instead of 12; FP64 issue is this kernel's bound), narrowed to FP32 in shared memory.
+// Each node then reads its 6 + 6 differences: the same values as the per-node gathers,
+// so the results equal k_reinit_sweep<true>'s bit for bit.
+constexpr int kRtX = 32, kRtY = 8;
+__global__ void __launch_bounds__(kRtX* kRtY) k_reinit_sweep_tiled(const double* __restrict__ src_a, double* __restrict__ dst_a,
+                                                                    const double* __restrict__ S, LSArgs a, double dtau) {
+  __shared__ double ph[kRtY + 6][kRtX + 6];
+  __shared__ float dxs[kRtY][kRtX + 5];
+  __shared__ float dys[kRtY + 5][kRtX];
+  const int ni = a.ni, nj = a.nj, tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = (int)blockIdx.x * kRtX - 2, j0 = (int)blockIdx.y * kRtY - 2;  // tile origin in node coordinates
+  const DField src = dfield((double*)src_a, 2, ni, nj), dst = dfield(dst_a, 2, ni, nj);
+  for (int k = ty * kRtX + tx; k < (kRtX + 6) * (kRtY + 6); k += kRtX * kRtY) {
+    const int x = k % (kRtX + 6), y = k / (kRtX + 6);
+    int ii = i0 - 3 + x, jj = j0 - 3 + y;
+    ii = ii < 0 ? 1 : (ii >= ni ? ni - 2 : ii);
+    jj = jj < 0 ? 1 : (jj >= nj ? nj - 2 : jj);
+    ph[y][x] = __ldg(&GB_AT(src, ii, jj));
+  }
+  __syncthreads();
+  for (int k = ty * kRtX + tx; k < kRtY * (kRtX + 5); k += kRtX * kRtY) {
+    const int p = k % (kRtX + 5), r = k / (kRtX + 5);
+    dxs[r][p] = narrow(ph[r + 3][p + 1] - ph[r + 3][p]);
+  }
+  for (int k = ty * kRtX + tx; k < (kRtY + 5) * kRtX; k += kRtX * kRtY) {
+    const int c = k % kRtX, p = k / kRtX;
+    dys[p][c] = narrow(ph[p + 1][c + 3] - ph[p][c + 3]);
+  }
+  __syncthreads();
+  const int i = i0 + tx, j = j0 + ty;
+  if (i > ni + 1 || j > nj + 1) return;
+  if (i < 0 || j < 0 || i >= ni || j >= nj) {  // the ghost ring is copied
+    GB_AT(dst, i, j) = GB_AT(src, i, j);
+    return;
+  }
+  const double old = ph[ty + 3][tx + 3];
+  double out = old;
+  float d[6], mx, px, my, py, h;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d[k] = dxs[ty][tx + k] * a.odx_f;
+  mx = weno5_side<float>(d[0], d[1], d[2], d[3], d[4], a.eps_f);
+  px = weno5_side<float>(d[5], d[4], d[3], d[2], d[1], a.eps_f);
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d[k] = dys[ty + k][tx] * a.ody_f;
+  my = weno5_side<float>(d[0], d[1], d[2], d[3], d[4], a.eps_f);
+  py = weno5_side<float>(d[5], d[4], d[3], d[2], d[1], a.eps_f);
+  const double sv = __ldg(&S[i + (size_t)j * ni]);
+  if (godunov_h<float>(narrow(sv), mx, px, my, py, h)) out = old - dtau * sv * widen(h);
   GB_AT(dst, i, j) = out;
 }
 
@@ -613,7 +668,15 @@ void launch_reinit_sign(cudaStream_t s, const gb2d_ctx* c, const double* phi, do
 void launch_reinit_sweep(cudaStream_t s, const gb2d_ctx* c, const double* src, double* dst, const double* S, double dtau, int mixed) {
   dim3 blk(32, 8);
   dim3 grd = grid2d(c->grid.ni + 4, c->grid.nj + 4, blk);
-  if (mixed)
+  // GB2D_REINIT_UNTILED=1 (read once) selects the per-node mixed kernel, which the tiled one
+  // must equal bit for bit.
+  static const bool untiled = [] {
+    const char* e = getenv("GB2D_REINIT_UNTILED");
+    return e && e[0] == '1';
+  }();
+  if (mixed && !untiled)
+    k_reinit_sweep_tiled<<<grd, blk, 0, s>>>(src, dst, S, ls_args(c), dtau);
+  else if (mixed)
     k_reinit_sweep<true><<<grd, blk, 0, s>>>(src, dst, S, ls_args(c), dtau);
   else
     k_reinit_sweep<false><<<grd, blk, 0, s>>>(src, dst, S, ls_args(c), dtau);
