@@ -506,6 +506,26 @@ def run_gb300(args):
     print(json.dumps(res))
 
 
+def profile_step():
+    """Two AdvanceOneFrame calls (curvature, CFL time step, order-3 time step) of the benchmark's
+    1024^2 state in mixed precision with the viscous term on: the workload of the time-step
+    launch list in profiles/."""
+    import importlib
+    gb = importlib.import_module("2d_engine_gb300")
+    case = make_case()
+    c = gb.Context(N, N, advection_precision=gb.PRECISION_MIXED)
+    c.set_flow_params(water_viscosity=1.0, air_viscosity=0.01, viscosity=True)
+    for f, k in ((gb.FIELD_PHI, "phi"), (gb.FIELD_U, "u"), (gb.FIELD_V, "v"), (gb.FIELD_P, "p"), (gb.FIELD_UA, "ua"),
+                 (gb.FIELD_VA, "va")):
+        c.set(f, case[k])
+    opts = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=TOL)
+    dt = 0.0
+    for _ in range(2):
+        dt, st = c.advance_frame(cfl=1.0, prev_dt=dt, opts=opts)
+    c.synchronize()
+    print(json.dumps({"frames": 2, "dt": dt, "cg_iterations_last_frame": st.iterations}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -513,7 +533,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile-step", action="store_true",
+                    help="only run two mixed-precision frames (CFL time steps, viscous term on) of the 1024^2 state, for profilers")
     args = ap.parse_args()
+    if args.profile_step:
+        profile_step()
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
