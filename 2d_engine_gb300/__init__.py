@@ -110,6 +110,7 @@ def library():
         "gb2d_batch_autotune": [vp, d, O, vp],
         "gb2d_batch_advance": [vp, i, d, vp, O, ctypes.POINTER(BatchStatsT)],
         "gb2d_jump_poisson_solve": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, O, S],
+        "gb2d_projection_density_gradient": [vp, d, ctypes.POINTER(d), ctypes.POINTER(d)],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
         "gb2d_poisson_solve": [vp, vp, vp, O, S],
@@ -362,6 +363,12 @@ class Context:
         if rc != 0 and not (allow_max_iters and rc == -4):
             self._check(rc)
         return p, nx, ny, st
+
+    def projection_density_gradient(self, dt):
+        """(dL/d water_density, dL/d air_density) of the loss of the last projection_adjoint call."""
+        w, a = ctypes.c_double(), ctypes.c_double()
+        self._check(self.L.gb2d_projection_density_gradient(self.h, dt, ctypes.byref(w), ctypes.byref(a)))
+        return w.value, a.value
 
     # Pressure system (a10/a15)
     def poisson_assemble(self, dt):

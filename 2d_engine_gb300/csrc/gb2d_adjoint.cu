@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
 #include "gb2d_internal.cuh"
 #include "gb2d_schemes.cuh"
@@ -260,7 +261,162 @@ __global__ void k_proj_adj_vel(const double* __restrict__ lu_a, const double* __
   }
 }
 
+// d/d(theta) of a projection loss, theta one of the two densities, after the projection
+// adjoint (z with A z = dL/dp):
+//   dL/dtheta = sum_f lam_f du'_f/dtheta |_p  +  z . (db/dtheta - (dA/dtheta) p).
+// The face weights beta = vc vn (|phi_n|+|phi_c|) / (vc |phi_n| + vn |phi_c|), v = 1/rho
+// of the node's phase, enter A (off-diagonals and the dx-only diagonal with its corner pin,
+// POISSON_SOLVER.cpp:743-872) and the jump fluxes of b (:878-948); the velocity update's
+// coefficients are 1/rho of the + node or 1/rho of the smeared face density
+// (PROJECTION_2D.h:1297-1416).  One partial sum per block.
+struct DensArgs {
+  int ni, nj;
+  double odx, ody, idx2, idy2, odx2, ody2, dt, sigma;
+  double water, air, inv_water, inv_air, eps_h, eps_v, oeh, oev;
+  int wrt_water;  // 1: d/d(water density), 0: d/d(air density)
+};
+
+__device__ __forceinline__ double v_of(double l, const DensArgs& a) {
+  if (lez(l)) return a.inv_air;
+  if (gtz(l)) return a.inv_water;
+  return 1.0;
+}
+__device__ __forceinline__ double dv_of(double l, const DensArgs& a) {  // d(1/rho)/d(theta)
+  if (lez(l)) return a.wrt_water ? 0.0 : -a.inv_air * a.inv_air;
+  if (gtz(l)) return a.wrt_water ? -a.inv_water * a.inv_water : 0.0;
+  return 0.0;
+}
+// d beta / d theta of the face between c and n (phi values lc, ln; ghost-mapped nodes).
+__device__ __forceinline__ double dbeta(double lc, double ln, double lvc, double lvn, const DensArgs& a) {
+  const double vc = v_of(lvc, a), vn = v_of(lvn, a), dvc = dv_of(lvc, a), dvn = dv_of(lvn, a);
+  if (dvc == 0.0 && dvn == 0.0) return 0.0;
+  const double ac = fabs(lc), an = fabs(ln), S = an + ac, D = vc * an + vn * ac;
+  return (vn * vn * S * ac * dvc + vc * vc * S * an * dvn) / (D * D);
+}
+
+__global__ void k_density_grad(const double* __restrict__ phi_a, const double* __restrict__ kappa, const double* __restrict__ p_a,
+                               const double* __restrict__ z_a, const double* __restrict__ lu_a, const double* __restrict__ lv_a,
+                               double* __restrict__ part, DensArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const DField phi = dfield((double*)phi_a, 2, ni, nj), P = dfield((double*)p_a, 1, ni, nj), Z = dfield((double*)z_a, 1, ni, nj);
+  const DField lu = dfield((double*)lu_a, 2, ni + 1, nj), lv = dfield((double*)lv_a, 2, ni, nj + 1);
+  auto L = [&](int i, int j) { return GB_AT(phi, i, j); };
+  // the node whose density a face weight reads (FillGhostCellsFrom mapping, as vnode)
+  auto LV = [&](int i, int j) {
+    i = i < 0 ? 1 : (i >= ni ? ni - 2 : i);
+    j = j < 0 ? 1 : (j >= nj ? nj - 2 : j);
+    return GB_AT(phi, i, j);
+  };
+  auto jc = [&](int i, int j) -> double {
+    if (i < 0 || j < 0 || i >= ni || j >= nj) return 0.0;
+    return a.sigma * kappa[i + (size_t)j * ni];
+  };
+  double acc = 0;
+  GB_FOR_IJ(i, j, ni, nj) {
+    const double lc = L(i, j);
+    const double bl = dbeta(lc, L(i - 1, j), LV(i, j), LV(i - 1, j), a), br = dbeta(lc, L(i + 1, j), LV(i, j), LV(i + 1, j), a);
+    const double bb = dbeta(lc, L(i, j - 1), LV(i, j), LV(i, j - 1), a), bt = dbeta(lc, L(i, j + 1), LV(i, j), LV(i, j + 1), a);
+    double coef = 0;
+    if (i > 0) coef += bl;
+    if (i < ni - 1) coef += br;
+    if (j > 0) coef += bb;
+    if (j < nj - 1) coef += bt;
+    if (i == 0 && j == 0) coef += bl + bb;  // the Neumann arms of the pinned corner cell
+    double Ap = a.idx2 * coef * GB_AT(P, i, j);
+    if (i > 0) Ap -= bl * a.idx2 * GB_AT(P, i - 1, j);
+    if (i < ni - 1) Ap -= br * a.idx2 * GB_AT(P, i + 1, j);
+    if (j > 0) Ap -= bb * a.idy2 * GB_AT(P, i, j - 1);
+    if (j < nj - 1) Ap -= bt * a.idy2 * GB_AT(P, i, j + 1);
+    // jump fluxes: +/- o2 av beta on arms that cross the interface
+    auto dF = [&](double ln, int in, int jn, double db, double o2) -> double {
+      const bool cneg = lez(lc), nneg = lez(ln);
+      const double ac = fabs(lc), an = fabs(ln);
+      if (cneg && !nneg && gtz(ln)) return o2 * ((jc(i, j) * an + jc(in, jn) * ac) / (ac + an)) * db;
+      if (!cneg && gtz(lc) && nneg) return -o2 * ((jc(i, j) * an + jc(in, jn) * ac) / (ac + an)) * db;
+      return 0.0;
+    };
+    const double db_node = -(dF(L(i - 1, j), i - 1, j, bl, a.odx2) + dF(L(i + 1, j), i + 1, j, br, a.odx2) +
+                             dF(L(i, j - 1), i, j - 1, bb, a.ody2) + dF(L(i, j + 1), i, j + 1, bt, a.ody2));
+    acc += GB_AT(Z, i, j) * (db_node - Ap);
+    // velocity update of the x-face (i, j) and the y-face (i, j), p fixed
+    for (int xc = 1; xc >= 0; --xc) {
+      const int in = xc ? i - 1 : i, jn = xc ? j : j - 1;
+      const double ln = L(in, jn), dp = GB_AT(P, i, j) - GB_AT(P, in, jn), od = xc ? a.odx : a.ody;
+      const double lam = xc ? GB_AT(lu, i, j) : GB_AT(lv, i, j);
+      double dc = 0, g = dp;
+      if (lc * ln >= 0) {
+        dc = dv_of(lc, a);
+      } else if (ltz(lc) || gtz(lc)) {
+        const double jcc = jc(i, j), jcn = jc(in, jn);
+        const double gam = (jcn * fabs(lc) + jcc * fabs(ln)) / (fabs(lc) + fabs(ln));
+        const double H = heaviside(0.5 * (lc + ln), xc ? a.eps_h : a.eps_v, xc ? a.oeh : a.oev);
+        const double dh = a.air + (a.water - a.air) * H;
+        const double ddh = a.wrt_water ? H : 1.0 - H;
+        dc = -ddh / (dh * dh);
+        g = ltz(lc) ? dp + gam : dp - gam;
+      }
+      acc += lam * (-a.dt * g * od * dc);
+    }
+  }
+  // block sum: warps by shuffle, then the warp sums in a fixed order
+  __shared__ double ws[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  const int lane = threadIdx.x & 31, warp = (threadIdx.x + threadIdx.y * blockDim.x) >> 5;
+  if (lane == 0) ws[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)((blockDim.x * blockDim.y + 31) / 32); ++w) t += ws[w];
+    part[blockIdx.x + (size_t)blockIdx.y * gridDim.x] = t;
+  }
+}
+
 }  // namespace
+
+int density_gradient(gb2d_ctx* c, double dt, double* d_water, double* d_air) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  const dim3 g = grid_ij(ni, nj);
+  const size_t nb = (size_t)g.x * g.y;
+  DensArgs a;
+  a.ni = ni;
+  a.nj = nj;
+  a.odx = c->base.odx;
+  a.ody = c->base.ody;
+  a.idx2 = 1.0 / (c->base.dx * c->base.dx);
+  a.idy2 = 1.0 / (c->base.dy * c->base.dy);
+  a.odx2 = c->base.odx2;
+  a.ody2 = c->base.ody2;
+  a.dt = dt;
+  a.sigma = c->prm.surface_tension;
+  a.water = c->prm.water_density;
+  a.air = c->prm.air_density;
+  a.inv_water = 1.0 / a.water;
+  a.inv_air = 1.0 / a.air;
+  a.eps_h = 1.5 * c->base.dx;
+  a.eps_v = 1.5 * c->base.dy;
+  a.oeh = 1.0 / a.eps_h;
+  a.oev = 1.0 / a.eps_v;
+  double out[2];
+  std::vector<double> host(nb);
+  for (int w = 0; w < 2; ++w) {
+    a.wrt_water = w == 0;
+    k_density_grad<<<g, kThreads, 0, c->stream>>>(c->phi_buf[c->phi_cur], c->kappa, c->p, c->xw, c->adj_lam_u, c->adj_lam_v,
+                                                   c->adj_gvel, a);
+    GB_LAUNCHED(1);
+    cudaError_t e = cudaMemcpyAsync(host.data(), c->adj_gvel, nb * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+      snprintf(c->err, sizeof(c->err), "density gradient: %s", cudaGetErrorString(e));
+      return GB2D_ERR_CUDA;
+    }
+    double sum = 0;
+    for (size_t k = 0; k < nb; ++k) sum += host[k];
+    out[w] = sum;
+  }
+  if (d_water) *d_water = out[0];
+  if (d_air) *d_air = out[1];
+  return GB2D_OK;
+}
 
 int adjoint_buffers(gb2d_ctx* c) {
   if (c->adj_coef) return GB2D_OK;

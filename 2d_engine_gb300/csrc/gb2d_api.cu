@@ -689,6 +689,11 @@ int gb2d_jump_poisson_solve(gb2d_ctx* c, const double* density, const int* bc, c
   return src;
 }
 
+int gb2d_projection_density_gradient(gb2d_ctx* c, double dt, double* d_water_density, double* d_air_density) {
+  if (!c || !std::isfinite(dt) || dt == 0.0 || !c->adj_coef) return GB2D_ERR_ARG;
+  return density_gradient(c, dt, d_water_density, d_air_density);
+}
+
 int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {
   if (!c || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
   int rc = curvature_and_assemble(c, dt);

@@ -209,6 +209,8 @@ void launch_weno5_adjoint(cudaStream_t s, gb2d_ctx* c, double dt, double* mu_ua,
 // solve into the padded z, adj_mu_u/v = lam + D^T z.
 void launch_projection_adjoint_rhs(cudaStream_t s, gb2d_ctx* c, double dt, int with_lam_p);
 void launch_projection_adjoint_vel(cudaStream_t s, gb2d_ctx* c, double dt, const double* z);
+// dL/d(water density), dL/d(air density) after the projection adjoint (z in c->xw).
+int density_gradient(gb2d_ctx* c, double dt, double* d_water, double* d_air);
 
 // ---- gb2d_jump.cu (FP64, compiled without FMA contraction) ----
 int jump_buffers(gb2d_ctx* c);

@@ -238,6 +238,12 @@ int gb2d_weno5_adjoint(gb2d_ctx* ctx, double dt, const double* lam_phi, double* 
 int gb2d_projection_adjoint(gb2d_ctx* ctx, double dt, const double* lam_u, const double* lam_v, const double* lam_p, double* mu_u,
                             double* mu_v, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
 
+/* The same loss's derivatives with respect to the two densities (water_density, air_density
+ * of gb2d_params), through the face weights of A, the jump fluxes of the right-hand side and
+ * the velocity update's 1/rho: dL/drho = sum lam du'/drho|p + z (db/drho - dA/drho p).  Call
+ * right after gb2d_projection_adjoint, which leaves z and the cotangents in the context. */
+int gb2d_projection_density_gradient(gb2d_ctx* ctx, double dt, double* d_water_density, double* d_air_density);
+
 /* Batches: many independent simulations of uneven grid sizes on one GPU (no counterpart
  * in the reference, which runs one simulation per process).  Each instance is a full
  * context with its own stream; host worker threads drive disjoint sets of instances frame

@@ -185,3 +185,39 @@ def test_window_gradient_against_oracle_reference(gb, oracle):
     got = phi0.grad.numpy()
     assert np.abs(got - ref).max() <= GRAD_TOL * np.abs(ref).max()
     c.close()
+
+
+@pytest.mark.parametrize("name", ["bubbles_17", "bubbles_33", "tall_24x40"])
+def test_projection_density_gradient(gb, name):
+    """dL/d(water density) and dL/d(air density) of a projection loss: adjoint against central
+    differences of the forward projection (the map is smooth in the densities)."""
+    g = load_golden(name)
+    dt = float(g["dt"])
+    opts = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=1e-11, max_iterations=20000)
+    rng = np.random.default_rng(10)
+    lu, lv, lp = rng.standard_normal(g["u"].shape), rng.standard_normal(g["v"].shape), rng.standard_normal(g["p"].shape)
+    lp[0, :] = lp[-1, :] = lp[:, 0] = lp[:, -1] = 0
+
+    def ctx(water, air):
+        c = gb.Context(int(g["ni"]), int(g["nj"]), 0.0, 0.0, float(g["x_max"]), float(g["y_max"]), water_density=water,
+                       air_density=air)
+        for f, k in ((gb.FIELD_PHI, "phi"), (gb.FIELD_U, "u"), (gb.FIELD_V, "v"), (gb.FIELD_P, "p")):
+            c.set(f, g[k])
+        c.projection(dt, opts, allow_max_iters=True)
+        return c
+
+    def L(water, air):
+        c = ctx(water, air)
+        val = float(np.sum(lu * c.get(gb.FIELD_U)) + np.sum(lv * c.get(gb.FIELD_V)) + np.sum(lp * c.get(gb.FIELD_P)))
+        c.close()
+        return val
+
+    c = ctx(1000.0, 1.0)
+    c.projection_adjoint(dt, lu, lv, lp, opts)
+    dw, da = c.projection_density_gradient(dt)
+    c.close()
+    for got, f, x in ((dw, lambda h: L(1000.0 + h, 1.0), 1000.0), (da, lambda h: L(1000.0, 1.0 + h), 1.0)):
+        h = 1e-2 * x  # large enough that the solves' 1e-11 residual does not show in the quotient
+        q = lambda s: (f(s) - f(-s)) / (2 * s)
+        fd = (4 * q(h / 2) - q(h)) / 3  # central differences, one Richardson step
+        assert abs(got - fd) <= GRAD_TOL * max(abs(fd), 1e-12), (got, fd)
