@@ -115,3 +115,74 @@ def window_loss(gb_ctx, phi0, ua, va, dt, steps, checkpoint_every=10, x_max=1.0,
         phi = torch.utils.checkpoint.checkpoint(segment, phi, use_reentrant=False) if phi.requires_grad else segment(phi)
         k += n
     return centroid_height(phi, gb_ctx.ni, gb_ctx.nj, x_max, y_max)
+
+
+class ProjectDensities(torch.autograd.Function):
+    """(u', v') = projection of a fixed intermediate velocity as a function of the two densities
+    (water, air: 0-d tensors); backward through gb2d_projection_adjoint and
+    gb2d_projection_density_gradient."""
+
+    @staticmethod
+    def forward(ctx, water, air, make_context, state, dt, opts):
+        c = make_context(float(water), float(air))
+        for f, k in ((FIELD_PHI, "phi"), (FIELD_U, "u"), (FIELD_V, "v"), (FIELD_P, "p")):
+            c.set(f, state[k])
+        c.projection(dt, opts, allow_max_iters=True)
+        ctx.c, ctx.dt, ctx.opts = c, dt, opts
+        return torch.from_numpy(c.get(FIELD_U)), torch.from_numpy(c.get(FIELD_V))
+
+    @staticmethod
+    def backward(ctx, gu, gv):
+        c = ctx.c
+        c.projection_adjoint(ctx.dt, _np(gu.contiguous()), _np(gv.contiguous()), None, ctx.opts)
+        dw, da = c.projection_density_gradient(ctx.dt)
+        c.close()
+        return (torch.tensor(dw, dtype=torch.float64), torch.tensor(da, dtype=torch.float64), None, None, None, None)
+
+
+def advecting_copy(u, g_in=2, g_out=3):
+    """The advecting copy of a MAC component, as Solve_Velocity makes it (FillGhostCellsFrom,
+    FIELD_STRUCTURE_2D.h:374-449): interior copied, every ghost layer the second interior line,
+    corners zero.  Differentiable."""
+    nJ, nI = u.shape[0] - 2 * g_in, u.shape[1] - 2 * g_in
+    inner = u[g_in:g_in + nJ, g_in:g_in + nI]
+    out = torch.zeros((nJ + 2 * g_out, nI + 2 * g_out), dtype=u.dtype)
+    out[g_out:g_out + nJ, g_out:g_out + nI] = inner
+    out[g_out:g_out + nJ, :g_out] = inner[:, 1:2].expand(nJ, g_out)
+    out[g_out:g_out + nJ, g_out + nI:] = inner[:, nI - 2:nI - 1].expand(nJ, g_out)
+    out[:g_out, g_out:g_out + nI] = inner[1:2, :].expand(g_out, nI)
+    out[g_out + nJ:, g_out:g_out + nI] = inner[nJ - 2:nJ - 1, :].expand(g_out, nI)
+    return out
+
+
+def buoyant_window_loss(gb, ni, nj, state, water, air, dt, steps, checkpoint_every=10, opts=None):
+    """A coupled differentiation window: the intermediate velocity u* of one gravity step
+    projected with densities (water, air) gives the advecting velocity, the bubble's level set
+    is advected `steps` level-set TVD-RK3 steps by it (reinitialisation off), and the loss is
+    the centroid height.  Differentiable in the densities (projection adjoint) and in the
+    advected level set's initial values (WENO5 adjoint); the projection's own level set is
+    held fixed."""
+    opts = opts or solve_opts(tolerance=1e-11, max_iterations=20000)
+
+    def make(w, a):
+        from . import Context
+        return Context(ni, nj, 0.0, 0.0, state["x_max"], state["y_max"], water_density=w, air_density=a)
+
+    u, v = ProjectDensities.apply(water, air, make, state, dt, opts)
+    ua, va = advecting_copy(u), advecting_copy(v)
+    c = make(1000.0, 1.0)
+    phi0 = torch.from_numpy(state["phi"].copy())
+    phi = phi0
+    k = 0
+    while k < steps:
+        n = min(checkpoint_every, steps - k)
+
+        def segment(p, a_, b_, n=n):
+            for _ in range(n):
+                p = levelset_rk3_frozen(c, p, a_, b_, dt)
+            return p
+
+        phi = torch.utils.checkpoint.checkpoint(segment, phi, ua, va, use_reentrant=False)
+        k += n
+    loss = centroid_height(phi, ni, nj, state["x_max"], state["y_max"])
+    return loss, c

@@ -221,3 +221,35 @@ def test_projection_density_gradient(gb, name):
         q = lambda s: (f(s) - f(-s)) / (2 * s)
         fd = (4 * q(h / 2) - q(h)) / 3  # central differences, one Richardson step
         assert abs(got - fd) <= GRAD_TOL * max(abs(fd), 1e-12), (got, fd)
+
+
+def test_buoyant_window_density_gradient(gb):
+    """Gradient of the bubble centroid after a buoyancy-driven projection and 10 level-set RK3
+    steps with respect to both densities, through the projection and WENO5 adjoints (with
+    checkpointed segments), against central differences of the whole window."""
+    ag = importlib.import_module("2d_engine_gb300.autograd")
+    case = rising_bubble_case(33, 33, seed=14)
+    dt = 0.25 / 32
+    u = case["u"].copy()
+    v = case["v"].copy()
+    v[2:-2, 2:-2] += dt * -9.8  # one gravity step on the y-faces (walls included, as ApplyGraivity)
+    state = dict(phi=case["phi"], u=u, v=v, p=case["p"], x_max=1.0, y_max=1.0)
+
+    def loss(w, a, grad=False):
+        W = torch.tensor(w, dtype=torch.float64, requires_grad=grad)
+        A = torch.tensor(a, dtype=torch.float64, requires_grad=grad)
+        L, c = ag.buoyant_window_loss(gb, 33, 33, state, W, A, dt, steps=10, checkpoint_every=5)
+        if grad:
+            L.backward()
+            out = (float(L), float(W.grad), float(A.grad))
+        else:
+            out = float(L)
+        c.close()
+        return out
+
+    L0, gw, ga = loss(1000.0, 1.0, grad=True)
+    for got, f, x in ((gw, lambda h: loss(1000.0 + h, 1.0), 1000.0), (ga, lambda h: loss(1000.0, 1.0 + h), 1.0)):
+        h = 1e-2 * x
+        q = lambda s: (f(s) - f(-s)) / (2 * s)
+        fd = (4 * q(h / 2) - q(h)) / 3
+        assert abs(got - fd) <= GRAD_TOL * max(abs(fd), 1e-3 * abs(L0)), (got, fd)
