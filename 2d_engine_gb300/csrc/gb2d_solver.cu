@@ -246,8 +246,12 @@ __global__ void __launch_bounds__(1024) k_dense_inverse(Level<T> C, double* __re
 
 // ---- tiled smoothing (levels above the tail) ----------------------------------
 //
-// A block of 32x8 threads owns a 64x16 tile; thread (tx, ty) owns the 2x2 quad of
-// cells (2tx..2tx+1, 2ty..2ty+1), which is also one coarse cell.  All NS
+// A block of 32x8 threads owns a tile of 64x16 cells (shape 0), 32x16 (shape 1)
+// or 32x8 (shape 2); its 2x2 quads of cells, each one coarse cell, are dealt to
+// the threads in order (shape 0: thread (tx, ty) owns the quad (tx, ty)).  The
+// smaller tiles serve the coarser levels, where a level has fewer large tiles than
+// the GPU has SMs and a launch lasts as long as one tile's staging and sweeps:
+// a smaller window halves the loads and half-sweep cells per thread.  All NS
 // red-black sweeps of one side of the V-cycle run in ONE launch: the block stages
 // x and the coefficients (b, 1/dg, cx, cy, and dg when it restricts) for the tile
 // plus a halo of 2 NS (+1 to restrict) cells in shared memory with unrolled,
@@ -260,25 +264,31 @@ __global__ void __launch_bounds__(1024) k_dense_inverse(Level<T> C, double* __re
 // in-place write would let a block read a neighbour's already-smoothed (and,
 // when prolonging, already-corrected) value.
 
-constexpr int BXT = 32, BYT = 8;          // threads per block (x, y)
-constexpr int TXS = 2 * BXT, TYS = 2 * BYT;  // tile of one block
+constexpr int BXT = 32, BYT = 8;  // threads per block (x, y)
+constexpr int kTileShapes = 3;
 
-template <typename T, int H>
-struct Win {
-  static constexpr int W = TXS + 2 * H, HH = TYS + 2 * H, N = W * HH;
+template <int SH>
+struct TileShape {
+  static constexpr int X = SH == 0 ? 64 : 32, Y = SH == 2 ? 8 : 16;  // cells of one block's tile
+  static constexpr int QX = X / 2, QY = Y / 2;                        // its quads (coarse cells)
 };
 
-template <typename T, int H, bool DG>
+template <typename T, int H, int SH>
+struct Win {
+  static constexpr int W = TileShape<SH>::X + 2 * H, HH = TileShape<SH>::Y + 2 * H, N = W * HH;
+};
+
+template <typename T, int H, bool DG, int SH>
 constexpr size_t sweep_smem() {
-  return sizeof(T) * (size_t)Win<T, H>::N * (DG ? 6 : 5);
+  return sizeof(T) * (size_t)Win<T, H, SH>::N * (DG ? 6 : 5);
 }
 
 // Stage the window.  LOAD_X: read x (else zero); PROLONG: add the coarse correction.
 // The window's cells are enumerated flat (division by compile-time constants
 // only), so every thread of the block has work in every pass.
-template <typename T, int H, bool LOAD_X, bool PROLONG, bool DG>
+template <typename T, int H, bool LOAD_X, bool PROLONG, bool DG, int SH>
 __device__ __forceinline__ void stage_window(const Level<T>& L, const Level<T>& C, T* sm, int i0, int j0) {
-  using Wn = Win<T, H>;
+  using Wn = Win<T, H, SH>;
   constexpr int W = Wn::W, HH = Wn::HH, N = Wn::N;
   T *xs = sm, *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N, *ds = sm + 5 * N;
   const int gi0 = i0 - H, gj0 = j0 - H;
@@ -315,9 +325,9 @@ __device__ __forceinline__ void stage_window(const Level<T>& L, const Level<T>& 
 
 // Half sweep of one colour over the window shrunk by R cells per side: the
 // colour's RH x RW/2 cells are enumerated flat over the block's threads.
-template <typename T, int H, int R>
+template <typename T, int H, int R, int SH>
 __device__ __forceinline__ void window_half(T* sm, int i0, int j0, int nI, int nJ, int color) {
-  using Wn = Win<T, H>;
+  using Wn = Win<T, H, SH>;
   constexpr int W = Wn::W, HH = Wn::HH, N = Wn::N;
   constexpr int RW = W - 2 * R, RH = HH - 2 * R, HALF = RW / 2, TOT = RH * HALF;
   static_assert(RW % 2 == 0, "window rows must hold an even number of cells");
@@ -395,96 +405,112 @@ __device__ __forceinline__ void publish_rz(Scalars* sc, double rz) {
 
 // Half sweeps R = R0..R1 (window shrunk by R), colour of the first = C0,
 // alternating, with a block barrier after each.
-template <typename T, int H, int R, int R1, int C0>
+template <typename T, int H, int R, int R1, int C0, int SH>
 __device__ __forceinline__ void window_halves(T* sm, int i0, int j0, int nI, int nJ) {
   if constexpr (R <= R1) {
-    window_half<T, H, R>(sm, i0, j0, nI, nJ, (C0 + R - 1) & 1);
+    window_half<T, H, R, SH>(sm, i0, j0, nI, nJ, (C0 + R - 1) & 1);
     __syncthreads();
-    window_halves<T, H, R + 1, R1, C0>(sm, i0, j0, nI, nJ);
+    window_halves<T, H, R + 1, R1, C0, SH>(sm, i0, j0, nI, nJ);
   }
 }
 
-template <typename T, int NS>
+template <typename T, int NS, int SH>
 constexpr size_t pre_smem() {
-  return sweep_smem<T, 2 * NS + 1, false>();
+  return sweep_smem<T, 2 * NS + 1, false, SH>();
 }
 
 // The diagonal from its staged reciprocal (the residual after pre-smoothing;
 // keeps dg out of shared memory).
 __device__ __forceinline__ float diag_of(float idg) { return __frcp_rn(idg); }
 __device__ __forceinline__ double diag_of(double idg) { return __drcp_rn(idg); }
-template <typename T, int NS>
+template <typename T, int NS, int SH>
 constexpr size_t post_smem() {
-  return sweep_smem<T, 2 * NS, false>();
+  return sweep_smem<T, 2 * NS, false, SH>();
 }
 
 // Pre-smoothing: NS red-black sweeps (red first) from x = 0, then the residual
 // of the red cells (the black ones are zero after the last black half sweep)
 // averaged into the coarse right-hand side, with the diagonal recovered from
 // 1/dg.  x is written to xout.
-template <typename T, int NS>
+template <typename T, int NS, int SH>
 __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C, T* __restrict__ xout, const int* __restrict__ done) {
   pdl_enter();
   if (*done) return;
   constexpr int H = 2 * NS + 1;
-  using Wn = Win<T, H>;
+  using Wn = Win<T, H, SH>;
+  using Ts = TileShape<SH>;
   constexpr int W = Wn::W, N = Wn::N;
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
-  const int i0 = blockIdx.x * TXS, j0 = blockIdx.y * TYS;
-  stage_window<T, H, false, false, false>(L, C, sm, i0, j0);
+  const int i0 = blockIdx.x * Ts::X, j0 = blockIdx.y * Ts::Y;
+  stage_window<T, H, false, false, false, SH>(L, C, sm, i0, j0);
   __syncthreads();
-  window_halves<T, H, 1, 2 * NS, 0>(sm, i0, j0, L.nI, L.nJ);
+  window_halves<T, H, 1, 2 * NS, 0, SH>(sm, i0, j0, L.nI, L.nJ);
   const T *xs = sm, *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N;
-  T acc = 0;
+  const int tid = threadIdx.x + threadIdx.y * BXT;
 #pragma unroll
-  for (int dr = 0; dr < 2; ++dr)
+  for (int q0 = 0; q0 < Ts::QX * Ts::QY; q0 += BXT * BYT) {
+    const int q = q0 + tid;
+    if (q >= Ts::QX * Ts::QY) continue;
+    const int qx = q % Ts::QX, qy = q / Ts::QX;
+    T acc = 0;
 #pragma unroll
-    for (int dc = 0; dc < 2; ++dc) {
-      const int ti = 2 * threadIdx.x + dc, tj = 2 * threadIdx.y + dr;
-      const int gi = i0 + ti, gj = j0 + tj;
-      if (gi >= L.nI || gj >= L.nJ) continue;
-      const int s = (ti + H) + (tj + H) * W;
-      xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
-      if (!((gi + gj) & 1)) {  // red cells: black residuals are zero after the black half sweep
-        T ax = diag_of(is[s]) * xs[s] - cxs[s] * xs[s - 1] - cxs[s + 1] * xs[s + 1] - cys[s] * xs[s - W] - cys[s + W] * xs[s + W];
-        acc += bs[s] - ax;
+    for (int dr = 0; dr < 2; ++dr)
+#pragma unroll
+      for (int dc = 0; dc < 2; ++dc) {
+        const int ti = 2 * qx + dc, tj = 2 * qy + dr;
+        const int gi = i0 + ti, gj = j0 + tj;
+        if (gi >= L.nI || gj >= L.nJ) continue;
+        const int s = (ti + H) + (tj + H) * W;
+        xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
+        if (!((gi + gj) & 1)) {  // red cells: black residuals are zero after the black half sweep
+          T ax = diag_of(is[s]) * xs[s] - cxs[s] * xs[s - 1] - cxs[s + 1] * xs[s + 1] - cys[s] * xs[s - W] - cys[s + W] * xs[s + W];
+          acc += bs[s] - ax;
+        }
       }
-    }
-  const int I = i0 / 2 + threadIdx.x, J = j0 / 2 + threadIdx.y;
-  if (I < C.nI && J < C.nJ) C.b[(size_t)(I + 1) + (size_t)(J + 1) * C.ld] = (T)0.25 * acc;
+    const int I = i0 / 2 + qx, J = j0 / 2 + qy;
+    if (I < C.nI && J < C.nJ) C.b[(size_t)(I + 1) + (size_t)(J + 1) * C.ld] = (T)0.25 * acc;
+  }
 }
 
 // Post-smoothing: x (from L.x) plus the prolonged coarse correction, then NS
 // black-red sweeps (black first); x to xout.  With part_rz (finest level) r.z
 // (b = r, x = z there) is reduced and beta published.
-template <typename T, int NS>
+template <typename T, int NS, int SH>
 __global__ void __launch_bounds__(BXT* BYT) k_post_smooth(Level<T> L, Level<T> C, T* __restrict__ xout, double* __restrict__ part_rz,
                                                          unsigned* __restrict__ counter, Scalars* sc, const int* __restrict__ done) {
   pdl_enter();
   if (*done) return;
   constexpr int H = 2 * NS;
-  using Wn = Win<T, H>;
+  using Wn = Win<T, H, SH>;
+  using Ts = TileShape<SH>;
   constexpr int W = Wn::W, N = Wn::N;
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
-  const int i0 = blockIdx.x * TXS, j0 = blockIdx.y * TYS;
-  stage_window<T, H, true, true, false>(L, C, sm, i0, j0);
+  const int i0 = blockIdx.x * Ts::X, j0 = blockIdx.y * Ts::Y;
+  stage_window<T, H, true, true, false, SH>(L, C, sm, i0, j0);
   __syncthreads();
-  window_halves<T, H, 1, 2 * NS, 1>(sm, i0, j0, L.nI, L.nJ);
+  window_halves<T, H, 1, 2 * NS, 1, SH>(sm, i0, j0, L.nI, L.nJ);
   const T *xs = sm, *bs = sm + N;
   Acc<T> acc;
+  const int tid = threadIdx.x + threadIdx.y * BXT;
 #pragma unroll
-  for (int dr = 0; dr < 2; ++dr)
+  for (int q0 = 0; q0 < Ts::QX * Ts::QY; q0 += BXT * BYT) {
+    const int q = q0 + tid;
+    if (q >= Ts::QX * Ts::QY) continue;
+    const int qx = q % Ts::QX, qy = q / Ts::QX;
 #pragma unroll
-    for (int dc = 0; dc < 2; ++dc) {
-      const int ti = 2 * threadIdx.x + dc, tj = 2 * threadIdx.y + dr;
-      const int gi = i0 + ti, gj = j0 + tj;
-      if (gi >= L.nI || gj >= L.nJ) continue;
-      const int s = (ti + H) + (tj + H) * W;
-      xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
-      if (part_rz) acc.add(bs[s] * xs[s]);
-    }
+    for (int dr = 0; dr < 2; ++dr)
+#pragma unroll
+      for (int dc = 0; dc < 2; ++dc) {
+        const int ti = 2 * qx + dc, tj = 2 * qy + dr;
+        const int gi = i0 + ti, gj = j0 + tj;
+        if (gi >= L.nI || gj >= L.nJ) continue;
+        const int s = (ti + H) + (tj + H) * W;
+        xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
+        if (part_rz) acc.add(bs[s] * xs[s]);
+      }
+  }
   if (part_rz) {
     double rz;
     if (last_block_sum(acc.value(), part_rz, gridDim.x * gridDim.y, counter, &rz)) publish_rz(sc, rz);
@@ -830,6 +856,7 @@ struct Hierarchy {
   size_t ct_smem = 0;
   CtArgs<T> ct;
   Level<T> L[kMaxLevels];
+  int shape[kMaxLevels] = {};  // tile shape of each tiled level's smoothing launches
   T* r = nullptr;  // the preconditioner's input (padded fine layout, = L[0].b); z = L[0].x
 };
 
@@ -1083,7 +1110,11 @@ inline unsigned nblocks(size_t n, unsigned cap) {
   return (unsigned)(b < cap ? b : cap);
 }
 
-inline dim3 tiles(int nI, int nJ) { return dim3((nI + TXS - 1) / TXS, (nJ + TYS - 1) / TYS); }
+inline dim3 tiles(int nI, int nJ, int sh) {
+  const int X = sh == 0 ? TileShape<0>::X : sh == 1 ? TileShape<1>::X : TileShape<2>::X;
+  const int Y = sh == 0 ? TileShape<0>::Y : sh == 1 ? TileShape<1>::Y : TileShape<2>::Y;
+  return dim3((nI + X - 1) / X, (nJ + Y - 1) / Y);
+}
 
 template <typename T>
 void build_hierarchy(cudaStream_t s, Hierarchy<T>& H, const gb2d_ctx* c, double* b64, double* ainv) {
@@ -1132,13 +1163,32 @@ void pdl_launch(cudaStream_t s, dim3 grid, dim3 block, size_t smem, void (*k)(P.
   cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
 }
 
-template <typename T, int NS>
-void launch_pre(cudaStream_t s, dim3 grd, const Level<T>& L, const Level<T>& C, T* xo, const int* done) {
-  pdl_launch(s, grd, dim3(BXT, BYT), pre_smem<T, NS>(), k_pre_smooth<T, NS>, L, C, xo, done);
+template <typename T, int NS, int SH>
+void launch_pre_sh(cudaStream_t s, const Level<T>& L, const Level<T>& C, T* xo, const int* done) {
+  pdl_launch(s, tiles(L.nI, L.nJ, SH), dim3(BXT, BYT), pre_smem<T, NS, SH>(), k_pre_smooth<T, NS, SH>, L, C, xo, done);
+}
+template <typename T, int NS, int SH>
+void launch_post_sh(cudaStream_t s, const Level<T>& L, const Level<T>& C, T* xo, double* prz, Solver* S) {
+  pdl_launch(s, tiles(L.nI, L.nJ, SH), dim3(BXT, BYT), post_smem<T, NS, SH>(), k_post_smooth<T, NS, SH>, L, C, xo, prz, S->counter + 3,
+             S->sc, (const int*)S->done);
 }
 template <typename T, int NS>
-void launch_post(cudaStream_t s, dim3 grd, const Level<T>& L, const Level<T>& C, T* xo, double* prz, Solver* S) {
-  pdl_launch(s, grd, dim3(BXT, BYT), post_smem<T, NS>(), k_post_smooth<T, NS>, L, C, xo, prz, S->counter + 3, S->sc, (const int*)S->done);
+void launch_pre(cudaStream_t s, int sh, const Level<T>& L, const Level<T>& C, T* xo, const int* done) {
+  if (sh == 0)
+    launch_pre_sh<T, NS, 0>(s, L, C, xo, done);
+  else if (sh == 1)
+    launch_pre_sh<T, NS, 1>(s, L, C, xo, done);
+  else
+    launch_pre_sh<T, NS, 2>(s, L, C, xo, done);
+}
+template <typename T, int NS>
+void launch_post(cudaStream_t s, int sh, const Level<T>& L, const Level<T>& C, T* xo, double* prz, Solver* S) {
+  if (sh == 0)
+    launch_post_sh<T, NS, 0>(s, L, C, xo, prz, S);
+  else if (sh == 1)
+    launch_post_sh<T, NS, 1>(s, L, C, xo, prz, S);
+  else
+    launch_post_sh<T, NS, 2>(s, L, C, xo, prz, S);
 }
 
 inline bool probe_begin(Probe* pr, cudaStream_t s) {
@@ -1165,14 +1215,14 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
   // buffer the next finer level prolongs from, and z on the finest level).
   for (int l = 0; l < tail; ++l) {
     Level<T>& L = H.L[l];
-    const dim3 grd = tiles(L.nI, L.nJ);
+    const int sh = H.shape[l];
     bool on = l == 0 && probe_begin(pr, s);
     if (nu == 1)
-      launch_pre<T, 1>(s, grd, L, H.L[l + 1], L.xa, done);
+      launch_pre<T, 1>(s, sh, L, H.L[l + 1], L.xa, done);
     else if (nu == 2)
-      launch_pre<T, 2>(s, grd, L, H.L[l + 1], L.xa, done);
+      launch_pre<T, 2>(s, sh, L, H.L[l + 1], L.xa, done);
     else
-      launch_pre<T, 3>(s, grd, L, H.L[l + 1], L.xa, done);
+      launch_pre<T, 3>(s, sh, L, H.L[l + 1], L.xa, done);
     GB_LAUNCHED(1);
     probe_end(pr, s, on, smooth_bytes(L));
   }
@@ -1194,17 +1244,17 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
   GB_LAUNCHED(1);
   for (int l = tail - 1; l >= 0; --l) {
     Level<T>& L = H.L[l];
-    const dim3 grd = tiles(L.nI, L.nJ);
+    const int sh = H.shape[l];
     Level<T> Lin = L;
     Lin.x = L.xa;
     double* prz = l == 0 ? P_rz : nullptr;
     bool on = l == 0 && probe_begin(pr, s);
     if (nu == 1)
-      launch_post<T, 1>(s, grd, Lin, H.L[l + 1], L.x, prz, S);
+      launch_post<T, 1>(s, sh, Lin, H.L[l + 1], L.x, prz, S);
     else if (nu == 2)
-      launch_post<T, 2>(s, grd, Lin, H.L[l + 1], L.x, prz, S);
+      launch_post<T, 2>(s, sh, Lin, H.L[l + 1], L.x, prz, S);
     else
-      launch_post<T, 3>(s, grd, Lin, H.L[l + 1], L.x, prz, S);
+      launch_post<T, 3>(s, sh, Lin, H.L[l + 1], L.x, prz, S);
     GB_LAUNCHED(1);
     probe_end(pr, s, on, smooth_bytes(L));
   }
@@ -1343,16 +1393,46 @@ int inner_pcg(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, doubl
   return iters;
 }
 
+template <typename T, int SH>
+cudaError_t set_smooth_smem_sh() {
+  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaFuncSetAttribute(k_pre_smooth<T, 1, SH>, a, (int)pre_smem<T, 1, SH>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_smooth<T, 2, SH>, a, (int)pre_smem<T, 2, SH>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_smooth<T, 3, SH>, a, (int)pre_smem<T, 3, SH>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 1, SH>, a, (int)post_smem<T, 1, SH>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 2, SH>, a, (int)post_smem<T, 2, SH>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 3, SH>, a, (int)post_smem<T, 3, SH>());
+  return e;
+}
 template <typename T>
 cudaError_t set_smooth_smem() {
-  const cudaFuncAttribute a = cudaFuncAttributeMaxDynamicSharedMemorySize;
-  cudaError_t e = cudaFuncSetAttribute(k_pre_smooth<T, 1>, a, (int)pre_smem<T, 1>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_smooth<T, 2>, a, (int)pre_smem<T, 2>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_pre_smooth<T, 3>, a, (int)pre_smem<T, 3>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 1>, a, (int)post_smem<T, 1>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 2>, a, (int)post_smem<T, 2>());
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_post_smooth<T, 3>, a, (int)post_smem<T, 3>());
+  cudaError_t e = set_smooth_smem_sh<T, 0>();
+  if (e == cudaSuccess) e = set_smooth_smem_sh<T, 1>();
+  if (e == cudaSuccess) e = set_smooth_smem_sh<T, 2>();
   return e;
+}
+
+// Tile shape per tiled level: 32x16 where that gives at least 8 blocks per SM,
+// else 32x8.  Measured on GB300 (MG-PCG projection to 1e-8, 1024^2-4096^2), the
+// 32x16 tile beats 64x16 on every level size: its 22 KB window (FP32, two sweeps)
+// lets 8 blocks share an SM, against 5, and the extra warps hide the staging
+// loads' latency better than the larger tile saves halo work; below 1024^2 the
+// 32x8 tile's shorter per-block pipeline wins.  GB2D_TILE_SHAPES="s0,s1,..."
+// (0, 1 or 2 per level from the finest) overrides the rule, for tuning.
+template <typename T>
+void plan_shapes(Hierarchy<T>& H, int nsm) {
+  const char* env = getenv("GB2D_TILE_SHAPES");
+  for (int l = 0; l < H.nlev; ++l) {
+    const dim3 t = tiles(H.L[l].nI, H.L[l].nJ, 1);
+    const int sh = (long long)t.x * t.y >= 8LL * nsm ? 1 : 2;
+    H.shape[l] = sh;
+  }
+  for (int l = 0; env && *env && l < H.nlev; ++l) {
+    const int v = *env - '0';
+    if (v >= 0 && v < kTileShapes) H.shape[l] = v;
+    while (*env && *env != ',') ++env;
+    if (*env == ',') ++env;
+  }
 }
 
 }  // namespace
@@ -1366,7 +1446,7 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
   S->nj = nj;
   size_t n = (size_t)ni * nj;
   S->G = (int)nblocks(n, 1216);
-  dim3 t = tiles(ni, nj);
+  dim3 t = tiles(ni, nj, kTileShapes - 1);  // the most blocks any tile shape launches
   S->nparts_cap = (int)(t.x * t.y) > S->G ? (int)(t.x * t.y) : S->G;
   size_t np = (size_t)(ni + 2) * (nj + 2);
   cudaError_t e = alloc_hierarchy(S->h64, ni, nj);
@@ -1375,6 +1455,10 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
     int P = ctail_cluster_size();
     plan_ctail(S->h64, P);
     plan_ctail(S->h32, P);
+    int dev = 0, nsm = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    plan_shapes(S->h64, nsm);
+    plan_shapes(S->h32, nsm);
   }
   if (e == cudaSuccess) e = cudaMalloc(&S->ainv64, sizeof(double) * kCoarseMax * kCoarseMax);
   if (e == cudaSuccess) e = cudaMalloc(&S->ainv32, sizeof(double) * kCoarseMax * kCoarseMax);

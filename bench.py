@@ -382,7 +382,6 @@ def run_gb300(args):
     nprobe, probe_ms, probe_bytes = cm.probe_read()
     cm.probe(False)
     ms_64, it_64, st_64 = timed(c64, fp64, max(1, min(args.steps, 3)), 0)
-    clk = clocks.stop()
 
     p_mixed = cm.get(gb.FIELD_P)
     p_64 = c64.get(gb.FIELD_P)
@@ -394,19 +393,23 @@ def run_gb300(args):
     out = {k: torch.empty(case[k].shape, dtype=torch.float64).pin_memory().numpy() for k in ("p", "u", "v")}
     h2d = sum(pin[k].nbytes for k in pin)
     d2h = sum(out[k].nbytes for k in out)
-    e2e = []
+    e2e, e2e_h2d, e2e_d2h = [], [], []
     for step in range(args.warmup + args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            ev[0].record(stream)
             cm.set(gb.FIELD_PHI, pin["phi"]); cm.set(gb.FIELD_U, pin["u"]); cm.set(gb.FIELD_V, pin["v"]); cm.set(gb.FIELD_P, pin["p"])
+            ev[1].record(stream)
             cm.projection(dt, mixed)
+            ev[2].record(stream)
             cm.get(gb.FIELD_P, out["p"]); cm.get(gb.FIELD_U, out["u"]); cm.get(gb.FIELD_V, out["v"])
-            e1.record(stream)
-        e1.synchronize()
+            ev[3].record(stream)
+        ev[3].synchronize()
         if step >= args.warmup:
-            e2e.append(e0.elapsed_time(e1))
+            e2e.append(ev[0].elapsed_time(ev[3]))
+            e2e_h2d.append(ev[0].elapsed_time(ev[1]))
+            e2e_d2h.append(ev[2].elapsed_time(ev[3]))
 
     # Level-set path of the same workload (not part of the metric): one level-set
     # TVD-RK3 step with its reinitialisation (3 WENO5 sweeps + 3 x 25 reinit sweeps),
@@ -464,6 +467,8 @@ def run_gb300(args):
 
     batch = run_batch(gb, BATCH_INSTANCES, BATCH_FRAMES, cpu=not args.no_cpu and rank == 0, dist=dist, rank=rank, ws=ws)
     rt = run_rayleigh_taylor(gb, stream)
+    clk = clocks.stop()
+    clk["window"] = "every timed leg (projections, end to end, level set, time step, batch, Rayleigh-Taylor)"
 
     ms_step = max_over_ranks(dist, statistics.mean(ms_m))
     value = ms_step / ws
@@ -494,7 +499,9 @@ def run_gb300(args):
                    "levelset_rk3_1024": levelset, "time_step_1024": time_step, "batched_rising_bubbles": batch,
                    "rayleigh_taylor_2048": rt},
         "clocks": clk,
-        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "h2d_ms": statistics.mean(e2e_h2d), "d2h_ms": statistics.mean(e2e_d2h),
+                "h2d_gbs": h2d / statistics.mean(e2e_h2d) / 1e6, "d2h_gbs": d2h / statistics.mean(e2e_d2h) / 1e6},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "finest-level smoothing launch (k_pre_smooth / k_post_smooth: two red-black sweeps each, FP32)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
@@ -526,6 +533,30 @@ def profile_step():
     print(json.dumps({"frames": 2, "dt": dt, "cg_iterations_last_frame": st.iterations}))
 
 
+def profile_projection():
+    """The headline workload alone: 4 mixed-precision projections of the 1024^2 state (3 warm-up,
+    1 as timed), each restored from a device checkpoint, then 1 FP64 projection: the workload of
+    the projection launch list and the smoothing-kernel capture in profiles/."""
+    import importlib
+    gb = importlib.import_module("2d_engine_gb300")
+    case = make_case()
+    dt = 0.5 / (N - 1)
+    out = {}
+    for name, prec, reps in (("mixed", gb.PRECISION_MIXED, 4), ("fp64", gb.PRECISION_FP64, 1)):
+        c = gb.Context(N, N)
+        for f, k in ((gb.FIELD_PHI, "phi"), (gb.FIELD_U, "u"), (gb.FIELD_V, "v"), (gb.FIELD_P, "p")):
+            c.set(f, case[k])
+        c.checkpoint_save()
+        opts = gb.solve_opts(precision=prec, tolerance=TOL)
+        for _ in range(reps):
+            c.checkpoint_restore()
+            st = c.projection(dt, opts)
+        c.synchronize()
+        out[name + "_iterations"] = st.iterations
+        c.close()
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -533,9 +564,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile-projection", action="store_true",
+                    help="only run the 1024^2 projections (4 mixed, 1 FP64), for profilers")
     ap.add_argument("--profile-step", action="store_true",
                     help="only run two mixed-precision frames (CFL time steps, viscous term on) of the 1024^2 state, for profilers")
     args = ap.parse_args()
+    if args.profile_projection:
+        profile_projection()
+        return
     if args.profile_step:
         profile_step()
         return
