@@ -118,6 +118,7 @@ def library():
         "gb2d_probe_enable": [vp, i],
         "gb2d_probe_read": [vp, ctypes.POINTER(i), ctypes.POINTER(d), ctypes.POINTER(d)],
         "gb2d_kernel_launches": [ctypes.POINTER(ctypes.c_ulonglong)],
+        "gb2d_alu_peaks": [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
         "gb2d_solver_layout": [vp, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)],
         "gb2d_check_exact_division": [ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)],
         "gb2d_checkpoint_save": [vp],
@@ -141,6 +142,15 @@ def kernel_launches():
     n = ctypes.c_ulonglong()
     library().gb2d_kernel_launches(ctypes.byref(n))
     return n.value
+
+
+def alu_peaks():
+    """(FP64, FP32) FMA peaks of the current device in TFLOP/s, measured (gb2d_alu_peaks)."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = library().gb2d_alu_peaks(ctypes.byref(a), ctypes.byref(b))
+    if rc:
+        raise RuntimeError(f"gb2d_alu_peaks failed ({rc})")
+    return a.value, b.value
 
 
 def check_exact_division(n, seed=1):

@@ -28,6 +28,7 @@ UNITS = {
     "gb2d_noalloc.cu": [],
     "gb2d_adjoint.cu": [],
     "gb2d_batch.cu": [],
+    "gb2d_peaks.cu": [],
 }
 
 

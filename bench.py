@@ -67,6 +67,15 @@ def barrier(dist):
         dist.barrier()
 
 
+# Flops per node of one WENO5 advection sweep and one reinitialisation sweep in the
+# reference's arithmetic (ADVECTION_METHOD_2D.h:508-663, 1401-1658): per one-sided
+# derivative 5 differences (10), smoothness indicators (33), weights (17), the three
+# candidate stencils and their blend (20); four of them per node in both sweeps.
+LS_ADVECT_FLOPS = 4 * 80 + 4 + 5 + 3
+LS_REINIT_FLOPS = 4 * 80 + 4 + 9 + 3
+REINIT_SWEEPS = 25
+
+
 def shard(n, rank, ws):
     """Instances of a batch that one rank runs: a host-side partition, no communication."""
     return [k for k in range(n) if k % ws == rank]
@@ -360,6 +369,7 @@ def run_gb300(args):
 
     mixed = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=TOL)
     fp64 = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=TOL)
+    alu_fp64, alu_fp32 = gb.alu_peaks()  # measured FMA peaks, outside every timed region
     cm = setup(gb.PRECISION_MIXED)
     c64 = setup(gb.PRECISION_FP64)
     timed(cm, mixed, 0, args.warmup)
@@ -435,6 +445,23 @@ def run_gb300(args):
                 ts.append(e0.elapsed_time(e1))
         levelset[name + "_rk3_ms"] = statistics.median(ts)
         cl.close()
+    # Roofline of the level-set step: both bounds, from the reference's arithmetic and
+    # arrays per node (one WENO5 advection sweep: 4 one-sided WENO5 derivatives of 80
+    # flops, velocity averages, update, RK blend = 332 flops, reads phi, U, V and writes
+    # phi = 32 B; one reinitialisation sweep: the same derivatives, Godunov selection and
+    # update, RK blend = 336 flops, reads phi, S and writes phi = 24 B; a step = 3 + 75).
+    ls_flops = (3 * LS_ADVECT_FLOPS + 3 * REINIT_SWEEPS * LS_REINIT_FLOPS) * float(N * N)
+    ls_bytes = (3 * 32 + 3 * REINIT_SWEEPS * 24) * float(N * N)
+    roof_ls = {"kernels": "level-set TVD-RK3 + reinit TVD-RK3 step at 1024^2 (3 WENO5 advection sweeps, 75 reinit sweeps)",
+               "flops_per_node": ls_flops / (N * N), "bytes_per_node": ls_bytes / (N * N),
+               "alu_peaks_tflops": {"fp64": alu_fp64, "fp32": alu_fp32, "source": "measured (gb2d_alu_peaks, FMA chains)"}}
+    peak_hbm, _ = measured_peaks()
+    for name, key, alu in (("fp64_exact", "fp64_exact_rk3_ms", alu_fp64), ("fp32_flux", "fp32_flux_rk3_ms", alu_fp32)):
+        sec = levelset[key] * 1e-3
+        tf, gbs = ls_flops / sec / 1e12, ls_bytes / sec / 1e9
+        roof_ls[name] = {"ms": levelset[key], "achieved_tflops": tf, "alu_peak_tflops": alu, "alu_frac": tf / alu,
+                         "achieved_gbs": gbs, "hbm_frac": gbs / peak_hbm,
+                         "bound": "alu" if tf / alu >= gbs / peak_hbm else "hbm"}
 
     # One whole time step of the same workload (not part of the metric): level-set and
     # reinit RK3, then three SolveForRK stages (ENO3 velocity advection, gravity +
@@ -496,7 +523,8 @@ def run_gb300(args):
                    "rel_residual_mixed": st_m.rel_residual,
                    "fp64_mgpcg_ms": statistics.mean(ms_64), "iterations_fp64": statistics.mean(it_64), "rel_residual_fp64": st_64.rel_residual,
                    "mixed_vs_fp64_rel_l2_p": diff, "replicas": ws,
-                   "levelset_rk3_1024": levelset, "time_step_1024": time_step, "batched_rising_bubbles": batch,
+                   "levelset_rk3_1024": levelset, "roofline_levelset": roof_ls, "time_step_1024": time_step,
+                   "batched_rising_bubbles": batch,
                    "rayleigh_taylor_2048": rt},
         "clocks": clk,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

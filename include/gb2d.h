@@ -137,14 +137,19 @@ int gb2d_synchronize(gb2d_ctx* ctx);
 int gb2d_set_stream(gb2d_ctx* ctx, void* stream);
 
 /* Kernel probe for roofline measurement: while enabled, the pressure solver
- * brackets every launch of its finest-level smoother (one red-black half sweep)
- * with CUDA events on the context stream.  gb2d_probe_read returns the launches
+ * brackets every launch of its finest-level smoother (one launch = every red-black
+ * sweep of one side of the V-cycle) with CUDA events on the context stream.  gb2d_probe_read returns the launches
  * seen, their summed event time and the algorithmic bytes of one launch
  * (every array the half sweep must read or write, once). */
 int gb2d_probe_enable(gb2d_ctx* ctx, int enable);
 int gb2d_probe_read(gb2d_ctx* ctx, int* launches, double* total_ms, double* bytes_per_launch);
 /* Kernels this library has launched in this process so far (all contexts). */
 int gb2d_kernel_launches(unsigned long long* count);
+/* Arithmetic peaks of the current device in TFLOP/s (2 flops per FMA), measured by
+ * timing independent FMA chains on every SM (about 0.1 s in total on a GB300): the
+ * denominators of the ALU roofline of the WENO5 and reinitialisation sweeps.
+ * GB2D_ERR_CUDA if a launch fails, GB2D_ERR_NO_DEVICE without a device. */
+int gb2d_alu_peaks(double* fp64_tflops, double* fp32_tflops);
 
 /* Self-check of the exact FP64 division by 3 and 6 used in the WENO5 kernels
  * (three FP64 operations instead of a division): compares it bit for bit with
