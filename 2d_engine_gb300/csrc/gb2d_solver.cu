@@ -970,9 +970,11 @@ bool plan_ctail(Hierarchy<T>& H, int P) {
   H.ctail = -1;
   if (P < 2 || P > kClusterMax) return false;
   const int nl = H.nlev;
+  const char* env = getenv("GB2D_CTAIL_TOP_CELLS");  // tuning override of kCtMaxTopCells
+  const long top_cells = env && atol(env) > 0 ? atol(env) : kCtMaxTopCells;
   for (int top = 0; top < nl - 1; ++top) {
     if (nl - top > kCtMaxLevels) continue;
-    if (H.L[top].nI * H.L[top].nJ > kCtMaxTopCells) continue;
+    if ((long)H.L[top].nI * H.L[top].nJ > top_cells) continue;
     int lb = top - 1;
     while (lb + 1 < nl - 1 && H.L[lb + 1].nJ >= P * kCtMinRows) ++lb;
     if (lb < top || H.L[lb].nJ > kCtOwnerRows) continue;

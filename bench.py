@@ -504,6 +504,20 @@ def run_gb300(args):
     achieved = (probe_bytes / (probe_ms / nprobe * 1e-3) / 1e9) if nprobe else None
     traffic = ncu_traffic_per_launch()
 
+    # Whole-projection roofline from the per-node algorithmic bytes of the path (every array
+    # a pass must read or write, once, at its storage width): setup (phi, U, V in; the face
+    # weights, b, kappa out) 64 B; each FP64 true-residual pass 40 B (one before the CG, one
+    # to confirm it); per CG iteration the FP64 vector work 13 x 8 B plus one V(2,2) cycle,
+    # (4/3) [5 s (2 + 2) + 6.5 s] with s the preconditioner's storage width.
+    def projection_bytes_per_node(iters, s):
+        return 64 + 2 * 40 + iters * (13 * 8 + (4.0 / 3.0) * (5 * s * 4 + 6.5 * s))
+    roof_proj = {"formula": "64 + 2*40 + iterations * (104 + (4/3)*(26 s)) B per node; s = 4 (mixed), 8 (FP64)",
+                 "peak_gbs": peak}
+    for name, its, ms_, s_w in (("mixed", statistics.mean(it_m), ms_step, 4), ("fp64", statistics.mean(it_64), statistics.mean(ms_64), 8)):
+        bpn = projection_bytes_per_node(its, s_w)
+        gbs = bpn * N * N / (ms_ * 1e-3) / 1e9
+        roof_proj[name] = {"iterations": its, "bytes_per_node": bpn, "ms": ms_, "achieved_gbs": gbs, "frac": gbs / peak}
+
     if rank != 0:
         return
     full = ref_full_iterations()
@@ -523,7 +537,8 @@ def run_gb300(args):
                    "rel_residual_mixed": st_m.rel_residual,
                    "fp64_mgpcg_ms": statistics.mean(ms_64), "iterations_fp64": statistics.mean(it_64), "rel_residual_fp64": st_64.rel_residual,
                    "mixed_vs_fp64_rel_l2_p": diff, "replicas": ws,
-                   "levelset_rk3_1024": levelset, "roofline_levelset": roof_ls, "time_step_1024": time_step,
+                   "roofline_projection": roof_proj, "levelset_rk3_1024": levelset, "roofline_levelset": roof_ls,
+                   "time_step_1024": time_step,
                    "batched_rising_bubbles": batch,
                    "rayleigh_taylor_2048": rt},
         "clocks": clk,
