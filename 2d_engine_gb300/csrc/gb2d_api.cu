@@ -142,6 +142,9 @@ void free_ctx(gb2d_ctx* c) {
   if (c->side) cudaStreamDestroy(c->side);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->side2) cudaStreamDestroy(c->side2);
+  if (c->ev_fork2) cudaEventDestroy(c->ev_fork2);
+  if (c->ev_join2) cudaEventDestroy(c->ev_join2);
   delete c;
 }
 
@@ -188,6 +191,9 @@ int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming);
   struct A {
     double** p;
     size_t n;
@@ -478,8 +484,10 @@ int gb2d_curvature(gb2d_ctx* c) {
 }
 
 // Curvature and the jump-system assembly: the curvature runs on the side stream
-// while the face weights (which do not need it) run on the context stream.
-static int curvature_and_assemble(gb2d_ctx* c, double dt) {
+// while the face weights and the diagonal (which do not need it) run on the context
+// stream; with solve options, the solver's FP32 hierarchy then starts building from
+// them on a third stream, and the right-hand side follows the curvature.
+static int curvature_and_assemble(gb2d_ctx* c, double dt, const gb2d_solve_opts* prebuild) {
   double* phi = c->phi_buf[c->phi_cur];
   GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->flag, 0, sizeof(int), c->stream));
   launch_extrapolate_ghosts(c->stream, phi, 2, c->grid.ni, c->grid.nj);
@@ -488,16 +496,21 @@ static int curvature_and_assemble(gb2d_ctx* c, double dt) {
   launch_curvature(c->side, c, phi, c->kappa, &c->sc->flag);
   GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_join, c->side));
   launch_faces(c->stream, c, phi, dt);
+  launch_diag(c->stream, c, dt);
+  if (prebuild) solver_prebuild(c, prebuild);
   GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
-  launch_rhs_diag(c->stream, c, phi, dt);
+  launch_rhs(c->stream, c, phi, dt);
   return check_launch(c, "assemble");
 }
 
 int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
   if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
   double* phi = c->phi_buf[c->phi_cur];
-  int rc = curvature_and_assemble(c, dt);
-  if (rc) return rc;
+  int rc = curvature_and_assemble(c, dt, o);
+  if (rc) {
+    solver_drop_prebuild(c);
+    return rc;
+  }
   gb2d_solve_stats local;
   memset(&local, 0, sizeof local);
   int src = solver_solve(c, c->rhs, c->p, o, &local);
@@ -696,7 +709,7 @@ int gb2d_projection_density_gradient(gb2d_ctx* c, double dt, double* d_water_den
 
 int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {
   if (!c || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
-  int rc = curvature_and_assemble(c, dt);
+  int rc = curvature_and_assemble(c, dt, nullptr);
   if (rc) return rc;
   size_t ni = c->grid.ni, nj = c->grid.nj;
   if (bx) GB2D_CUDA_TRY(c, cudaMemcpyAsync(bx, c->bx, (ni + 1) * nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

@@ -408,13 +408,10 @@ __device__ __forceinline__ double arm_flux(double pc, double pn, double jcc, con
   return 0.0;
 }
 
-// Diagonal (dx^2 only, POISSON_SOLVER.cpp:872) and right-hand side -div - F_X - F_Y.
-__global__ void k_rhs_diag(const double* __restrict__ phi_a, const double* __restrict__ kappa, const double* __restrict__ u_a,
-                           const double* __restrict__ v_a, const double* __restrict__ bx, const double* __restrict__ by, double* __restrict__ diag,
-                           double* __restrict__ rhs, AsmArgs a) {
+// Diagonal (dx^2 only, POISSON_SOLVER.cpp:872): the face weights of the FULL arms and
+// the first cell's Neumann arms (the corner pin).
+__global__ void k_diag(const double* __restrict__ bx, const double* __restrict__ by, double* __restrict__ diag, AsmArgs a) {
   int ni = a.ni, nj = a.nj;
-  DField phi = dfield((double*)phi_a, 2, ni, nj);
-  DField u = dfield((double*)u_a, 2, ni + 1, nj), v = dfield((double*)v_a, 2, ni, nj + 1);
   GB_FOR_IJ(i, j, ni, nj) {
     const size_t t = (size_t)j * ni + i;
     double bl = bx[i + (size_t)j * (ni + 1)], br = bx[i + 1 + (size_t)j * (ni + 1)];
@@ -432,7 +429,20 @@ __global__ void k_rhs_diag(const double* __restrict__ phi_a, const double* __res
     }
     if ((__double_as_longlong(coef) & kAbsBits) == 0) coef = 1;  // coef == 0
     diag[t] = a.inv_dxdx * coef;
+  }
+}
 
+// Right-hand side -div - F_X - F_Y (POISSON_SOLVER.cpp:878-948).
+__global__ void k_rhs(const double* __restrict__ phi_a, const double* __restrict__ kappa, const double* __restrict__ u_a,
+                      const double* __restrict__ v_a, const double* __restrict__ bx, const double* __restrict__ by, double* __restrict__ rhs,
+                      AsmArgs a) {
+  int ni = a.ni, nj = a.nj;
+  DField phi = dfield((double*)phi_a, 2, ni, nj);
+  DField u = dfield((double*)u_a, 2, ni + 1, nj), v = dfield((double*)v_a, 2, ni, nj + 1);
+  GB_FOR_IJ(i, j, ni, nj) {
+    const size_t t = (size_t)j * ni + i;
+    double bl = bx[i + (size_t)j * (ni + 1)], br = bx[i + 1 + (size_t)j * (ni + 1)];
+    double bb = by[i + (size_t)j * ni], bt = by[i + (size_t)(j + 1) * ni];
     double pc = GB_AT(phi, i, j);
     double jcc = jc_at(kappa, i, j, a);
     double FL = arm_flux(pc, GB_AT(phi, i - 1, j), jcc, kappa, i - 1, j, bl, a.s.odx2, a);
@@ -721,10 +731,17 @@ void launch_faces(cudaStream_t s, const gb2d_ctx* c, const double* phi, double d
   GB_LAUNCHED(1);
 }
 
-// Needs the face weights and the curvature.
-void launch_rhs_diag(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt) {
+// Needs the face weights.
+void launch_diag(cudaStream_t s, const gb2d_ctx* c, double dt) {
   AsmArgs a = asm_args(c, dt);
-  k_rhs_diag<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, c->kappa, c->u, c->v, c->bx, c->by, c->diag, c->rhs, a);
+  k_diag<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, a);
+  GB_LAUNCHED(1);
+}
+
+// Needs the face weights and the curvature.
+void launch_rhs(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt) {
+  AsmArgs a = asm_args(c, dt);
+  k_rhs<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, c->kappa, c->u, c->v, c->bx, c->by, c->rhs, a);
   GB_LAUNCHED(1);
 }
 

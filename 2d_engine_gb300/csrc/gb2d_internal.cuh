@@ -139,6 +139,8 @@ struct gb2d_ctx {
   cudaStream_t own_stream;
   cudaStream_t side;              // second stream for independent setup branches
   cudaEvent_t ev_fork, ev_join;   // fork / join of the side stream
+  cudaStream_t side2;             // third stream: the preconditioner hierarchy built during the assembly
+  cudaEvent_t ev_fork2, ev_join2;
   gb2d::Probe probe;
   // Level-set buffers (ghost 2): current index into phi_buf.
   double* phi_buf[4];
@@ -183,7 +185,8 @@ void launch_blend(cudaStream_t s, const gb2d_ctx* c, const double* keep, double*
 void launch_eno3(cudaStream_t s, const gb2d_ctx* c, double dt);
 void launch_curvature(cudaStream_t s, const gb2d_ctx* c, const double* phi, double* kappa, int* flag);
 void launch_faces(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt);
-void launch_rhs_diag(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt);
+void launch_diag(cudaStream_t s, const gb2d_ctx* c, double dt);
+void launch_rhs(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt);
 void launch_poisson_apply_exact(cudaStream_t s, const gb2d_ctx* c, const double* x, double* y);
 void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt, Scalars* sc);
 void launch_copy_interior(cudaStream_t s, const double* src, int gs, double* dst, int gd, int nI, int nJ);
@@ -223,6 +226,12 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen);
 void solver_destroy(Solver* s);
 // Solve A x = rhs (system held in ctx->bx/by/diag) with x (ni x nj, FP64, compact) as warm start.
 int solver_solve(gb2d_ctx* c, const double* rhs, double* x, const gb2d_solve_opts* o, gb2d_solve_stats* st);
+// With o's mixed-precision MG-PCG: start building the FP32 preconditioner hierarchy from
+// ctx->bx/by/diag (complete on ctx->stream) on ctx->side2; the next solver_solve joins it
+// instead of building it.  Other options: no-op.
+void solver_prebuild(gb2d_ctx* c, const gb2d_solve_opts* o);
+// Abandon a started prebuild (an error before the solve): ctx->stream waits for it.
+void solver_drop_prebuild(gb2d_ctx* c);
 void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, int* cluster_ctas);
 
 }  // namespace gb2d

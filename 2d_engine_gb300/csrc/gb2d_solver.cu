@@ -882,6 +882,7 @@ struct Solver {
   Scalars* sc = nullptr;
   int G = 0;               // blocks of the grid-stride CG kernels
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  bool prebuilt32 = false;  // the FP32 hierarchy is building on ctx->side2 (solver_prebuild)
   // Graphs per (precision, solver, smoothing sweeps) and the x they update.
   GraphSet graphs[2][2][3];
   double* graph_x[2][2][3] = {};
@@ -1534,6 +1535,23 @@ void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, in
   }
 }
 
+void solver_prebuild(gb2d_ctx* c, const gb2d_solve_opts* o) {
+  Solver* S = c->solver;
+  if (!S || o->solver != GB2D_SOLVER_MGPCG || o->precision != GB2D_PRECISION_MIXED) return;
+  cudaEventRecord(c->ev_fork2, c->stream);
+  cudaStreamWaitEvent(c->side2, c->ev_fork2, 0);
+  build_hierarchy<float>(c->side2, S->h32, c, nullptr, S->ainv32);
+  cudaEventRecord(c->ev_join2, c->side2);
+  S->prebuilt32 = true;
+}
+
+void solver_drop_prebuild(gb2d_ctx* c) {
+  Solver* S = c->solver;
+  if (!S || !S->prebuilt32) return;
+  cudaStreamWaitEvent(c->stream, c->ev_join2, 0);  // later builds on the side stream follow it
+  S->prebuilt32 = false;
+}
+
 // x: padded FP64 solution (warm start in, result out); the system is ctx->bx/by/diag/rhs.
 // FP64 CG throughout; the preconditioner runs in FP64 or, for
 // GB2D_PRECISION_MIXED, in FP32.  The loop around the CG recomputes the true
@@ -1551,11 +1569,10 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
   double* P_rr = slot(S, kSlotRr);
   double* P_bb = slot(S, kSlotBb);
 
-  if (prec || !use_mg)
-    build_level0_f64(s, S->h64, c, S->b64);
-  else
-    build_hierarchy<double>(s, S->h64, c, S->b64, S->ainv64);
-  if (prec && use_mg) {
+  cudaEvent_t join_ev = c->ev_join;
+  if (prec && use_mg && S->prebuilt32) {
+    join_ev = c->ev_join2;  // started by solver_prebuild during the assembly
+  } else if (prec && use_mg) {
     // The FP32 hierarchy (its dense coarse inverse keeps one SM busy) builds on
     // the side stream while the FP64 residual runs; joined before the first V-cycle.
     cudaEventRecord(c->ev_fork, s);
@@ -1563,6 +1580,11 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
     build_hierarchy<float>(c->side, S->h32, c, nullptr, S->ainv32);
     cudaEventRecord(c->ev_join, c->side);
   }
+  S->prebuilt32 = false;
+  if (prec || !use_mg)
+    build_level0_f64(s, S->h64, c, S->b64);
+  else
+    build_hierarchy<double>(s, S->h64, c, S->b64, S->ainv64);
   bool joined = !(prec && use_mg);
   if (prec && !use_mg) {
     double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
@@ -1602,7 +1624,7 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
     double rr_in = rr;
     int it;
     if (!joined) {
-      cudaStreamWaitEvent(s, c->ev_join, 0);
+      cudaStreamWaitEvent(s, join_ev, 0);
       joined = true;
     }
     if (prec)
@@ -1622,7 +1644,7 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
       break;
     }
   }
-  if (!joined) cudaStreamWaitEvent(s, c->ev_join, 0);  // later work on the context stream follows the side build
+  if (!joined) cudaStreamWaitEvent(s, join_ev, 0);  // later work on the context stream follows the side build
   if (st) {
     st->iterations = total;
     st->outer_iterations = outer;
