@@ -111,6 +111,7 @@ def library():
         "gb2d_batch_advance": [vp, i, d, vp, O, ctypes.POINTER(BatchStatsT)],
         "gb2d_jump_poisson_solve": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, O, S],
         "gb2d_projection_density_gradient": [vp, d, ctypes.POINTER(d), ctypes.POINTER(d)],
+        "gb2d_projection_host": [vp, d, O, vp, vp, vp, vp, vp, vp, vp, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
         "gb2d_poisson_solve": [vp, vp, vp, O, S],
@@ -278,6 +279,30 @@ class Context:
         opts = opts or solve_opts()
         st = SolveStatsT()
         rc = self.L.gb2d_projection(self.h, dt, ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return st
+
+    def projection_host(self, dt, opts=None, phi=None, u=None, v=None, p=None, p_out=None, u_out=None, v_out=None,
+                        allow_max_iters=False):
+        """gb2d_projection_host: the projection with its inputs copied in from, and its outputs
+        copied out to, host arrays (float64, C-contiguous, the field shapes; None = skip),
+        the copies overlapping the assembly and the velocity update."""
+        opts = opts or solve_opts()
+        st = SolveStatsT()
+        ins = []
+        for f, a in ((FIELD_PHI, phi), (FIELD_U, u), (FIELD_V, v), (FIELD_P, p)):
+            if a is not None:
+                a = np.ascontiguousarray(a, dtype=np.float64)
+                if a.shape != self.shape(f):
+                    raise ValueError(f"field {f}: expected shape {self.shape(f)}, got {a.shape}")
+            ins.append(a)
+        for f, a in ((FIELD_P, p_out), (FIELD_U, u_out), (FIELD_V, v_out)):
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != self.shape(f)):
+                raise ValueError(f"field {f}: output must be float64, C-contiguous, shape {self.shape(f)}")
+        ptr = lambda a: _ptr(a) if a is not None else None
+        rc = self.L.gb2d_projection_host(self.h, dt, ctypes.byref(opts), *[ptr(a) for a in ins], ptr(p_out), ptr(u_out), ptr(v_out),
+                                         ctypes.byref(st))
         if rc != 0 and not (allow_max_iters and rc == -4):
             self._check(rc)
         return st

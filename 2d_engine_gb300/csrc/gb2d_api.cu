@@ -145,6 +145,9 @@ void free_ctx(gb2d_ctx* c) {
   if (c->side2) cudaStreamDestroy(c->side2);
   if (c->ev_fork2) cudaEventDestroy(c->ev_fork2);
   if (c->ev_join2) cudaEventDestroy(c->ev_join2);
+  if (c->xfer) cudaStreamDestroy(c->xfer);
+  if (c->ev_xfer0) cudaEventDestroy(c->ev_xfer0);
+  if (c->ev_xfer) cudaEventDestroy(c->ev_xfer);
   delete c;
 }
 
@@ -194,6 +197,9 @@ int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_xfer0, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_xfer, cudaEventDisableTiming);
   struct A {
     double** p;
     size_t n;
@@ -487,7 +493,7 @@ int gb2d_curvature(gb2d_ctx* c) {
 // while the face weights and the diagonal (which do not need it) run on the context
 // stream; with solve options, the solver's FP32 hierarchy then starts building from
 // them on a third stream, and the right-hand side follows the curvature.
-static int curvature_and_assemble(gb2d_ctx* c, double dt, const gb2d_solve_opts* prebuild) {
+static int curvature_and_assemble(gb2d_ctx* c, double dt, const gb2d_solve_opts* prebuild, cudaEvent_t inputs = nullptr) {
   double* phi = c->phi_buf[c->phi_cur];
   GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->flag, 0, sizeof(int), c->stream));
   launch_extrapolate_ghosts(c->stream, phi, 2, c->grid.ni, c->grid.nj);
@@ -499,14 +505,39 @@ static int curvature_and_assemble(gb2d_ctx* c, double dt, const gb2d_solve_opts*
   launch_diag(c->stream, c, dt);
   if (prebuild) solver_prebuild(c, prebuild);
   GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+  if (inputs) GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->stream, inputs, 0));  // U, V (and p) copied in
   launch_rhs(c->stream, c, phi, dt);
   return check_launch(c, "assemble");
 }
 
-int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
-  if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
+// Host buffers of gb2d_projection_host (null: the context's field as it is / not copied out).
+struct HostIO {
+  const double *phi, *u, *v, *p;
+  double *p_out, *u_out, *v_out;
+};
+
+static size_t field_bytes(const gb2d_ctx* c, int field) {
+  FieldDesc d;
+  return field_desc(&c->grid, field, &d) ? field_count(d) * sizeof(double) : 0;
+}
+
+static int projection_run(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve_stats* st, const HostIO* io) {
   double* phi = c->phi_buf[c->phi_cur];
-  int rc = curvature_and_assemble(c, dt, o);
+  cudaEvent_t inputs = nullptr;
+  if (io && io->phi)
+    GB2D_CUDA_TRY(c, cudaMemcpyAsync(phi, io->phi, field_bytes(c, GB2D_FIELD_PHI), cudaMemcpyHostToDevice, c->stream));
+  if (io && (io->u || io->v || io->p)) {
+    // U, V and the warm-start p stream in beside the curvature, face weights and
+    // diagonal, which need phi only; the right-hand side waits for them.
+    GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_xfer0, c->stream));
+    GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->xfer, c->ev_xfer0, 0));
+    if (io->u) GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->u, io->u, field_bytes(c, GB2D_FIELD_U), cudaMemcpyHostToDevice, c->xfer));
+    if (io->v) GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->v, io->v, field_bytes(c, GB2D_FIELD_V), cudaMemcpyHostToDevice, c->xfer));
+    if (io->p) GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->p, io->p, field_bytes(c, GB2D_FIELD_P), cudaMemcpyHostToDevice, c->xfer));
+    GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_xfer, c->xfer));
+    inputs = c->ev_xfer;
+  }
+  int rc = curvature_and_assemble(c, dt, o, inputs);
   if (rc) {
     solver_drop_prebuild(c);
     return rc;
@@ -515,8 +546,20 @@ int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve
   memset(&local, 0, sizeof local);
   int src = solver_solve(c, c->rhs, c->p, o, &local);
   if (src != GB2D_OK && src != GB2D_ERR_MAX_ITERS) return src;
+  const bool p_out = io && io->p_out;
+  if (p_out) {  // p is final: it streams out while the velocity update runs
+    GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_xfer0, c->stream));
+    GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->xfer, c->ev_xfer0, 0));
+    GB2D_CUDA_TRY(c, cudaMemcpyAsync(io->p_out, c->p, field_bytes(c, GB2D_FIELD_P), cudaMemcpyDeviceToHost, c->xfer));
+    GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_xfer, c->xfer));
+  }
   GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->maxu_bits, 0, 2 * sizeof(unsigned long long), c->stream));
   launch_velocity_update(c->stream, c, phi, dt, c->sc);
+  if (io && io->u_out)
+    GB2D_CUDA_TRY(c, cudaMemcpyAsync(io->u_out, c->u, field_bytes(c, GB2D_FIELD_U), cudaMemcpyDeviceToHost, c->stream));
+  if (io && io->v_out)
+    GB2D_CUDA_TRY(c, cudaMemcpyAsync(io->v_out, c->v, field_bytes(c, GB2D_FIELD_V), cudaMemcpyDeviceToHost, c->stream));
+  if (p_out) GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_xfer, 0));
   if ((rc = read_flag(c))) return rc;
   const Scalars* h = (const Scalars*)c->host_stage;
   double mu, mv;
@@ -526,6 +569,18 @@ int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve
   local.max_velocity_y = mv;
   if (st) *st = local;
   return src;
+}
+
+int gb2d_projection(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d_solve_stats* st) {
+  if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
+  return projection_run(c, dt, o, st, nullptr);
+}
+
+int gb2d_projection_host(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, const double* phi, const double* u, const double* v,
+                         const double* p, double* p_out, double* u_out, double* v_out, gb2d_solve_stats* st) {
+  if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
+  const HostIO io{phi, u, v, p, p_out, u_out, v_out};
+  return projection_run(c, dt, o, st, &io);
 }
 
 int gb2d_set_flow_params(gb2d_ctx* c, const gb2d_flow_params* f) {

@@ -141,6 +141,8 @@ struct gb2d_ctx {
   cudaEvent_t ev_fork, ev_join;   // fork / join of the side stream
   cudaStream_t side2;             // third stream: the preconditioner hierarchy built during the assembly
   cudaEvent_t ev_fork2, ev_join2;
+  cudaStream_t xfer;              // host copies that overlap the projection (gb2d_projection_host)
+  cudaEvent_t ev_xfer0, ev_xfer;
   gb2d::Probe probe;
   // Level-set buffers (ghost 2): current index into phi_buf.
   double* phi_buf[4];

@@ -397,29 +397,40 @@ def run_gb300(args):
     p_64 = c64.get(gb.FIELD_P)
     diff = float(np.linalg.norm(p_mixed - p_64) / np.linalg.norm(p_64))
 
-    # End to end through the C ABI with host buffers: H2D of the step's inputs, the
-    # projection, D2H of p, u, v, all inside the timed region.
+    # End to end through the C ABI with host buffers: one gb2d_projection_host call per
+    # step copies the step's inputs (phi, U, V, warm-start p) in from page-locked host
+    # memory, projects, and copies p, U, V out; all of it inside the timed region.
     pin = {k: torch.from_numpy(np.ascontiguousarray(case[k])).pin_memory().numpy() for k in ("phi", "u", "v", "p")}
     out = {k: torch.empty(case[k].shape, dtype=torch.float64).pin_memory().numpy() for k in ("p", "u", "v")}
     h2d = sum(pin[k].nbytes for k in pin)
     d2h = sum(out[k].nbytes for k in out)
-    e2e, e2e_h2d, e2e_d2h = [], [], []
+    e2e = []
     for step in range(args.warmup + args.steps):
         with torch.cuda.stream(stream):
             flush.zero_()
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            cm.projection_host(dt, mixed, phi=pin["phi"], u=pin["u"], v=pin["v"], p=pin["p"], p_out=out["p"], u_out=out["u"],
+                               v_out=out["v"])
+            e1.record(stream)
+        e1.synchronize()
+        if step >= args.warmup:
+            e2e.append(e0.elapsed_time(e1))
+    # The machine's host-link throughput for the same copies made one by one (not timed as
+    # e2e): blocking gb2d_set_field / gb2d_get_field calls of the four inputs and three
+    # outputs, so that e2e can be read against the copy cost it overlaps.
+    e2e_h2d, e2e_d2h = [], []
+    for step in range(3):
+        with torch.cuda.stream(stream):
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
             ev[0].record(stream)
             cm.set(gb.FIELD_PHI, pin["phi"]); cm.set(gb.FIELD_U, pin["u"]); cm.set(gb.FIELD_V, pin["v"]); cm.set(gb.FIELD_P, pin["p"])
             ev[1].record(stream)
-            cm.projection(dt, mixed)
-            ev[2].record(stream)
             cm.get(gb.FIELD_P, out["p"]); cm.get(gb.FIELD_U, out["u"]); cm.get(gb.FIELD_V, out["v"])
-            ev[3].record(stream)
-        ev[3].synchronize()
-        if step >= args.warmup:
-            e2e.append(ev[0].elapsed_time(ev[3]))
-            e2e_h2d.append(ev[0].elapsed_time(ev[1]))
-            e2e_d2h.append(ev[2].elapsed_time(ev[3]))
+            ev[2].record(stream)
+        ev[2].synchronize()
+        e2e_h2d.append(ev[0].elapsed_time(ev[1]))
+        e2e_d2h.append(ev[1].elapsed_time(ev[2]))
 
     # Level-set path of the same workload (not part of the metric): one level-set
     # TVD-RK3 step with its reinitialisation (3 WENO5 sweeps + 3 x 25 reinit sweeps),
@@ -511,7 +522,7 @@ def run_gb300(args):
     # (4/3) [5 s (2 + 2) + 6.5 s] with s the preconditioner's storage width.
     def projection_bytes_per_node(iters, s):
         return 64 + 2 * 40 + iters * (13 * 8 + (4.0 / 3.0) * (5 * s * 4 + 6.5 * s))
-    roof_proj = {"formula": "64 + 2*40 + iterations * (104 + (4/3)*(26 s)) B per node; s = 4 (mixed), 8 (FP64)",
+    roof_proj = {"formula": "64 + 2*40 + iterations * (104 + (4/3)*(26.5 s)) B per node; s = 4 (mixed), 8 (FP64)",
                  "peak_gbs": peak}
     for name, its, ms_, s_w in (("mixed", statistics.mean(it_m), ms_step, 4), ("fp64", statistics.mean(it_64), statistics.mean(ms_64), 8)):
         bpn = projection_bytes_per_node(its, s_w)
@@ -543,8 +554,10 @@ def run_gb300(args):
                    "rayleigh_taylor_2048": rt},
         "clocks": clk,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "h2d_ms": statistics.mean(e2e_h2d), "d2h_ms": statistics.mean(e2e_d2h),
-                "h2d_gbs": h2d / statistics.mean(e2e_h2d) / 1e6, "d2h_gbs": d2h / statistics.mean(e2e_d2h) / 1e6},
+                "call": "gb2d_projection_host (page-locked host buffers; copies overlap the assembly and the velocity update)",
+                "separate_copies": {"h2d_ms": statistics.median(e2e_h2d), "d2h_ms": statistics.median(e2e_d2h),
+                                    "h2d_gbs": h2d / statistics.median(e2e_h2d) / 1e6,
+                                    "d2h_gbs": d2h / statistics.median(e2e_d2h) / 1e6}},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "finest-level smoothing launch (k_pre_smooth / k_post_smooth: two red-black sweeps each, FP32)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,

@@ -191,6 +191,16 @@ int gb2d_curvature(gb2d_ctx* ctx);
 /* One PROJECTION_2D::Solve(dt): density, divergence, sigma*kappa jump, matrix-free
  * ghost-fluid Poisson system, solve (P is the warm start), GFM velocity update (a9-a14). */
 int gb2d_projection(gb2d_ctx* ctx, double dt, const gb2d_solve_opts* opts, gb2d_solve_stats* stats);
+/* gb2d_projection on a state held in host memory: copies PHI, U, V and the warm-start P
+ * in, projects, and copies P, U, V out, in the ghost-inclusive layouts of gb2d_set_field
+ * (a null input keeps the context's field, a null output is not copied).  One call
+ * instead of seven: U, V and P stream in on a copy stream while the curvature, face
+ * weights and diagonal compute from PHI, and P streams out while the velocity update
+ * runs.  Page-locked host buffers let the copies overlap; pageable ones work too.
+ * Returns when the outputs are in place, with gb2d_projection's status. */
+int gb2d_projection_host(gb2d_ctx* ctx, double dt, const gb2d_solve_opts* opts, const double* phi, const double* u,
+                         const double* v, const double* p, double* p_out, double* u_out, double* v_out,
+                         gb2d_solve_stats* stats);
 
 /* Flow constants for the stages below (see gb2d_flow_params). */
 int gb2d_set_flow_params(gb2d_ctx* ctx, const gb2d_flow_params* flow);

@@ -66,6 +66,14 @@ class GB2D_FLUID_STEP {
     if (thread_id == 0) Solved(gb2d_projection(ctx_, dt, &solve_, &stats_), "Projection");
     Sync(thread_id);
   }
+  // Projection(dt, thread_id) on a state kept in the reference's own host arrays (the
+  // array_for_this.values of the level set, the two MAC velocity fields and the pressure):
+  // phi, U, V and the warm-start p go in, and the projected U, V and p come back in place,
+  // in one call whose copies overlap the GPU work (gb2d_projection_host).
+  void ProjectionOnHost(const double& dt, const int& thread_id, const double* phi, double* u, double* v, double* p) {
+    if (thread_id == 0) Solved(gb2d_projection_host(ctx_, dt, &solve_, phi, u, v, p, p, u, v, &stats_), "Projection");
+    Sync(thread_id);
+  }
 
   // Constants of gravity, viscosity and the CFL time step (gb2d_flow_params).
   void SetFlowParams(const gb2d_flow_params& flow) { Check(gb2d_set_flow_params(ctx_, &flow), "gb2d_set_flow_params"); }
