@@ -145,6 +145,7 @@ void free_ctx(gb2d_ctx* c) {
   if (c->side2) cudaStreamDestroy(c->side2);
   if (c->ev_fork2) cudaEventDestroy(c->ev_fork2);
   if (c->ev_join2) cudaEventDestroy(c->ev_join2);
+  if (c->ev_pre0) cudaEventDestroy(c->ev_pre0);
   if (c->xfer) cudaStreamDestroy(c->xfer);
   if (c->ev_xfer0) cudaEventDestroy(c->ev_xfer0);
   if (c->ev_xfer) cudaEventDestroy(c->ev_xfer);
@@ -197,6 +198,7 @@ int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side2, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_pre0, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_xfer0, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_xfer, cudaEventDisableTiming);

@@ -140,7 +140,7 @@ struct gb2d_ctx {
   cudaStream_t side;              // second stream for independent setup branches
   cudaEvent_t ev_fork, ev_join;   // fork / join of the side stream
   cudaStream_t side2;             // third stream: the preconditioner hierarchy built during the assembly
-  cudaEvent_t ev_fork2, ev_join2;
+  cudaEvent_t ev_fork2, ev_join2, ev_pre0;  // ev_pre0: the FP64 finest level is built
   cudaStream_t xfer;              // host copies that overlap the projection (gb2d_projection_host)
   cudaEvent_t ev_xfer0, ev_xfer;
   gb2d::Probe probe;
@@ -228,9 +228,10 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen);
 void solver_destroy(Solver* s);
 // Solve A x = rhs (system held in ctx->bx/by/diag) with x (ni x nj, FP64, compact) as warm start.
 int solver_solve(gb2d_ctx* c, const double* rhs, double* x, const gb2d_solve_opts* o, gb2d_solve_stats* st);
-// With o's mixed-precision MG-PCG: start building the FP32 preconditioner hierarchy from
-// ctx->bx/by/diag (complete on ctx->stream) on ctx->side2; the next solver_solve joins it
-// instead of building it.  Other options: no-op.
+// With MG-PCG options: start building the solver's levels from ctx->bx/by/diag (complete
+// on ctx->stream) on ctx->side2 (the FP64 finest level, then the FP32 hierarchy or the
+// FP64 coarse levels and dense inverse); the next solver_solve joins them instead of
+// building them.  Jacobi-PCG: no-op.
 void solver_prebuild(gb2d_ctx* c, const gb2d_solve_opts* o);
 // Abandon a started prebuild (an error before the solve): ctx->stream waits for it.
 void solver_drop_prebuild(gb2d_ctx* c);

@@ -882,7 +882,7 @@ struct Solver {
   Scalars* sc = nullptr;
   int G = 0;               // blocks of the grid-stride CG kernels
   cudaEvent_t ev[2] = {nullptr, nullptr};
-  bool prebuilt32 = false;  // the FP32 hierarchy is building on ctx->side2 (solver_prebuild)
+  bool prebuilt = false;  // the hierarchies are building on ctx->side2 (solver_prebuild)
   // Graphs per (precision, solver, smoothing sweeps) and the x they update.
   GraphSet graphs[2][2][3];
   double* graph_x[2][2][3] = {};
@@ -1120,17 +1120,22 @@ inline dim3 tiles(int nI, int nJ, int sh) {
 }
 
 template <typename T>
-void build_hierarchy(cudaStream_t s, Hierarchy<T>& H, const gb2d_ctx* c, double* b64, double* ainv) {
-  double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
-  Level<T>& L0 = H.L[0];
-  k_build_level0<T><<<grid_ij(L0.nI, L0.nJ), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, c->sys_shift, L0, b64, idx2, idy2);
-  GB_LAUNCHED(1);
+void build_coarse(cudaStream_t s, Hierarchy<T>& H, double* ainv) {
   for (int l = 1; l < H.nlev; ++l) {
     k_coarsen<T><<<grid_ij(H.L[l].nI, H.L[l].nJ), kThreads, 0, s>>>(H.L[l - 1], H.L[l]);
     GB_LAUNCHED(1);
   }
   k_dense_inverse<T><<<1, 1024, 0, s>>>(H.L[H.nlev - 1], ainv);
   GB_LAUNCHED(1);
+}
+
+template <typename T>
+void build_hierarchy(cudaStream_t s, Hierarchy<T>& H, const gb2d_ctx* c, double* b64, double* ainv) {
+  double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
+  Level<T>& L0 = H.L[0];
+  k_build_level0<T><<<grid_ij(L0.nI, L0.nJ), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, c->sys_shift, L0, b64, idx2, idy2);
+  GB_LAUNCHED(1);
+  build_coarse<T>(s, H, ainv);
 }
 
 // Only the finest FP64 level (the refinement residual's operator) and b.
@@ -1537,19 +1542,29 @@ void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, in
 
 void solver_prebuild(gb2d_ctx* c, const gb2d_solve_opts* o) {
   Solver* S = c->solver;
-  if (!S || o->solver != GB2D_SOLVER_MGPCG || o->precision != GB2D_PRECISION_MIXED) return;
+  if (!S || o->solver != GB2D_SOLVER_MGPCG) return;
   cudaEventRecord(c->ev_fork2, c->stream);
   cudaStreamWaitEvent(c->side2, c->ev_fork2, 0);
-  build_hierarchy<float>(c->side2, S->h32, c, nullptr, S->ainv32);
+  if (o->precision == GB2D_PRECISION_MIXED) {
+    // The FP32 hierarchy; the FP64 finest level stays on the context stream (it is
+    // short, and queued here it would delay the hierarchy the first V-cycle waits for).
+    build_hierarchy<float>(c->side2, S->h32, c, nullptr, S->ainv32);
+  } else {
+    // The FP64 finest level first (the residual waits for it; solver_solve copies its
+    // right-hand side once that exists), then the coarse levels and dense inverse.
+    build_level0_f64(c->side2, S->h64, c, nullptr);
+    cudaEventRecord(c->ev_pre0, c->side2);
+    build_coarse<double>(c->side2, S->h64, S->ainv64);
+  }
   cudaEventRecord(c->ev_join2, c->side2);
-  S->prebuilt32 = true;
+  S->prebuilt = true;
 }
 
 void solver_drop_prebuild(gb2d_ctx* c) {
   Solver* S = c->solver;
-  if (!S || !S->prebuilt32) return;
+  if (!S || !S->prebuilt) return;
   cudaStreamWaitEvent(c->stream, c->ev_join2, 0);  // later builds on the side stream follow it
-  S->prebuilt32 = false;
+  S->prebuilt = false;
 }
 
 // x: padded FP64 solution (warm start in, result out); the system is ctx->bx/by/diag/rhs.
@@ -1570,22 +1585,32 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
   double* P_bb = slot(S, kSlotBb);
 
   cudaEvent_t join_ev = c->ev_join;
-  if (prec && use_mg && S->prebuilt32) {
-    join_ev = c->ev_join2;  // started by solver_prebuild during the assembly
-  } else if (prec && use_mg) {
-    // The FP32 hierarchy (its dense coarse inverse keeps one SM busy) builds on
-    // the side stream while the FP64 residual runs; joined before the first V-cycle.
-    cudaEventRecord(c->ev_fork, s);
-    cudaStreamWaitEvent(c->side, c->ev_fork, 0);
-    build_hierarchy<float>(c->side, S->h32, c, nullptr, S->ainv32);
-    cudaEventRecord(c->ev_join, c->side);
-  }
-  S->prebuilt32 = false;
-  if (prec || !use_mg)
-    build_level0_f64(s, S->h64, c, S->b64);
-  else
-    build_hierarchy<double>(s, S->h64, c, S->b64, S->ainv64);
   bool joined = !(prec && use_mg);
+  if (use_mg && S->prebuilt) {
+    // Started by solver_prebuild during the assembly; joined before the first V-cycle.
+    if (prec) {
+      build_level0_f64(s, S->h64, c, S->b64);
+    } else {  // b here, the finest FP64 level before the residual
+      launch_copy_interior(s, c->rhs, 0, S->b64, 1, c->grid.ni, c->grid.nj);
+      cudaStreamWaitEvent(s, c->ev_pre0, 0);
+    }
+    join_ev = c->ev_join2;
+    joined = false;
+  } else {
+    if (prec && use_mg) {
+      // The FP32 hierarchy (its dense coarse inverse keeps one SM busy) builds on
+      // the side stream while the FP64 residual runs; joined before the first V-cycle.
+      cudaEventRecord(c->ev_fork, s);
+      cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+      build_hierarchy<float>(c->side, S->h32, c, nullptr, S->ainv32);
+      cudaEventRecord(c->ev_join, c->side);
+    }
+    if (prec || !use_mg)
+      build_level0_f64(s, S->h64, c, S->b64);
+    else
+      build_hierarchy<double>(s, S->h64, c, S->b64, S->ainv64);
+  }
+  S->prebuilt = false;
   if (prec && !use_mg) {
     double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
     k_build_level0<float><<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, c->sys_shift,
