@@ -1543,6 +1543,15 @@ void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, in
 void solver_prebuild(gb2d_ctx* c, const gb2d_solve_opts* o) {
   Solver* S = c->solver;
   if (!S || o->solver != GB2D_SOLVER_MGPCG) return;
+  // Below this size the assembly kernels are too short for the overlap to repay the
+  // extra fork and join: a batch of 256 rising bubbles of 64^2-512^2 on 16 host threads
+  // took 2.25 s with the prebuild and 2.16 s without (GB2D_PREBUILD_MIN_CELLS overrides,
+  // for tuning).
+  static const long min_cells = [] {
+    const char* e = getenv("GB2D_PREBUILD_MIN_CELLS");
+    return e && atol(e) >= 0 ? atol(e) : 300000L;
+  }();
+  if ((long)S->ni * S->nj < min_cells) return;
   cudaEventRecord(c->ev_fork2, c->stream);
   cudaStreamWaitEvent(c->side2, c->ev_fork2, 0);
   if (o->precision == GB2D_PRECISION_MIXED) {
