@@ -246,9 +246,9 @@ __global__ void __launch_bounds__(1024) k_dense_inverse(Level<T> C, double* __re
 
 // ---- tiled smoothing (levels above the tail) ----------------------------------
 //
-// A block of 32x8 threads owns a tile of 64x16 cells (shape 0), 32x16 (shape 1)
-// or 32x8 (shape 2); its 2x2 quads of cells, each one coarse cell, are dealt to
-// the threads in order (shape 0: thread (tx, ty) owns the quad (tx, ty)).  The
+// A block of 32x8 threads owns a tile of 64x16 cells (shape 0), 32x16 (shape 1),
+// 32x8 (shape 2) or 32x32 (shape 3); its 2x2 quads of cells, each one coarse cell,
+// are dealt to the threads in order (shapes 0 and 3: one quad per thread).  The
 // smaller tiles serve the coarser levels, where a level has fewer large tiles than
 // the GPU has SMs and a launch lasts as long as one tile's staging and sweeps:
 // a smaller window halves the loads and half-sweep cells per thread.  All NS
@@ -265,11 +265,11 @@ __global__ void __launch_bounds__(1024) k_dense_inverse(Level<T> C, double* __re
 // when prolonging, already-corrected) value.
 
 constexpr int BXT = 32, BYT = 8;  // threads per block (x, y)
-constexpr int kTileShapes = 3;
+constexpr int kTileShapes = 4;
 
 template <int SH>
 struct TileShape {
-  static constexpr int X = SH == 0 ? 64 : 32, Y = SH == 2 ? 8 : 16;  // cells of one block's tile
+  static constexpr int X = SH == 0 ? 64 : 32, Y = SH == 2 ? 8 : SH == 3 ? 32 : 16;  // cells of one block's tile
   static constexpr int QX = X / 2, QY = Y / 2;                        // its quads (coarse cells)
 };
 
@@ -1114,8 +1114,8 @@ inline unsigned nblocks(size_t n, unsigned cap) {
 }
 
 inline dim3 tiles(int nI, int nJ, int sh) {
-  const int X = sh == 0 ? TileShape<0>::X : sh == 1 ? TileShape<1>::X : TileShape<2>::X;
-  const int Y = sh == 0 ? TileShape<0>::Y : sh == 1 ? TileShape<1>::Y : TileShape<2>::Y;
+  const int X = sh == 0 ? TileShape<0>::X : sh == 1 ? TileShape<1>::X : sh == 2 ? TileShape<2>::X : TileShape<3>::X;
+  const int Y = sh == 0 ? TileShape<0>::Y : sh == 1 ? TileShape<1>::Y : sh == 2 ? TileShape<2>::Y : TileShape<3>::Y;
   return dim3((nI + X - 1) / X, (nJ + Y - 1) / Y);
 }
 
@@ -1186,8 +1186,10 @@ void launch_pre(cudaStream_t s, int sh, const Level<T>& L, const Level<T>& C, T*
     launch_pre_sh<T, NS, 0>(s, L, C, xo, done);
   else if (sh == 1)
     launch_pre_sh<T, NS, 1>(s, L, C, xo, done);
-  else
+  else if (sh == 2)
     launch_pre_sh<T, NS, 2>(s, L, C, xo, done);
+  else
+    launch_pre_sh<T, NS, 3>(s, L, C, xo, done);
 }
 template <typename T, int NS>
 void launch_post(cudaStream_t s, int sh, const Level<T>& L, const Level<T>& C, T* xo, double* prz, Solver* S) {
@@ -1195,8 +1197,10 @@ void launch_post(cudaStream_t s, int sh, const Level<T>& L, const Level<T>& C, T
     launch_post_sh<T, NS, 0>(s, L, C, xo, prz, S);
   else if (sh == 1)
     launch_post_sh<T, NS, 1>(s, L, C, xo, prz, S);
-  else
+  else if (sh == 2)
     launch_post_sh<T, NS, 2>(s, L, C, xo, prz, S);
+  else
+    launch_post_sh<T, NS, 3>(s, L, C, xo, prz, S);
 }
 
 inline bool probe_begin(Probe* pr, cudaStream_t s) {
@@ -1417,22 +1421,26 @@ cudaError_t set_smooth_smem() {
   cudaError_t e = set_smooth_smem_sh<T, 0>();
   if (e == cudaSuccess) e = set_smooth_smem_sh<T, 1>();
   if (e == cudaSuccess) e = set_smooth_smem_sh<T, 2>();
+  if (e == cudaSuccess) e = set_smooth_smem_sh<T, 3>();
   return e;
 }
 
 // Tile shape per tiled level: 32x16 where that gives at least 8 blocks per SM,
-// else 32x8.  Measured on GB300 (MG-PCG projection to 1e-8, 1024^2-4096^2), the
-// 32x16 tile beats 64x16 on every level size: its 22 KB window (FP32, two sweeps)
-// lets 8 blocks share an SM, against 5, and the extra warps hide the staging
-// loads' latency better than the larger tile saves halo work; below 1024^2 the
-// 32x8 tile's shorter per-block pipeline wins.  GB2D_TILE_SHAPES="s0,s1,..."
-// (0, 1 or 2 per level from the finest) overrides the rule, for tuning.
+// else 32x8; FP32 levels of 2048^2 cells and more take 32x32.  Measured on GB300
+// (MG-PCG projection to 1e-8, 512^2-4096^2): the 32x16 tile beats 64x16 on every
+// level size, its 22 KB window (FP32, two sweeps) letting 8 blocks share an SM
+// against 5, and the extra warps hide the staging loads' latency better than the
+// larger tile saves halo work; below 1024^2 the 32x8 tile's shorter per-block
+// pipeline wins; on the largest FP32 levels the 32x32 tile's smaller halo share
+// wins by 1-3% (not in FP64, nor at 1024^2).  GB2D_TILE_SHAPES="s0,s1,..." (0-3
+// per level from the finest) overrides the rule, for tuning.
 template <typename T>
 void plan_shapes(Hierarchy<T>& H, int nsm) {
   const char* env = getenv("GB2D_TILE_SHAPES");
   for (int l = 0; l < H.nlev; ++l) {
     const dim3 t = tiles(H.L[l].nI, H.L[l].nJ, 1);
-    const int sh = (long long)t.x * t.y >= 8LL * nsm ? 1 : 2;
+    int sh = (long long)t.x * t.y >= 8LL * nsm ? 1 : 2;
+    if (sizeof(T) == 4 && (long long)H.L[l].nI * H.L[l].nJ >= 2048LL * 2048) sh = 3;
     H.shape[l] = sh;
   }
   for (int l = 0; env && *env && l < H.nlev; ++l) {
@@ -1454,7 +1462,7 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
   S->nj = nj;
   size_t n = (size_t)ni * nj;
   S->G = (int)nblocks(n, 1216);
-  dim3 t = tiles(ni, nj, kTileShapes - 1);  // the most blocks any tile shape launches
+  dim3 t = tiles(ni, nj, 2);  // the most blocks any tile shape launches (32x8)
   S->nparts_cap = (int)(t.x * t.y) > S->G ? (int)(t.x * t.y) : S->G;
   size_t np = (size_t)(ni + 2) * (nj + 2);
   cudaError_t e = alloc_hierarchy(S->h64, ni, nj);

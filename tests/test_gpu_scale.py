@@ -35,8 +35,9 @@ def test_projection_matches_oracle(gb, oracle, n):
     assert rel_l2(c.get(gb.FIELD_U), u) <= 1e-9
 
 
-@pytest.mark.parametrize("n", [1024])
+@pytest.mark.parametrize("n", [1024, 2048])
 def test_benchmark_size_fp64_vs_mixed(gb, n):
+    """At 1024^2 (the finest FP32 level in 32x16 tiles) and 2048^2 (32x32 tiles)."""
     case = bubbles_case(n, seed=0)
     dt = 0.5 / (n - 1)
     res = {}
