@@ -2,9 +2,11 @@
 // one GPU.  Each instance is a full gb2d context with its own stream; host worker
 // threads (one per in-flight instance) drive disjoint sets of instances frame by frame,
 // so that the small grids' kernels from different instances overlap on the 152 SMs
-// while each instance's solver keeps its own convergence checks.  Instances are placed
-// on workers longest-first by their measured cost per frame, and each grid size gets the
-// V-cycle smoothing count an autotuning pass measured fastest.
+// while each instance's solver keeps its own convergence test, on the device: every CG
+// solve of an instance is one graph launch whose WHILE node iterates until it
+// converges.  Instances are placed on workers longest-first by their measured cost per
+// frame, and each grid size gets the V-cycle smoothing count an autotuning pass
+// measured fastest.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -65,6 +67,7 @@ int gb2d_batch_create(int n, const gb2d_grid* grids, const gb2d_params* params, 
   for (int k = 0; k < n; ++k) {
     gb2d_ctx* c = nullptr;
     int rc = gb2d_create(&grids[k], &params[k], &c);
+    if (rc == GB2D_OK) c->device_loop = 1;  // each CG solve one graph launch (fewer host calls per thread)
     if (rc == GB2D_OK && flows) rc = gb2d_set_flow_params(c, &flows[k]);
     if (rc != GB2D_OK) {
       if (c) gb2d_destroy(c);

@@ -106,6 +106,8 @@ struct Scalars {
   double bb;       // ||b||^2
   int flag;        // non-finite / zero-gradient detections
   int pad;
+  int iters;       // CG iterations of the device-driven loop so far
+  int max_it;      // its cap
   unsigned long long maxu_bits, maxv_bits;  // max |u|, |v| of the velocity update
   unsigned long long cfl_bits[3];           // max |u|, |v|, |kappa| for the CFL time step
   double cfl[5];                            // CFL dt, c_f, g_f, v_f, s_f
@@ -141,6 +143,7 @@ struct gb2d_ctx {
   cudaEvent_t ev_fork, ev_join;   // fork / join of the side stream
   cudaStream_t side2;             // third stream: the preconditioner hierarchy built during the assembly
   cudaEvent_t ev_fork2, ev_join2, ev_pre0;  // ev_pre0: the FP64 finest level is built
+  int device_loop;                // run each CG solve as one graph launch (a device-side WHILE loop)
   cudaStream_t xfer;              // host copies that overlap the projection (gb2d_projection_host)
   cudaEvent_t ev_xfer0, ev_xfer;
   gb2d::Probe probe;

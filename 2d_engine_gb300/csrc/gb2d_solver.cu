@@ -843,6 +843,29 @@ __global__ void k_begin_inner(Scalars* sc, int* done, double thr2) {
   sc->rz_cur = 1.0;
 }
 
+// Start of a device-driven CG run (the solve graph's WHILE loop): as k_begin_inner,
+// with the iteration count reset and its cap.
+__global__ void k_begin_loop(Scalars* sc, int* done, double thr2, int max_it) {
+  *done = 0;
+  sc->thr2 = thr2;
+  sc->rz_cur = 1.0;
+  sc->iters = 0;
+  sc->max_it = max_it;
+}
+
+// Last node of the loop body: counts the iteration, hands the count and the latest
+// ||r||^2 to the host, and continues the loop only while the run has not converged
+// and is under its cap.  It never returns early: every pass sets the condition, so the
+// loop ends after at most max_it passes (and after 1 << 20 in any case).
+__global__ void k_loop_cond(cudaGraphConditionalHandle h, Scalars* sc, const int* __restrict__ done, double* host_out) {
+  pdl_enter();
+  const int n = ++sc->iters;
+  host_out[0] = sc->rr;
+  host_out[1] = (double)n;
+  const bool more = *done == 0 && n < sc->max_it && n < (1 << 20);
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
 }  // namespace
 
 // ---- host side -------------------------------------------------------------------
@@ -864,6 +887,9 @@ struct GraphSet {
   bool ok = false;
   cudaGraphExec_t init = nullptr, iter[2] = {nullptr, nullptr};
   unsigned long long nodes_init = 0, nodes_iter = 0;
+  cudaGraphExec_t loop = nullptr;  // init + a WHILE node over one iteration: the whole CG run
+  cudaGraph_t loop_graph = nullptr;  // its source (holds the conditional handle), kept while loop lives
+  unsigned long long nodes_body = 0;
 };
 
 struct Solver {
@@ -1340,6 +1366,77 @@ bool capture_graph(gb2d_ctx* c, cudaGraphExec_t* exec, unsigned long long* nodes
   return true;
 }
 
+// The whole CG run as one graph: the init step, then a WHILE node whose body is one
+// iteration followed by k_loop_cond.  Built by capturing into the graph (the init),
+// adding the conditional node behind the captured work, and capturing the iteration
+// into its body.  Returns false (nothing kept) if any step is refused.
+template <typename T>
+bool capture_loop_graph(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, double* x64, int use_mg, int nu, GraphSet& gs) {
+  cudaStream_t cs = c->own_stream;
+  cudaGraph_t g = nullptr;
+  cudaGraphConditionalHandle h;
+  bool ok = cudaGraphCreate(&g, 0) == cudaSuccess && cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+  unsigned long long captured = 0;
+  if (ok && cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    t_capture_count = &captured;
+    enqueue_init<T>(cs, S, H, ainv, use_mg, nu, nullptr);
+    t_capture_count = nullptr;
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode = nullptr;
+    ok = cudaStreamGetCaptureInfo(cs, &st, nullptr, nullptr, &deps, nullptr, &nd) == cudaSuccess && st == cudaStreamCaptureStatusActive &&
+         cudaGraphAddNode(&cnode, g, deps, nullptr, nd, &cp) == cudaSuccess &&
+         cudaStreamUpdateCaptureDependencies(cs, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies) == cudaSuccess;
+    cudaGraph_t gout = nullptr;
+    ok = cudaStreamEndCapture(cs, &gout) == cudaSuccess && ok;
+    if (ok) {
+      cudaGraph_t body = cp.conditional.phGraph_out[0];
+      unsigned long long nb = 0;
+      ok = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+      if (ok) {
+        t_capture_count = &nb;
+        enqueue_iter<T>(cs, S, H, ainv, x64, use_mg, nu, 0, nullptr);
+        pdl_launch(cs, dim3(1), dim3(1), 0, k_loop_cond, h, S->sc, (const int*)S->done, S->host + 2);
+        GB_LAUNCHED(1);
+        t_capture_count = nullptr;
+        cudaGraph_t bout = nullptr;
+        ok = cudaStreamEndCapture(cs, &bout) == cudaSuccess;
+      }
+      gs.nodes_body = nb;
+    }
+  } else {
+    ok = false;
+  }
+  if (ok) ok = cudaGraphInstantiate(&gs.loop, g, 0) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    gs.loop = nullptr;
+    if (g) cudaGraphDestroy(g);
+    return false;
+  }
+  gs.loop_graph = g;
+  return true;
+}
+
+// Whether a context runs each CG solve as one graph launch.  A standalone solve does
+// not gain from it: the host already checks iteration k-1 while k runs, and the WHILE
+// node's pass boundary costs a few microseconds per iteration (1024^2: 2.45 -> 2.49 ms).
+// Many contexts driven by contending host threads do (batch of 256 small grids:
+// 2.19 -> 2.05 s), so batch instances turn it on.  GB2D_DEVICE_LOOP=0 / =1 forces it.
+inline bool device_loop_enabled(const gb2d_ctx* c) {
+  static const int forced = [] {
+    const char* e = getenv("GB2D_DEVICE_LOOP");
+    return e && (e[0] == '0' || e[0] == '1') ? e[0] - '0' : -1;
+  }();
+  return forced >= 0 ? forced == 1 : c->device_loop != 0;
+}
+
 template <typename T>
 GraphSet* graphs_for(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, double* x64, int prec, int use_mg, int nu) {
   int slot = nu - 1;
@@ -1348,10 +1445,13 @@ GraphSet* graphs_for(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv
   if (gs.init) cudaGraphExecDestroy(gs.init);
   for (auto& g : gs.iter)
     if (g) cudaGraphExecDestroy(g);
+  if (gs.loop) cudaGraphExecDestroy(gs.loop);
+  if (gs.loop_graph) cudaGraphDestroy(gs.loop_graph);
   gs = GraphSet();
   bool ok = capture_graph(c, &gs.init, &gs.nodes_init, [&](cudaStream_t cs) { enqueue_init<T>(cs, S, H, ainv, use_mg, nu, nullptr); });
   for (int par = 0; par < 2 && ok; ++par)
     ok = capture_graph(c, &gs.iter[par], &gs.nodes_iter, [&](cudaStream_t cs) { enqueue_iter<T>(cs, S, H, ainv, x64, use_mg, nu, par, nullptr); });
+  if (ok && device_loop_enabled(c)) capture_loop_graph<T>(c, S, H, ainv, x64, use_mg, nu, gs);
   gs.ok = ok;
   S->graph_x[prec][use_mg][slot] = x64;
   return ok ? &gs : nullptr;
@@ -1368,6 +1468,15 @@ int inner_pcg(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, doubl
   cudaStream_t s = c->stream;
   Probe* pr = &c->probe;
   GraphSet* gs = pr->on ? nullptr : graphs_for<T>(c, S, H, ainv, x64, prec, use_mg, nu);
+  if (gs && gs->loop) {  // the whole run on the device: one launch, one wait
+    k_begin_loop<<<1, 1, 0, s>>>(S->sc, S->done, thr2, max_it);
+    cudaGraphLaunch(gs->loop, s);
+    cudaStreamSynchronize(s);
+    const int n = (int)S->host[3];
+    *last_rr = S->host[2];
+    GB_LAUNCHED(1 + gs->nodes_init + (unsigned long long)n * gs->nodes_body);
+    return n;
+  }
   k_begin_inner<<<1, 1, 0, s>>>(S->sc, S->done, thr2);
   GB_LAUNCHED(1);
   if (gs) {
@@ -1521,6 +1630,8 @@ void solver_destroy(Solver* S) {
         if (g.init) cudaGraphExecDestroy(g.init);
         for (auto& it : g.iter)
           if (it) cudaGraphExecDestroy(it);
+        if (g.loop) cudaGraphExecDestroy(g.loop);
+        if (g.loop_graph) cudaGraphDestroy(g.loop_graph);
       }
   free_hierarchy(S->h64);
   free_hierarchy(S->h32);
