@@ -70,3 +70,13 @@ def test_reinitialization_restores_distance(gb):
     band = np.abs(out) < 3.0 / (n - 1)
     mag = np.sqrt(gx ** 2 + gy ** 2)[band]
     assert abs(np.median(mag) - 1.0) < 0.05
+
+
+def test_alu_peaks_plausible(gb):
+    """gb2d_alu_peaks (the denominators of the level-set sweeps' ALU roofline): both finite and
+    positive, FP32 far above FP64, neither above the part's nominal rates (GB300: FP32 FMA
+    about 80 TFLOP/s at 2.07 GHz, FP64 about 1.3 TFLOP/s)."""
+    f64, f32 = gb.alu_peaks()
+    assert 0.1 < f64 < 2.0, f64
+    assert 10.0 < f32 < 100.0, f32
+    assert f32 > 20 * f64
