@@ -582,7 +582,11 @@ int gb2d_projection_host(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, const
                          const double* p, double* p_out, double* u_out, double* v_out, gb2d_solve_stats* st) {
   if (!c || !o || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
   const HostIO io{phi, u, v, p, p_out, u_out, v_out};
-  return projection_run(c, dt, o, st, &io);
+  const int rc = projection_run(c, dt, o, st, &io);
+  // On every return, error paths included, no copy still reads or writes the caller's buffers.
+  cudaStreamSynchronize(c->stream);
+  cudaStreamSynchronize(c->xfer);
+  return rc;
 }
 
 int gb2d_set_flow_params(gb2d_ctx* c, const gb2d_flow_params* f) {
