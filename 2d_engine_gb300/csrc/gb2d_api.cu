@@ -539,8 +539,19 @@ static int projection_run(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d
     GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_xfer, c->xfer));
     inputs = c->ev_xfer;
   }
-  int rc = curvature_and_assemble(c, dt, o, inputs);
-  if (rc) {
+  int rc;
+  if (c->asm_reuse) {
+    // The level set's interior has not changed since the previous projection of this
+    // time step: its curvature, face weights, diagonal and the solver's levels stand;
+    // only the right-hand side follows the new velocity.  phi's ghosts are extrapolated
+    // again as every projection does: the extrapolation is not idempotent (its outer
+    // layer reads the previous inner layer), and the ghosts are part of the state.
+    launch_extrapolate_ghosts(c->stream, phi, 2, c->grid.ni, c->grid.nj);
+    if (inputs) GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->stream, inputs, 0));
+    launch_rhs(c->stream, c, phi, dt);
+    if ((rc = check_launch(c, "assemble"))) return rc;
+    solver_keep_levels(c);
+  } else if ((rc = curvature_and_assemble(c, dt, o, inputs))) {
     solver_drop_prebuild(c);
     return rc;
   }
@@ -634,9 +645,19 @@ int gb2d_advance_time_step(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2
   gb2d_solve_stats sum, one;
   memset(&sum, 0, sizeof sum);
   int capped = 0;
+  // The level set is fixed through the velocity stages (SolveForRK advects, forces and
+  // projects the velocity only): stages 2 and 3 keep the first projection's curvature,
+  // face weights, diagonal and solver levels and rebuild only the right-hand side
+  // (GB2D_ASM_REUSE=0 rebuilds everything, for comparison).
+  static const bool reuse = [] {
+    const char* e = getenv("GB2D_ASM_REUSE");
+    return !(e && e[0] == '0');
+  }();
   for (int stage = 0; stage < 3; ++stage) {
     memset(&one, 0, sizeof one);
+    c->asm_reuse = reuse && stage > 0 ? 1 : 0;
     rc = gb2d_solve_for_rk(c, dt, o, &one);
+    c->asm_reuse = 0;
     if (rc == GB2D_ERR_MAX_ITERS)
       capped = 1;
     else if (rc)

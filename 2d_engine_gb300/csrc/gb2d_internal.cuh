@@ -144,6 +144,7 @@ struct gb2d_ctx {
   cudaStream_t side2;             // third stream: the preconditioner hierarchy built during the assembly
   cudaEvent_t ev_fork2, ev_join2, ev_pre0;  // ev_pre0: the FP64 finest level is built
   int device_loop;                // run each CG solve as one graph launch (a device-side WHILE loop)
+  int asm_reuse;                  // the next projection keeps the phi-dependent assembly and solver levels
   cudaStream_t xfer;              // host copies that overlap the projection (gb2d_projection_host)
   cudaEvent_t ev_xfer0, ev_xfer;
   gb2d::Probe probe;
@@ -238,6 +239,9 @@ int solver_solve(gb2d_ctx* c, const double* rhs, double* x, const gb2d_solve_opt
 void solver_prebuild(gb2d_ctx* c, const gb2d_solve_opts* o);
 // Abandon a started prebuild (an error before the solve): ctx->stream waits for it.
 void solver_drop_prebuild(gb2d_ctx* c);
+// The next solver_solve keeps its levels (built by the previous solve from the same
+// ctx->bx/by/diag) and refreshes only the right-hand side.
+void solver_keep_levels(gb2d_ctx* c);
 void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, int* cluster_ctas);
 
 }  // namespace gb2d

@@ -909,6 +909,7 @@ struct Solver {
   int G = 0;               // blocks of the grid-stride CG kernels
   cudaEvent_t ev[2] = {nullptr, nullptr};
   bool prebuilt = false;  // the hierarchies are building on ctx->side2 (solver_prebuild)
+  bool keep = false;      // the levels of the previous solve stand (solver_keep_levels)
   // Graphs per (precision, solver, smoothing sweeps) and the x they update.
   GraphSet graphs[2][2][3];
   double* graph_x[2][2][3] = {};
@@ -1688,6 +1689,10 @@ void solver_prebuild(gb2d_ctx* c, const gb2d_solve_opts* o) {
   S->prebuilt = true;
 }
 
+void solver_keep_levels(gb2d_ctx* c) {
+  if (c->solver) c->solver->keep = true;
+}
+
 void solver_drop_prebuild(gb2d_ctx* c) {
   Solver* S = c->solver;
   if (!S || !S->prebuilt) return;
@@ -1714,7 +1719,14 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
 
   cudaEvent_t join_ev = c->ev_join;
   bool joined = !(prec && use_mg);
-  if (use_mg && S->prebuilt) {
+  const bool keep = S->keep && !S->prebuilt;
+  S->keep = false;
+  if (keep) {
+    // The system's coefficients are those of the previous solve: its levels stand,
+    // only b changes.
+    launch_copy_interior(s, c->rhs, 0, S->b64, 1, c->grid.ni, c->grid.nj);
+    joined = true;
+  } else if (use_mg && S->prebuilt) {
     // Started by solver_prebuild during the assembly; joined before the first V-cycle.
     if (prec) {
       build_level0_f64(s, S->h64, c, S->b64);
@@ -1739,7 +1751,7 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
       build_hierarchy<double>(s, S->h64, c, S->b64, S->ainv64);
   }
   S->prebuilt = false;
-  if (prec && !use_mg) {
+  if (prec && !use_mg && !keep) {
     double idx2 = 1.0 / (c->base.dx * c->base.dx), idy2 = 1.0 / (c->base.dy * c->base.dy);
     k_build_level0<float><<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, c->sys_shift,
                                                                                                 S->h32.L[0], nullptr, idx2, idy2);
