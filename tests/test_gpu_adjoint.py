@@ -16,7 +16,7 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 EPS_FD = 1e-6
-GRAD_TOL = 1e-5  # spec bound: adjoint gradients against finite differences
+GRAD_TOL = 1e-5  # adjoint gradients against central differences (relative)
 
 
 def central(f, x, d, eps=EPS_FD):

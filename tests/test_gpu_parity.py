@@ -10,7 +10,7 @@ from conftest import golden_names, load_golden
 pytestmark = pytest.mark.gpu
 NAMES = golden_names()
 
-P_TOL_FP64 = 1e-10    # pressure / velocity, FP64 path (spec bound)
+P_TOL_FP64 = 1e-10    # pressure / velocity of the FP64 path against the reference (relative L2)
 P_TOL_MIXED = 1e-8    # mixed path: refinement to 1e-10 residual, then held to 1e-8 of the FP64 result
 
 
