@@ -111,6 +111,7 @@ def library():
         "gb2d_batch_advance": [vp, i, d, vp, O, ctypes.POINTER(BatchStatsT)],
         "gb2d_jump_poisson_solve": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, O, S],
         "gb2d_projection_density_gradient": [vp, d, ctypes.POINTER(d), ctypes.POINTER(d)],
+        "gb2d_projection_phi_gradient": [vp, d, vp],
         "gb2d_projection_host": [vp, d, O, vp, vp, vp, vp, vp, vp, vp, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
@@ -405,7 +406,14 @@ class Context:
         self._check(self.L.gb2d_projection_density_gradient(self.h, dt, ctypes.byref(w), ctypes.byref(a)))
         return w.value, a.value
 
+    def projection_phi_gradient(self, dt):
+        """dL/dphi (PHI's shape) of the loss of the last projection_adjoint (gb2d_projection_phi_gradient)."""
+        out = np.zeros(self.shape(FIELD_PHI))
+        self._check(self.L.gb2d_projection_phi_gradient(self.h, dt, _ptr(out)))
+        return out
+
     # Pressure system (a10/a15)
+
     def poisson_assemble(self, dt):
         ni, nj = self.ni, self.nj
         bx, by = np.zeros((nj, ni + 1)), np.zeros((nj + 1, ni))

@@ -371,6 +371,206 @@ __global__ void k_density_grad(const double* __restrict__ phi_a, const double* _
   }
 }
 
+// ---- d/d(phi) of a projection loss (after the projection adjoint) -----------------
+//
+//   dL/dphi = sum_f lam_f du'_f/dphi |_p  +  z . (db/dphi - (dA/dphi) p)
+//
+// phi enters through the face weights beta (|phi|-weighted harmonic mean of 1/rho, in A's
+// off-diagonals and dx-only diagonal with the corner pin and in b's jump fluxes), the jump
+// fluxes' |phi|-weighted interpolation of jc = sigma kappa, the curvature kappa(phi) (a
+// 9-point stencil, zero slope where it is clamped), and on the velocity update's interface
+// faces the |phi|-weighted jump and the smeared Heaviside density.  The phases (signs of
+// phi) are piecewise constant: no derivative.  Two passes, both gathers (deterministic):
+// per node the cotangent of kappa and from it the coefficients of the curvature's five
+// differences; then per node of the ghost-1 ring and interior the direct terms of its four
+// faces plus the curvature stencils that read it.  The extrapolation of phi's ghosts that
+// the projection starts with is reversed last.
+struct PhiArgs {
+  int ni, nj;
+  double odx, ody, o2dx, o2dy, odx2, ody2, idx2, idy2, dt, sigma, tol;
+  double water, air, inv_water, inv_air, eps_h, eps_v, oeh, oev;
+};
+
+__device__ __forceinline__ double sgn(double x) { return gtz(x) ? 1.0 : (ltz(x) ? -1.0 : 0.0); }
+__device__ __forceinline__ double vphase(double l, const PhiArgs& a) { return lez(l) ? a.inv_air : (gtz(l) ? a.inv_water : 1.0); }
+// d H / d x of the smeared Heaviside inside its band (0 outside), PI as the forward's.
+__device__ __forceinline__ double dheaviside(double x, double eps, double oe) {
+  if (lt_neg(x, eps) || gt_pos(x, eps)) return 0.0;
+  const double PI_REF = 3.141592;
+  return 0.5 * oe * (1.0 + cos(PI_REF * x * oe));
+}
+// Jump-flux sign of the arm c -> n: +1 (c <= 0 < n), -1 (c > 0 >= n), 0.
+__device__ __forceinline__ double arm_sign(double lc, double ln) {
+  if (lez(lc) && !lez(ln) && gtz(ln)) return 1.0;
+  if (!lez(lc) && gtz(lc) && lez(ln)) return -1.0;
+  return 0.0;
+}
+
+struct PhiView {
+  DField phi, P, Z, lu, lv;
+  const double* kappa;
+  int ni, nj;
+  __device__ double L(int i, int j) const { return GB_AT(phi, i, j); }
+  __device__ double LV(int i, int j) const {  // the node a face weight takes its phase from (as vnode)
+    i = i < 0 ? 1 : (i >= ni ? ni - 2 : i);
+    j = j < 0 ? 1 : (j >= nj ? nj - 2 : j);
+    return GB_AT(phi, i, j);
+  }
+  __device__ double jc(int i, int j, double sigma) const {
+    if (i < 0 || j < 0 || i >= ni || j >= nj) return 0.0;
+    return sigma * kappa[i + (size_t)j * ni];
+  }
+  __device__ bool interior(int i, int j) const { return i >= 0 && j >= 0 && i < ni && j < nj; }
+};
+
+// One face between node c (the + side: (i, j)) and node n ((i-1, j) for an x-face, (i, j-1)
+// for a y-face): its direct contributions to dL/dphi_c and dL/dphi_n, and to dL/djc_c and
+// dL/djc_n (the curvature pass uses the latter).
+__device__ void face_terms(const PhiView& v, const PhiArgs& a, bool xc, int i, int j, double& gc, double& gn, double& kc, double& kn) {
+  gc = gn = kc = kn = 0.0;
+  const int in = xc ? i - 1 : i, jn = xc ? j : j - 1;
+  const int nmax = xc ? a.ni : a.nj, f = xc ? i : j;  // the face's index along its axis, 0..nmax
+  const double lc = v.L(i, j), ln = v.L(in, jn);
+  const double vc = vphase(v.LV(i, j), a), vn = vphase(v.LV(in, jn), a);
+  const double ac = fabs(lc), an = fabs(ln), S = ac + an, D = vc * an + vn * ac;
+  const double beta = vc * vn * (an + ac) / D;
+  const double dbc = sgn(lc) * vc * vn * an * (vc - vn) / (D * D), dbn = sgn(ln) * vc * vn * ac * (vn - vc) / (D * D);
+  const bool crow = v.interior(i, j), nrow = v.interior(in, jn);
+  const double pc = crow ? GB_AT(v.P, i, j) : 0.0, pn = nrow ? GB_AT(v.P, in, jn) : 0.0;
+  const double zc = crow ? GB_AT(v.Z, i, j) : 0.0, zn = nrow ? GB_AT(v.Z, in, jn) : 0.0;
+  const double hoff = xc ? a.idx2 : a.idy2, o2 = xc ? a.odx2 : a.ody2;
+  // A p: the c row's arm toward n (an interior face, or the pinned corner's wall arm) and
+  // the n row's arm toward c (unless it is the far wall)
+  double dLdb = 0.0;
+  if (crow) {
+    if (f > 0)
+      dLdb -= zc * (a.idx2 * pc - hoff * pn);
+    else if (i == 0 && j == 0)
+      dLdb -= zc * a.idx2 * pc;
+  }
+  if (nrow && f < nmax) dLdb -= zn * (a.idx2 * pn - hoff * pc);
+  // jump fluxes F = s o2 av beta, in b as -F: arm c -> n in row c, arm n -> c in row n
+  const double jcc = v.jc(i, j, a.sigma), jcn = v.jc(in, jn, a.sigma);
+  if (S > 0.0) {
+    const double av = (jcc * an + jcn * ac) / S;
+    const double scn = crow ? arm_sign(lc, ln) : 0.0, snc = nrow ? arm_sign(ln, lc) : 0.0;
+    const double wc = -zc * scn * o2, wn = -zn * snc * o2;  // dL/dF-weights times o2 s
+    dLdb += (wc + wn) * av;
+    const double dav_ac = an * (jcn - jcc) / (S * S), dav_an = ac * (jcc - jcn) / (S * S);
+    gc += (wc + wn) * beta * dav_ac * sgn(lc);
+    gn += (wc + wn) * beta * dav_an * sgn(ln);
+    kc += (wc + wn) * beta * an / S * a.sigma;
+    kn += (wc + wn) * beta * ac / S * a.sigma;
+  }
+  gc += dLdb * dbc;
+  gn += dLdb * dbn;
+  // velocity update of this face (updated for i < ni on x-faces, j < nj on y-faces)
+  if (crow && lc * ln < 0 && (ltz(lc) || gtz(lc))) {
+    const double lam = xc ? GB_AT(v.lu, i, j) : GB_AT(v.lv, i, j);
+    const double od = xc ? a.odx : a.ody, eps = xc ? a.eps_h : a.eps_v, oe = xc ? a.oeh : a.oev;
+    const double s0 = ltz(lc) ? 1.0 : -1.0;
+    const double gam = (jcn * ac + jcc * an) / S;
+    const double m = 0.5 * (lc + ln);
+    const double dh = a.air + (a.water - a.air) * heaviside(m, eps, oe), odh = 1.0 / dh;
+    const double dp = pc - pn;
+    const double w_gam = -a.dt * od * s0 * odh * lam;                  // dL/dgam
+    const double w_odh = -a.dt * od * (dp + s0 * gam) * lam;            // dL/dodh
+    const double dodh_dm = -odh * odh * (a.water - a.air) * dheaviside(m, eps, oe);
+    gc += w_gam * sgn(lc) * an * (jcn - jcc) / (S * S) + w_odh * dodh_dm * 0.5;
+    gn += w_gam * sgn(ln) * ac * (jcc - jcn) / (S * S) + w_odh * dodh_dm * 0.5;
+    kc += w_gam * an / S * a.sigma;
+    kn += w_gam * ac / S * a.sigma;
+  }
+}
+
+// Pass 1, per interior node: dL/dkappa from its faces, then the coefficients of the five
+// curvature differences (central: cx, cy; one-sided fallback: fx, fy; cxx, cyy, cxy).
+__global__ void k_phi_grad_kappa(PhiView v, PhiArgs a, double* __restrict__ co) {
+  const int ni = a.ni, nj = a.nj;
+  const size_t n = (size_t)ni * nj;
+  GB_FOR_IJ(i, j, ni, nj) {
+    double gk = 0.0, t0, t1, kc, kn;
+    face_terms(v, a, true, i, j, t0, t1, kc, kn);  // x-face (i, j): this node is c
+    gk += kc;
+    face_terms(v, a, false, i, j, t0, t1, kc, kn);  // y-face (i, j)
+    gk += kc;
+    face_terms(v, a, true, i + 1, j, t0, t1, kc, kn);  // x-face (i+1, j): this node is n
+    gk += kn;
+    face_terms(v, a, false, i, j + 1, t0, t1, kc, kn);  // y-face (i, j+1)
+    gk += kn;
+    // kappa's partials, as the forward computes kappa (the clamp has zero slope)
+    const double c = v.L(i, j), l = v.L(i - 1, j), r = v.L(i + 1, j), b = v.L(i, j - 1), tp = v.L(i, j + 1);
+    double px = (r - l) * a.o2dx, py = (tp - b) * a.o2dy;
+    const double pxx = (r - 2 * c + l) * a.odx2, pyy = (tp - 2 * c + b) * a.ody2;
+    const double pxy = (v.L(i + 1, j + 1) - v.L(i + 1, j - 1) - v.L(i - 1, j + 1) + v.L(i - 1, j - 1)) * a.o2dx * a.o2dy;
+    double mag = sqrt(px * px + py * py);
+    bool central = mag * mag * mag != 0.0;
+    if (!central) {
+      px = (r - c) * a.odx;
+      py = (tp - c) * a.ody;
+      mag = sqrt(px * px + py * py);
+    }
+    const double deno = mag * mag * mag;
+    double e[7] = {0, 0, 0, 0, 0, 0, 0};
+    if (deno != 0.0 && gk != 0.0) {
+      const double N = px * px * pyy - 2.0 * px * py * pxy + py * py * pxx;
+      const double curv = -N / deno;
+      if (fabs(curv) <= a.tol) {
+        const double dpx = -(2 * px * pyy - 2 * py * pxy) / deno + N * 3 * px * mag / (deno * deno);
+        const double dpy = -(2 * py * pxx - 2 * px * pxy) / deno + N * 3 * py * mag / (deno * deno);
+        e[central ? 0 : 2] = gk * dpx;
+        e[central ? 1 : 3] = gk * dpy;
+        e[4] = gk * (-py * py / deno);
+        e[5] = gk * (-px * px / deno);
+        e[6] = gk * (2 * px * py / deno);
+      }
+    }
+    const size_t t = (size_t)j * ni + i;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) co[k * n + t] = e[k];
+  }
+}
+
+// Pass 2, per node of the interior and the ghost-1 ring: the direct terms of its four faces
+// and the curvature stencils that read it, into g (phi's layout, ghost 2).
+__global__ void k_phi_grad_gather(PhiView v, PhiArgs a, const double* __restrict__ co, double* __restrict__ g_a) {
+  const int ni = a.ni, nj = a.nj;
+  const size_t n = (size_t)ni * nj;
+  DField g = dfield(g_a, 2, ni, nj);
+  GB_FOR_IJ(ii, jj, ni + 2, nj + 2) {
+    const int i = ii - 1, j = jj - 1;
+    double acc = 0.0, gc, gn, kc, kn;
+    if (i >= 0 && i <= ni && j >= 0 && j < nj) {  // x-face (i, j): this node is c
+      face_terms(v, a, true, i, j, gc, gn, kc, kn);
+      acc += gc;
+    }
+    if (i + 1 >= 0 && i + 1 <= ni && j >= 0 && j < nj) {  // x-face (i+1, j): this node is n
+      face_terms(v, a, true, i + 1, j, gc, gn, kc, kn);
+      acc += gn;
+    }
+    if (j >= 0 && j <= nj && i >= 0 && i < ni) {
+      face_terms(v, a, false, i, j, gc, gn, kc, kn);
+      acc += gc;
+    }
+    if (j + 1 >= 0 && j + 1 <= nj && i >= 0 && i < ni) {
+      face_terms(v, a, false, i, j + 1, gc, gn, kc, kn);
+      acc += gn;
+    }
+    auto C = [&](int k, int mi, int mj) -> double {
+      return (mi >= 0 && mj >= 0 && mi < ni && mj < nj) ? co[k * n + (size_t)mj * ni + mi] : 0.0;
+    };
+    // curvature of (i-1, j), (i+1, j), (i, j-1), (i, j+1), (i, j) and the four diagonal nodes
+    acc += C(0, i - 1, j) * a.o2dx + C(2, i - 1, j) * a.odx + C(4, i - 1, j) * a.odx2;
+    acc += -C(0, i + 1, j) * a.o2dx + C(4, i + 1, j) * a.odx2;
+    acc += C(1, i, j - 1) * a.o2dy + C(3, i, j - 1) * a.ody + C(5, i, j - 1) * a.ody2;
+    acc += -C(1, i, j + 1) * a.o2dy + C(5, i, j + 1) * a.ody2;
+    acc += -C(2, i, j) * a.odx - C(3, i, j) * a.ody - 2 * C(4, i, j) * a.odx2 - 2 * C(5, i, j) * a.ody2;
+    const double oxy = a.o2dx * a.o2dy;
+    acc += (C(6, i - 1, j - 1) - C(6, i - 1, j + 1) - C(6, i + 1, j - 1) + C(6, i + 1, j + 1)) * oxy;
+    GB_AT(g, i, j) = acc;
+  }
+}
+
 }  // namespace
 
 int density_gradient(gb2d_ctx* c, double dt, double* d_water, double* d_air) {
@@ -490,5 +690,57 @@ void launch_projection_adjoint_vel(cudaStream_t s, gb2d_ctx* c, double dt, const
   k_proj_adj_vel<<<grid_ij(ni + 5, nj + 5), kThreads, 0, s>>>(c->adj_lam_u, c->adj_lam_v, z, c->adj_mu_u, c->adj_mu_v, a);
   GB_LAUNCHED(1);
 }
+
+int phi_gradient(gb2d_ctx* c, double dt, double* host_out) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  PhiArgs a;
+  a.ni = ni;
+  a.nj = nj;
+  a.odx = c->base.odx;
+  a.ody = c->base.ody;
+  a.o2dx = c->base.o2dx;
+  a.o2dy = c->base.o2dy;
+  a.odx2 = c->base.odx2;
+  a.ody2 = c->base.ody2;
+  a.idx2 = 1.0 / (c->base.dx * c->base.dx);
+  a.idy2 = 1.0 / (c->base.dy * c->base.dy);
+  a.dt = dt;
+  a.sigma = c->prm.surface_tension;
+  a.tol = c->base.dx < c->base.dy ? c->base.odx : c->base.ody;
+  a.water = c->prm.water_density;
+  a.air = c->prm.air_density;
+  a.inv_water = 1.0 / a.water;
+  a.inv_air = 1.0 / a.air;
+  a.eps_h = 1.5 * c->base.dx;
+  a.eps_v = 1.5 * c->base.dy;
+  a.oeh = 1.0 / a.eps_h;
+  a.oev = 1.0 / a.eps_v;
+  PhiView v;
+  v.phi = dfield(c->phi_buf[c->phi_cur], 2, ni, nj);
+  v.P = dfield(c->p, 1, ni, nj);
+  v.Z = dfield(c->xw, 1, ni, nj);
+  v.lu = dfield(c->adj_lam_u, 2, ni + 1, nj);
+  v.lv = dfield(c->adj_lam_v, 2, ni, nj + 1);
+  v.kappa = c->kappa;
+  v.ni = ni;
+  v.nj = nj;
+  const size_t nphi = (size_t)(ni + 4) * (nj + 4);
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(c->adj_mu_phi, 0, nphi * sizeof(double), c->stream));
+  k_phi_grad_kappa<<<grid_ij(ni, nj), kThreads, 0, c->stream>>>(v, a, c->adj_coef);
+  k_phi_grad_gather<<<grid_ij(ni + 2, nj + 2), kThreads, 0, c->stream>>>(v, a, c->adj_coef, c->adj_mu_phi);
+  const int m = ni > nj ? ni : nj;
+  k_extrap_adj_rows<<<(m + 127) / 128, 128, 0, c->stream>>>(c->adj_mu_phi, ni, nj);
+  k_extrap_adj_cols<<<(m + 127) / 128, 128, 0, c->stream>>>(c->adj_mu_phi, ni, nj);
+  GB_LAUNCHED(4);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(host_out, c->adj_mu_phi, nphi * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  cudaError_t e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(c->err, sizeof(c->err), "phi gradient: %s", cudaGetErrorString(e));
+    return GB2D_ERR_CUDA;
+  }
+  return GB2D_OK;
+}
+
 
 }  // namespace gb2d

@@ -789,6 +789,11 @@ int gb2d_projection_density_gradient(gb2d_ctx* c, double dt, double* d_water_den
   return density_gradient(c, dt, d_water_density, d_air_density);
 }
 
+int gb2d_projection_phi_gradient(gb2d_ctx* c, double dt, double* d_phi) {
+  if (!c || !d_phi || !std::isfinite(dt) || dt == 0.0 || !c->adj_coef) return GB2D_ERR_ARG;
+  return phi_gradient(c, dt, d_phi);
+}
+
 int gb2d_poisson_assemble(gb2d_ctx* c, double dt, double* bx, double* by, double* diag, double* rhs) {
   if (!c || !std::isfinite(dt) || dt == 0.0) return GB2D_ERR_ARG;
   int rc = curvature_and_assemble(c, dt, nullptr);

@@ -220,6 +220,8 @@ void launch_projection_adjoint_rhs(cudaStream_t s, gb2d_ctx* c, double dt, int w
 void launch_projection_adjoint_vel(cudaStream_t s, gb2d_ctx* c, double dt, const double* z);
 // dL/d(water density), dL/d(air density) after the projection adjoint (z in c->xw).
 int density_gradient(gb2d_ctx* c, double dt, double* d_water, double* d_air);
+// dL/dphi (phi's layout, ghost 2) after the projection adjoint, into host_out.
+int phi_gradient(gb2d_ctx* c, double dt, double* host_out);
 
 // ---- gb2d_jump.cu (FP64, compiled without FMA contraction) ----
 int jump_buffers(gb2d_ctx* c);

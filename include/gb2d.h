@@ -258,6 +258,15 @@ int gb2d_projection_adjoint(gb2d_ctx* ctx, double dt, const double* lam_u, const
  * the velocity update's 1/rho: dL/drho = sum lam du'/drho|p + z (db/drho - dA/drho p).  Call
  * right after gb2d_projection_adjoint, which leaves z and the cotangents in the context. */
 int gb2d_projection_density_gradient(gb2d_ctx* ctx, double dt, double* d_water_density, double* d_air_density);
+/* dL/dphi of the same loss, after gb2d_projection_adjoint and before the state changes: the
+ * projection's dependence on the level set through the face weights (the |phi|-weighted
+ * harmonic mean of 1/rho in A and in the jump fluxes of b), the jump fluxes' |phi|-weighted
+ * interpolation of sigma kappa, the curvature kappa(phi) (zero slope where clamped), and the
+ * velocity update's interface faces (|phi|-weighted jump, smeared-Heaviside density); the
+ * phases (signs of phi) are piecewise constant.  The ghost extrapolation the projection
+ * starts with is reversed, so d_phi (PHI's layout, ghost 2) is the gradient with respect to
+ * the PHI the projection was given. */
+int gb2d_projection_phi_gradient(gb2d_ctx* ctx, double dt, double* d_phi);
 
 /* Batches: many independent simulations of uneven grid sizes on one GPU (no counterpart
  * in the reference, which runs one simulation per process).  Each instance is a full
