@@ -186,3 +186,60 @@ def buoyant_window_loss(gb, ni, nj, state, water, air, dt, steps, checkpoint_eve
         k += n
     loss = centroid_height(phi, ni, nj, state["x_max"], state["y_max"])
     return loss, c
+
+
+class Project(torch.autograd.Function):
+    """(u', v') = projection of a fixed intermediate velocity as a function of the level set
+    (PHI's layout, ghost 2) and the two densities (0-d tensors); backward through
+    gb2d_projection_adjoint, gb2d_projection_phi_gradient and gb2d_projection_density_gradient."""
+
+    @staticmethod
+    def forward(ctx, phi, water, air, make_context, state, dt, opts):
+        c = make_context(float(water), float(air))
+        c.set(FIELD_PHI, _np(phi.detach().contiguous()))
+        for f, k in ((FIELD_U, "u"), (FIELD_V, "v"), (FIELD_P, "p")):
+            c.set(f, state[k])
+        c.projection(dt, opts, allow_max_iters=True)
+        ctx.c, ctx.dt, ctx.opts = c, dt, opts
+        return torch.from_numpy(c.get(FIELD_U)), torch.from_numpy(c.get(FIELD_V))
+
+    @staticmethod
+    def backward(ctx, gu, gv):
+        c = ctx.c
+        c.projection_adjoint(ctx.dt, _np(gu.contiguous()), _np(gv.contiguous()), None, ctx.opts)
+        dphi = torch.from_numpy(c.projection_phi_gradient(ctx.dt))
+        dw, da = c.projection_density_gradient(ctx.dt)
+        c.close()
+        return (dphi, torch.tensor(dw, dtype=torch.float64), torch.tensor(da, dtype=torch.float64), None, None, None, None)
+
+
+def coupled_window_loss(gb, ni, nj, state, phi0, water, air, dt, steps, checkpoint_every=10, opts=None):
+    """The fully coupled window: the level set phi0 (PHI's layout) and the densities set the
+    projection of the intermediate velocity of one gravity step; the projected faces, copied
+    into the advecting velocity, carry phi0 through `steps` level-set TVD-RK3 steps
+    (reinitialisation off); the loss is the centroid height.  Differentiable in phi0 through
+    both paths (the projection's face weights, jump terms, curvature and velocity update, and
+    the WENO5 advection) and in the two densities."""
+    opts = opts or solve_opts(tolerance=1e-11, max_iterations=20000)
+
+    def make(w, a):
+        from . import Context
+        return Context(ni, nj, 0.0, 0.0, state["x_max"], state["y_max"], water_density=w, air_density=a,
+                       surface_tension=state.get("sigma", 0.0728))
+
+    u, v = Project.apply(phi0, water, air, make, state, dt, opts)
+    ua, va = advecting_copy(u), advecting_copy(v)
+    c = make(1000.0, 1.0)
+    phi = phi0
+    k = 0
+    while k < steps:
+        n = min(checkpoint_every, steps - k)
+
+        def segment(p, a_, b_, n=n):
+            for _ in range(n):
+                p = levelset_rk3_frozen(c, p, a_, b_, dt)
+            return p
+
+        phi = torch.utils.checkpoint.checkpoint(segment, phi, ua, va, use_reentrant=False)
+        k += n
+    return centroid_height(phi, ni, nj, state["x_max"], state["y_max"]), c

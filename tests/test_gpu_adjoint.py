@@ -303,3 +303,47 @@ def test_projection_phi_gradient(gb, name):
         fd = (4 * q(h / 2) - q(h)) / 3
         got = float(np.sum(grad * d))
         assert abs(got - fd) <= 1e-4 * max(abs(fd), 1e-9 * abs(L(phi0))), (k, got, fd)
+
+
+def test_coupled_window_phi_gradient(gb):
+    """The fully coupled window: the initial level set drives the projection (face weights,
+    jump terms, curvature, velocity update) and is advected 6 level-set RK3 steps by the
+    projected velocity; the centroid height's gradient in the initial level set, through both
+    paths, against central differences of the whole window along seeded smooth directions
+    (densities 3:1, sigma = 1; steps that keep every node's phase)."""
+    ag = importlib.import_module("2d_engine_gb300.autograd")
+    n = 33
+    case = rising_bubble_case(n, n, seed=15)
+    dt = 0.25 / 32
+    u = case["u"].copy()
+    v = case["v"].copy()
+    v[2:-2, 2:-2] += dt * -9.8
+    state = dict(u=u, v=v, p=case["p"], x_max=1.0, y_max=1.0, sigma=1.0)
+    opts = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=1e-13, max_iterations=20000)
+    phi0 = case["phi"].copy()
+    W, A = torch.tensor(3.0, dtype=torch.float64), torch.tensor(1.0, dtype=torch.float64)
+
+    def loss(phi, grad=False):
+        P = torch.from_numpy(phi.copy()).requires_grad_(grad)
+        L, c = ag.coupled_window_loss(gb, n, n, state, P, W, A, dt, steps=6, checkpoint_every=3, opts=opts)
+        if grad:
+            L.backward()
+            out = (float(L), P.grad.numpy().copy())
+        else:
+            out = float(L)
+        c.close()
+        return out
+
+    L0, g = loss(phi0, grad=True)
+    rng = np.random.default_rng(16)
+    inner = np.abs(phi0[2:2 + n, 2:2 + n])
+    y, x = np.mgrid[0:n, 0:n]
+    for k in range(2):
+        a, b, ph = rng.uniform(1, 3), rng.uniform(1, 3), rng.uniform(0, 2 * np.pi)
+        d = np.zeros_like(phi0)
+        d[2:2 + n, 2:2 + n] = np.sin(a * np.pi * x / n + ph) * np.cos(b * np.pi * y / n)
+        h = 2e-2 * float(inner.min())
+        q = lambda s: (loss(phi0 + s * d) - loss(phi0 - s * d)) / (2 * s)
+        fd = (4 * q(h / 2) - q(h)) / 3
+        got = float(np.sum(g * d))
+        assert abs(got - fd) <= 1e-4 * max(abs(fd), 1e-9 * abs(L0)), (k, got, fd)
