@@ -112,6 +112,7 @@ def library():
         "gb2d_jump_poisson_solve": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, O, S],
         "gb2d_projection_density_gradient": [vp, d, ctypes.POINTER(d), ctypes.POINTER(d)],
         "gb2d_projection_phi_gradient": [vp, d, vp],
+        "gb2d_velocity_advection_adjoint": [vp, d, vp, vp, vp, vp],
         "gb2d_projection_host": [vp, d, O, vp, vp, vp, vp, vp, vp, vp, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
@@ -405,6 +406,15 @@ class Context:
         w, a = ctypes.c_double(), ctypes.c_double()
         self._check(self.L.gb2d_projection_density_gradient(self.h, dt, ctypes.byref(w), ctypes.byref(a)))
         return w.value, a.value
+
+    def velocity_advection_adjoint(self, dt, lam_u, lam_v):
+        """VJP of the last velocity_advection: (mu_ua, mu_va), the cotangents of the advecting
+        copies UA, VA (gb2d_velocity_advection_adjoint)."""
+        lam_u = np.ascontiguousarray(lam_u, dtype=np.float64)
+        lam_v = np.ascontiguousarray(lam_v, dtype=np.float64)
+        mu_ua, mu_va = np.zeros(self.shape(FIELD_UA)), np.zeros(self.shape(FIELD_VA))
+        self._check(self.L.gb2d_velocity_advection_adjoint(self.h, dt, _ptr(lam_u), _ptr(lam_v), _ptr(mu_ua), _ptr(mu_va)))
+        return mu_ua, mu_va
 
     def projection_phi_gradient(self, dt):
         """dL/dphi (PHI's shape) of the loss of the last projection_adjoint (gb2d_projection_phi_gradient)."""

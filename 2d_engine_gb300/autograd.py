@@ -243,3 +243,20 @@ def coupled_window_loss(gb, ni, nj, state, phi0, water, air, dt, steps, checkpoi
         phi = torch.utils.checkpoint.checkpoint(segment, phi, ua, va, use_reentrant=False)
         k += n
     return centroid_height(phi, ni, nj, state["x_max"], state["y_max"]), c
+
+
+def ghost_copy_transpose(mu, nI, nJ, g_src=2, g_dst=3):
+    """Transpose of the ghost-filled copy (FillGhostCellsFrom: interior copied, each ghost layer the
+    second interior line, corners left alone) of a field with ghost g_src into one with ghost
+    g_dst: the cotangent mu of the copy (ghost g_dst layout) summed back onto the source's cells
+    (ghost g_src layout).  numpy, float64."""
+    out = np.zeros((nJ + 2 * g_src, nI + 2 * g_src))
+    inner = mu[g_dst:g_dst + nJ, g_dst:g_dst + nI]
+    out[g_src:g_src + nJ, g_src:g_src + nI] += inner
+    rows = mu[g_dst:g_dst + nJ, :]                    # in-range rows, ghost columns
+    out[g_src:g_src + nJ, g_src + 1] += rows[:, :g_dst].sum(axis=1)
+    out[g_src:g_src + nJ, g_src + nI - 2] += rows[:, g_dst + nI:].sum(axis=1)
+    cols = mu[:, g_dst:g_dst + nI]                    # in-range columns, ghost rows
+    out[g_src + 1, g_src:g_src + nI] += cols[:g_dst, :].sum(axis=0)
+    out[g_src + nJ - 2, g_src:g_src + nI] += cols[g_dst + nJ:, :].sum(axis=0)
+    return out

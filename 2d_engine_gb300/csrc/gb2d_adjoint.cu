@@ -571,6 +571,131 @@ __global__ void k_phi_grad_gather(PhiView v, PhiArgs a, const double* __restrict
   }
 }
 
+// ---- ENO3 velocity advection (the FP64 forms of k_eno3) -------------------------------
+//
+// u'_f = u_f - dt (uu f_x + vv f_y) on every face of both MAC components, f_x the upwind
+// ENO3 one-sided derivative of the advected component's copy (UA or VA) along x, f_y along
+// y, uu and vv the face's advecting velocities (its own copy value or a 4-face average).  With
+// the divided-difference choices and the upwind sides held (piecewise constant), f_x and f_y
+// are linear in their seven stencil values.  Per face: its 14 stencil coefficients times
+// lam (-dt uu) / lam (-dt vv) and its two velocity shares lam (-dt f_x), lam (-dt f_y); then
+// per cell of UA and VA a gather over the faces that read it.
+struct EnoAdjArgs {
+  int ni, nj;
+  Space xs, ys;
+  double o3[2][2];
+  double dt;
+};
+
+// eno3_select's four choices, and its formulas for any d with those choices.
+__device__ __forceinline__ void eno3_flags(const double d[6], double o2, double o3, bool f[4]) {
+  const double d2n2 = o2 * (d[1] - d[0]), d2n1 = o2 * (d[2] - d[1]), d20 = o2 * (d[3] - d[2]);
+  const double d2p1 = o2 * (d[4] - d[3]), d2p2 = o2 * (d[5] - d[4]);
+  const double d3n2 = o3 * (d2n1 - d2n2), d3n1 = o3 * (d20 - d2n1), d30 = o3 * (d2p1 - d20), d3p1 = o3 * (d2p2 - d2p1);
+  f[0] = mag_le(d2n1, d20);
+  f[1] = f[0] ? mag_le(d3n2, d3n1) : mag_le(d3n1, d30);
+  f[2] = mag_le(d20, d2p1);
+  f[3] = f[2] ? mag_le(d3n1, d30) : mag_le(d30, d3p1);
+}
+__device__ __forceinline__ void eno3_apply(const double d[6], const bool f[4], double o2, double o3, double h, double& dm, double& dp) {
+  const double d1n1 = d[2], d10 = d[3];
+  const double d2n2 = o2 * (d[1] - d[0]), d2n1 = o2 * (d[2] - d[1]), d20 = o2 * (d[3] - d[2]);
+  const double d2p1 = o2 * (d[4] - d[3]), d2p2 = o2 * (d[5] - d[4]);
+  const double d3n2 = o3 * (d2n1 - d2n2), d3n1 = o3 * (d20 - d2n1), d30 = o3 * (d2p1 - d20), d3p1 = o3 * (d2p2 - d2p1);
+  if (f[0])
+    dm = d1n1 + d2n1 * h + 2.0 * (f[1] ? d3n2 : d3n1) * h * h;
+  else
+    dm = d1n1 + d20 * h - (f[1] ? d3n1 : d30) * h * h;
+  if (f[2])
+    dp = d10 - d20 * h - (f[3] ? d3n1 : d30) * h * h;
+  else
+    dp = d10 - d2p1 * h + 2.0 * (f[3] ? d30 : d3p1) * h * h;
+}
+// The coefficients of the chosen dm and dp on q[0..6] (d_k = o (q_{k+1} - q_k)).
+__device__ void eno3_coef(const double q[7], double o, double o2, double o3, double h, double cm[7], double cp[7]) {
+  double d[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) d[k] = o * (q[k + 1] - q[k]);
+  bool f[4];
+  eno3_flags(d, o2, o3, f);
+  double am[6], ap[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double e[6] = {0, 0, 0, 0, 0, 0};
+    e[k] = 1.0;
+    eno3_apply(e, f, o2, o3, h, am[k], ap[k]);
+  }
+#pragma unroll
+  for (int m = 0; m < 7; ++m) {
+    cm[m] = o * ((m > 0 ? am[m - 1] : 0.0) - (m < 6 ? am[m] : 0.0));
+    cp[m] = o * ((m > 0 ? ap[m - 1] : 0.0) - (m < 6 ? ap[m] : 0.0));
+  }
+}
+
+__global__ void k_eno3_adj_face(const double* __restrict__ ua_a, const double* __restrict__ va_a, const double* __restrict__ lu_a,
+                                const double* __restrict__ lv_a, double* __restrict__ co, EnoAdjArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const DField ua = dfield((double*)ua_a, 3, ni + 1, nj), va = dfield((double*)va_a, 3, ni, nj + 1);
+  const DField lu = dfield((double*)lu_a, 2, ni + 1, nj), lv = dfield((double*)lv_a, 2, ni, nj + 1);
+  auto face = [&](bool xc, int i, int j, double* out) {
+    const DField& g = xc ? ua : va;
+    const Space& s = xc ? a.xs : a.ys;
+    double qx[7], qy[7], cmx[7], cpx[7], cmy[7], cpy[7], mx, px, my, py;
+    for (int m = 0; m < 7; ++m) qx[m] = GB_AT(g, i - 3 + m, j);
+    for (int m = 0; m < 7; ++m) qy[m] = GB_AT(g, i, j - 3 + m);
+    eno3_pair(qx, s.odx, s.o2dx, a.o3[xc ? 0 : 1][0], s.dx, mx, px);
+    eno3_pair(qy, s.ody, s.o2dy, a.o3[xc ? 0 : 1][1], s.dy, my, py);
+    eno3_coef(qx, s.odx, s.o2dx, a.o3[xc ? 0 : 1][0], s.dx, cmx, cpx);
+    eno3_coef(qy, s.ody, s.o2dy, a.o3[xc ? 0 : 1][1], s.dy, cmy, cpy);
+    double uu, vv;
+    if (xc) {
+      uu = GB_AT(ua, i, j);
+      vv = (GB_AT(va, i, j) + GB_AT(va, i, j + 1) + GB_AT(va, i - 1, j) + GB_AT(va, i - 1, j + 1)) * 0.25;
+    } else {
+      uu = (GB_AT(ua, i, j - 1) + GB_AT(ua, i + 1, j - 1) + GB_AT(ua, i, j) + GB_AT(ua, i + 1, j)) * 0.25;
+      vv = GB_AT(va, i, j);
+    }
+    const bool ux = gtz(uu), vy = gtz(vv);
+    const double lam = xc ? GB_AT(lu, i, j) : GB_AT(lv, i, j), w = -a.dt * lam;
+    for (int m = 0; m < 7; ++m) {
+      out[m] = w * uu * (ux ? cmx[m] : cpx[m]);
+      out[7 + m] = w * vv * (vy ? cmy[m] : cpy[m]);
+    }
+    out[14] = w * (ux ? mx : px);
+    out[15] = w * (vy ? my : py);
+  };
+  const size_t nu = (size_t)(ni + 1) * nj;
+  GB_FOR_IJ(i, j, ni + 1, nj) face(true, i, j, co + 16 * ((size_t)j * (ni + 1) + i));
+  GB_FOR_IJ(i, j, ni, nj + 1) face(false, i, j, co + 16 * (nu + (size_t)j * ni + i));
+}
+
+__global__ void k_eno3_adj_gather(const double* __restrict__ co, double* __restrict__ mua_a, double* __restrict__ mva_a, EnoAdjArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const size_t nu = (size_t)(ni + 1) * nj;
+  DField mua = dfield(mua_a, 3, ni + 1, nj), mva = dfield(mva_a, 3, ni, nj + 1);
+  auto CU = [&](int i, int j, int k) -> double {  // x-face (i, j): 0 <= i <= ni, 0 <= j < nj
+    return (i >= 0 && i <= ni && j >= 0 && j < nj) ? co[16 * ((size_t)j * (ni + 1) + i) + k] : 0.0;
+  };
+  auto CV = [&](int i, int j, int k) -> double {  // y-face (i, j): 0 <= i < ni, 0 <= j <= nj
+    return (i >= 0 && i < ni && j >= 0 && j <= nj) ? co[16 * (nu + (size_t)j * ni + i) + k] : 0.0;
+  };
+  GB_FOR_IJ(ii, jj, ni + 7, nj + 7) {
+    const int i = ii - 3, j = jj - 3;
+    if (i <= ni + 3 && j <= nj + 2) {  // UA cell
+      double acc = CU(i, j, 14);
+      for (int m = 0; m < 7; ++m) acc += CU(i + 3 - m, j, m) + CU(i, j + 3 - m, 7 + m);
+      acc += 0.25 * (CV(i, j, 14) + CV(i - 1, j, 14) + CV(i, j + 1, 14) + CV(i - 1, j + 1, 14));
+      GB_AT(mua, i, j) = acc;
+    }
+    if (i <= ni + 2 && j <= nj + 3) {  // VA cell
+      double acc = CV(i, j, 15);
+      for (int m = 0; m < 7; ++m) acc += CV(i + 3 - m, j, m) + CV(i, j + 3 - m, 7 + m);
+      acc += 0.25 * (CU(i, j, 15) + CU(i + 1, j, 15) + CU(i, j - 1, 15) + CU(i + 1, j - 1, 15));
+      GB_AT(mva, i, j) = acc;
+    }
+  }
+}
+
 }  // namespace
 
 int density_gradient(gb2d_ctx* c, double dt, double* d_water, double* d_air) {
@@ -629,7 +754,7 @@ int adjoint_buffers(gb2d_ctx* c) {
       {&c->adj_lam_phi, (ni + 4) * (nj + 4)}, {&c->adj_mu_phi, (ni + 4) * (nj + 4)},
       {&c->adj_lam_u, (ni + 5) * (nj + 4)},   {&c->adj_lam_v, (ni + 4) * (nj + 5)},
       {&c->adj_mu_u, (ni + 7) * (nj + 6)},    {&c->adj_mu_v, (ni + 6) * (nj + 7)},
-      {&c->adj_lam_p, (ni + 2) * (nj + 2)},
+      {&c->adj_lam_p, (ni + 2) * (nj + 2)},    {&c->adj_eno, 16 * ((ni + 1) * nj + ni * (nj + 1))},
   };
   for (auto& a : allocs) {
     cudaError_t e = cudaMalloc(a.p, a.n * sizeof(double));
@@ -739,6 +864,26 @@ int phi_gradient(gb2d_ctx* c, double dt, double* host_out) {
     snprintf(c->err, sizeof(c->err), "phi gradient: %s", cudaGetErrorString(e));
     return GB2D_ERR_CUDA;
   }
+  return GB2D_OK;
+}
+
+
+int eno3_adjoint(gb2d_ctx* c, double dt) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  EnoAdjArgs a;
+  a.ni = ni;
+  a.nj = nj;
+  a.xs = c->xs;
+  a.ys = c->ys;
+  a.dt = dt;
+  const Space* sp[2] = {&c->xs, &c->ys};
+  for (int g = 0; g < 2; ++g) {
+    a.o3[g][0] = sp[g]->odx / 3;
+    a.o3[g][1] = sp[g]->ody / 3;
+  }
+  k_eno3_adj_face<<<grid_ij(ni + 1, nj + 1), kThreads, 0, c->stream>>>(c->ua, c->va, c->adj_lam_u, c->adj_lam_v, c->adj_eno, a);
+  k_eno3_adj_gather<<<grid_ij(ni + 7, nj + 7), kThreads, 0, c->stream>>>(c->adj_eno, c->adj_mu_u, c->adj_mu_v, a);
+  GB_LAUNCHED(2);
   return GB2D_OK;
 }
 

@@ -124,7 +124,7 @@ void free_ctx(gb2d_ctx* c) {
   double* bufs[] = {c->phi_buf[0], c->phi_buf[1], c->phi_buf[2], c->phi_buf[3], c->u, c->v, c->ua, c->va, c->p,
                     c->kappa, c->sign, c->bx, c->by, c->diag, c->rhs, c->tmp_a, c->tmp_b, c->xw, c->u_alt, c->v_alt,
                     c->u_keep, c->v_keep, c->density, c->adj_coef, c->adj_gvel, c->adj_lam_phi, c->adj_mu_phi,
-                    c->adj_lam_u, c->adj_lam_v, c->adj_mu_u, c->adj_mu_v, c->adj_lam_p, c->jmp_dens, c->jmp_div,
+                    c->adj_lam_u, c->adj_lam_v, c->adj_mu_u, c->adj_mu_v, c->adj_lam_p, c->adj_eno, c->jmp_dens, c->jmp_div,
                     c->jmp_js, c->jmp_jd, c->jmp_nx, c->jmp_ny, c->jmp_phi};
   for (auto b : bufs)
     if (b) cudaFree(b);
@@ -787,6 +787,21 @@ int gb2d_jump_poisson_solve(gb2d_ctx* c, const double* density, const int* bc, c
 int gb2d_projection_density_gradient(gb2d_ctx* c, double dt, double* d_water_density, double* d_air_density) {
   if (!c || !std::isfinite(dt) || dt == 0.0 || !c->adj_coef) return GB2D_ERR_ARG;
   return density_gradient(c, dt, d_water_density, d_air_density);
+}
+
+int gb2d_velocity_advection_adjoint(gb2d_ctx* c, double dt, const double* lam_u, const double* lam_v, double* mu_ua, double* mu_va) {
+  if (!c || !lam_u || !lam_v || !mu_ua || !mu_va || !std::isfinite(dt)) return GB2D_ERR_ARG;
+  int rc = adjoint_buffers(c);
+  if (rc) return rc;
+  const size_t ni = c->grid.ni, nj = c->grid.nj;
+  const size_t nu = (ni + 5) * (nj + 4), nv = (ni + 4) * (nj + 5), nua = (ni + 7) * (nj + 6), nva = (ni + 6) * (nj + 7);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_u, lam_u, nu * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_v, lam_v, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  eno3_adjoint(c, dt);
+  if ((rc = check_launch(c, "velocity_advection_adjoint"))) return rc;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_ua, c->adj_mu_u, nua * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_va, c->adj_mu_v, nva * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return sync_check(c, "velocity_advection_adjoint");
 }
 
 int gb2d_projection_phi_gradient(gb2d_ctx* c, double dt, double* d_phi) {

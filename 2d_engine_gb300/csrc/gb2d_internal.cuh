@@ -161,6 +161,7 @@ struct gb2d_ctx {
   double *adj_lam_u, *adj_lam_v;      // cotangents of U, V (ghost 2)
   double *adj_mu_u, *adj_mu_v;        // results for U/V (ghost 2) or UA/VA (ghost 3)
   double* adj_lam_p;                  // cotangent of p (ghost 1)
+  double* adj_eno;                    // ENO3 adjoint: 16 coefficients per face of both MAC grids
   // General jump-Poisson inputs (allocated by the first gb2d_jump_poisson_solve)
   double *jmp_dens, *jmp_div, *jmp_js, *jmp_jd, *jmp_nx, *jmp_ny, *jmp_phi;
   int* jmp_bc;
@@ -222,6 +223,9 @@ void launch_projection_adjoint_vel(cudaStream_t s, gb2d_ctx* c, double dt, const
 int density_gradient(gb2d_ctx* c, double dt, double* d_water, double* d_air);
 // dL/dphi (phi's layout, ghost 2) after the projection adjoint, into host_out.
 int phi_gradient(gb2d_ctx* c, double dt, double* host_out);
+// VJP of the last velocity advection (the FP64 forms of ENO3) at the current UA, VA: cotangents
+// adj_lam_u / adj_lam_v of the advected U, V -> adj_mu_u / adj_mu_v on UA / VA (ghost 3).
+int eno3_adjoint(gb2d_ctx* c, double dt);
 
 // ---- gb2d_jump.cu (FP64, compiled without FMA contraction) ----
 int jump_buffers(gb2d_ctx* c);

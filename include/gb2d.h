@@ -267,6 +267,14 @@ int gb2d_projection_density_gradient(gb2d_ctx* ctx, double dt, double* d_water_d
  * starts with is reversed, so d_phi (PHI's layout, ghost 2) is the gradient with respect to
  * the PHI the projection was given. */
 int gb2d_projection_phi_gradient(gb2d_ctx* ctx, double dt, double* d_phi);
+/* VJP of the last gb2d_velocity_advection (the FP64 forms of ENO3; call before UA / VA
+ * change): lam_u, lam_v (U, V layouts) are the cotangents of the advected U, V; mu_ua, mu_va
+ * (UA, VA layouts, ghost 3) receive the cotangents of the advecting copies that step read
+ * (both as advected values and as advecting velocities).  The advected U, V also pass lam_u,
+ * lam_v straight through (u' = u - dt (...)), and UA / VA are the ghost-filled copies of U / V
+ * (FillGhostCellsFrom): a caller maps mu_ua, mu_va back onto U, V through that copy's transpose. */
+int gb2d_velocity_advection_adjoint(gb2d_ctx* ctx, double dt, const double* lam_u, const double* lam_v, double* mu_ua,
+                                    double* mu_va);
 
 /* Batches: many independent simulations of uneven grid sizes on one GPU (no counterpart
  * in the reference, which runs one simulation per process).  Each instance is a full
