@@ -260,3 +260,96 @@ def ghost_copy_transpose(mu, nI, nJ, g_src=2, g_dst=3):
     out[g_src + 1, g_src:g_src + nI] += cols[:g_dst, :].sum(axis=0)
     out[g_src + nJ - 2, g_src:g_src + nI] += cols[g_dst + nJ:, :].sum(axis=0)
     return out
+
+
+class VelocityAdvection(torch.autograd.Function):
+    """(u', v') = Velocity_Advection of (u, v): the advecting copies UA, VA refreshed from u, v,
+    then ENO3 on both MAC components (gb2d_velocity_advection, FP64 forms).  Backward:
+    gb2d_velocity_advection_adjoint on the copies, mapped back through the copy's transpose,
+    plus the identity part of u' = u - dt (...)."""
+
+    @staticmethod
+    def forward(ctx, u, v, make_context, dt):
+        c = make_context()
+        c.set(FIELD_U, _np(u.detach().contiguous()))
+        c.set(FIELD_V, _np(v.detach().contiguous()))
+        c.velocity_advection(dt)
+        ctx.c, ctx.dt = c, dt
+        return torch.from_numpy(c.get(FIELD_U)), torch.from_numpy(c.get(FIELD_V))
+
+    @staticmethod
+    def backward(ctx, gu, gv):
+        c = ctx.c
+        gu_np, gv_np = _np(gu.contiguous()), _np(gv.contiguous())
+        mu_ua, mu_va = c.velocity_advection_adjoint(ctx.dt, gu_np, gv_np)
+        ni, nj = c.ni, c.nj
+        du = gu_np + ghost_copy_transpose(mu_ua, ni + 1, nj)
+        dv = gv_np + ghost_copy_transpose(mu_va, ni, nj + 1)
+        c.close()
+        return torch.from_numpy(du), torch.from_numpy(dv), None, None
+
+
+class ProjectVelocity(torch.autograd.Function):
+    """(u', v') = projection of (u, v) with level set phi and the two densities; backward through
+    gb2d_projection_adjoint (velocity), gb2d_projection_phi_gradient and
+    gb2d_projection_density_gradient.  p is the warm start (the solve's result does not depend
+    on it beyond its tolerance); the projected pressure is left in state["p"]."""
+
+    @staticmethod
+    def forward(ctx, phi, u, v, water, air, make_context, state, dt, opts):
+        c = make_context(float(water), float(air))
+        c.set(FIELD_PHI, _np(phi.detach().contiguous()))
+        c.set(FIELD_U, _np(u.detach().contiguous()))
+        c.set(FIELD_V, _np(v.detach().contiguous()))
+        c.set(FIELD_P, state["p"])
+        c.projection(dt, opts, allow_max_iters=True)
+        state["p"] = c.get(FIELD_P)
+        ctx.c, ctx.dt, ctx.opts = c, dt, opts
+        return torch.from_numpy(c.get(FIELD_U)), torch.from_numpy(c.get(FIELD_V))
+
+    @staticmethod
+    def backward(ctx, gu, gv):
+        c = ctx.c
+        mu, mv, _ = c.projection_adjoint(ctx.dt, _np(gu.contiguous()), _np(gv.contiguous()), None, ctx.opts, allow_max_iters=True)
+        dphi = c.projection_phi_gradient(ctx.dt)
+        dw, da = c.projection_density_gradient(ctx.dt)
+        c.close()
+        t = lambda x: torch.tensor(x, dtype=torch.float64)
+        return (torch.from_numpy(dphi), torch.from_numpy(mu), torch.from_numpy(mv), t(dw), t(da), None, None, None, None)
+
+
+def gravity_walls(u, v, dt, gravity=(0.0, -9.8), g=2):
+    """The flow stage without viscosity (k_flow with gravity and walls): every interior face
+    gains dt * gravity, then the wall-normal faces (U at i = 0 and i = ni, V at j = 0 and
+    j = nj) become zero; ghost faces are left as they are.  Differentiable."""
+    nj, ni1 = u.shape[0] - 2 * g, u.shape[1] - 2 * g
+    nj1, ni = v.shape[0] - 2 * g, v.shape[1] - 2 * g
+    u2, v2 = u.clone(), v.clone()
+    u2[g:g + nj, g:g + ni1] = u[g:g + nj, g:g + ni1] + dt * gravity[0]
+    v2[g:g + nj1, g:g + ni] = v[g:g + nj1, g:g + ni] + dt * gravity[1]
+    u2[g:g + nj, g] = 0.0
+    u2[g:g + nj, g + ni1 - 1] = 0.0
+    v2[g, g:g + ni] = 0.0
+    v2[g + nj1 - 1, g:g + ni] = 0.0
+    return u2, v2
+
+
+def time_step(gb_ls, phi, u, v, ua, va, water, air, dt, make_context, state, opts, gravity=(0.0, -9.8)):
+    """One order-3 AdvanceOneTimeStepThread (EULERIAN_FLUID_SOLVER_2D.h:1694-1794) with the
+    reinitialisation off and no viscosity, as autograd operations: the level-set TVD-RK3 in the
+    advecting copies ua, va of the previous step's last velocity stage, then the velocity
+    TVD-RK3 of three SolveForRK stages (ENO3 advection, gravity and walls, projection).
+    Returns the new (phi, u, v) and the advecting copies the last stage read (the next step's
+    ua, va).  Differentiable in phi, u, v, ua, va and the two densities."""
+    phi = levelset_rk3_frozen(gb_ls, phi, ua, va, dt)
+    uk, vk = u, v
+    for stage in range(3):
+        ua, va = advecting_copy(u), advecting_copy(v)
+        u, v = VelocityAdvection.apply(u, v, lambda: make_context(1000.0, 1.0), dt)
+        u, v = gravity_walls(u, v, dt, gravity)
+        u, v = ProjectVelocity.apply(phi, u, v, water, air, make_context, state, dt, opts)
+        if stage == 1:
+            u, v = 0.75 * uk + 0.25 * u, 0.75 * vk + 0.25 * v
+        elif stage == 2:
+            u, v = (1 / 3.0) * uk + (2 / 3.0) * u, (1 / 3.0) * vk + (2 / 3.0) * v
+    return phi, u, v, ua, va

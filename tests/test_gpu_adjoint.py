@@ -387,3 +387,71 @@ def test_velocity_advection_adjoint(gb):
         got = float(np.sum(gu * du) + np.sum(gv * dv))
         assert abs(got - fd) <= 1e-6 * max(abs(fd), 1.0), (k, got, fd)
     c.close()
+
+
+def test_time_step_window_gradient(gb):
+    """Two whole order-3 time steps (level-set RK3, then three velocity stages of ENO3 advection,
+    gravity and walls, projection, with the RK3 blends; reinitialisation and viscosity off) as
+    autograd operations: the forward equals gb2d_advance_time_step, and the centroid height's
+    gradient in the initial level set and the initial x-velocity matches central differences of
+    the whole window (densities 3:1, sigma = 1; generic velocities; steps that change no phase
+    and no ENO choice)."""
+    ag = importlib.import_module("2d_engine_gb300.autograd")
+    n = 25
+    case = rising_bubble_case(n, n, seed=19)
+    rng = np.random.default_rng(20)
+    dt = 0.2 / (n - 1)
+    u0 = case["u"] * 5.0 + 0.1 * rng.standard_normal(case["u"].shape)
+    v0 = case["v"] * 5.0 + 0.1 * rng.standard_normal(case["v"].shape)
+    ua0, va0 = ag.advecting_copy(torch.from_numpy(u0)).numpy(), ag.advecting_copy(torch.from_numpy(v0)).numpy()
+    opts = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=1e-13, max_iterations=20000)
+    kw = dict(surface_tension=1.0, advection_precision=gb.PRECISION_FP64)
+
+    def make(w, a):
+        return gb.Context(n, n, water_density=w, air_density=a, **kw)
+
+    def window(phi, u, v, grad=False):
+        P, U, V = (torch.from_numpy(x.copy()).requires_grad_(grad) for x in (phi, u, v))
+        W, A = torch.tensor(3.0, dtype=torch.float64), torch.tensor(1.0, dtype=torch.float64)
+        ls = gb.Context(n, n, **kw)
+        state = {"p": case["p"].copy()}
+        p, uu, vv, ua, va = P, U, V, torch.from_numpy(ua0), torch.from_numpy(va0)
+        for _ in range(2):
+            p, uu, vv, ua, va = ag.time_step(ls, p, uu, vv, ua, va, W, A, dt, make, state, opts)
+        L = ag.centroid_height(p, n, n)
+        out = (float(L), p.detach().numpy().copy(), uu.detach().numpy().copy(), vv.detach().numpy().copy())
+        if grad:
+            L.backward()
+            out = out + (P.grad.numpy().copy(), U.grad.numpy().copy())
+        ls.close()
+        return out
+
+    # the forward against the library's own time step (0 reinitialisation sweeps, no viscosity)
+    c = gb.Context(n, n, water_density=3.0, air_density=1.0, reinit_iterations=0, **kw)
+    for f, x in ((gb.FIELD_PHI, case["phi"]), (gb.FIELD_U, u0), (gb.FIELD_V, v0), (gb.FIELD_P, case["p"]), (gb.FIELD_UA, ua0),
+                 (gb.FIELD_VA, va0)):
+        c.set(f, x)
+    for _ in range(2):
+        c.advance_time_step(dt, opts)
+    L0, phi_t, u_t, v_t, g_phi, g_u = window(case["phi"], u0, v0, grad=True)
+    it = (slice(2, 2 + n), slice(2, 2 + n))
+    assert np.abs(phi_t[it] - c.get(gb.FIELD_PHI)[it]).max() <= 1e-11
+    assert np.abs(u_t[2:2 + n, 2:3 + n] - c.get(gb.FIELD_U)[2:2 + n, 2:3 + n]).max() <= 1e-9
+    c.close()
+
+    phi0 = case["phi"]
+    inner = np.abs(phi0[it])
+    y, x = np.mgrid[0:n, 0:n]
+    d = np.zeros_like(phi0)
+    d[it] = np.sin(2.3 * np.pi * x / n + 0.4) * np.cos(1.7 * np.pi * y / n)
+    h = 2e-2 * float(inner.min())
+    q = lambda s: (window(phi0 + s * d, u0, v0)[0] - window(phi0 - s * d, u0, v0)[0]) / (2 * s)
+    fd = (4 * q(h / 2) - q(h)) / 3
+    got = float(np.sum(g_phi * d))
+    assert abs(got - fd) <= 1e-4 * max(abs(fd), 1e-9), ("phi", got, fd)
+    du = rng.standard_normal(u0.shape)
+    h = 1e-6
+    q = lambda s: (window(phi0, u0 + s * du, v0)[0] - window(phi0, u0 - s * du, v0)[0]) / (2 * s)
+    fd = (4 * q(h / 2) - q(h)) / 3
+    got = float(np.sum(g_u * du))
+    assert abs(got - fd) <= 1e-4 * max(abs(fd), 1e-9), ("u", got, fd)
