@@ -113,6 +113,8 @@ def library():
         "gb2d_projection_density_gradient": [vp, d, ctypes.POINTER(d), ctypes.POINTER(d)],
         "gb2d_projection_phi_gradient": [vp, d, vp],
         "gb2d_velocity_advection_adjoint": [vp, d, vp, vp, vp, vp],
+        "gb2d_reinit_sweep_apply": [vp, vp, vp, vp],
+        "gb2d_reinit_sweep_adjoint": [vp, vp, vp, vp, vp, vp],
         "gb2d_projection_host": [vp, d, O, vp, vp, vp, vp, vp, vp, vp, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
@@ -415,6 +417,21 @@ class Context:
         mu_ua, mu_va = np.zeros(self.shape(FIELD_UA)), np.zeros(self.shape(FIELD_VA))
         self._check(self.L.gb2d_velocity_advection_adjoint(self.h, dt, _ptr(lam_u), _ptr(lam_v), _ptr(mu_ua), _ptr(mu_va)))
         return mu_ua, mu_va
+
+    def reinit_sweep(self, phi, sign):
+        """One reinitialisation sweep of phi with S = sign (gb2d_reinit_sweep_apply)."""
+        phi = np.ascontiguousarray(phi, dtype=np.float64)
+        sign = np.ascontiguousarray(sign, dtype=np.float64)
+        out = np.empty(self.shape(FIELD_PHI))
+        self._check(self.L.gb2d_reinit_sweep_apply(self.h, _ptr(phi), _ptr(sign), _ptr(out)))
+        return out
+
+    def reinit_sweep_adjoint(self, phi, sign, lam):
+        """VJP of reinit_sweep at (phi, sign): (mu_phi, mu_sign) (gb2d_reinit_sweep_adjoint)."""
+        phi, sign, lam = (np.ascontiguousarray(x, dtype=np.float64) for x in (phi, sign, lam))
+        mu, ms = np.empty(self.shape(FIELD_PHI)), np.empty((self.nj, self.ni))
+        self._check(self.L.gb2d_reinit_sweep_adjoint(self.h, _ptr(phi), _ptr(sign), _ptr(lam), _ptr(mu), _ptr(ms)))
+        return mu, ms
 
     def projection_phi_gradient(self, dt):
         """dL/dphi (PHI's shape) of the loss of the last projection_adjoint (gb2d_projection_phi_gradient)."""

@@ -87,6 +87,55 @@ def levelset_rk3_frozen(gb_ctx, phi, ua, va, dt):
     return p5
 
 
+class ReinitSweep(torch.autograd.Function):
+    """phi' = one WENO5thReinitialization sweep (ADVECTION_METHOD_2D.h:1401-1658) of phi with the
+    sign field S held (gb2d_reinit_sweep_apply; backward gb2d_reinit_sweep_adjoint)."""
+
+    @staticmethod
+    def forward(ctx, phi, sign, gb_ctx):
+        out = torch.from_numpy(gb_ctx.reinit_sweep(_np(phi), _np(sign)))
+        ctx.save_for_backward(phi, sign)
+        ctx.gb = gb_ctx
+        return out
+
+    @staticmethod
+    def backward(ctx, grad):
+        phi, sign = ctx.saved_tensors
+        mu, ms = ctx.gb.reinit_sweep_adjoint(_np(phi), _np(sign), _np(grad.contiguous()))
+        return torch.from_numpy(mu), torch.from_numpy(ms), None
+
+
+def reinitialization(gb_ctx, phi):
+    """LEVELSET_2D Reinitialization (EULERIAN_FLUID_SOLVER_2D.h:2425-2445): S = phi / sqrt(phi^2 +
+    dx^2) of the starting level set, then the context's reinit_iterations sweeps with pseudo time
+    step dx / reinit_scaling.  S is a torch expression, so the sweeps' derivative in S flows back
+    into the starting level set."""
+    g = gb_ctx.grid
+    dx = (g.x_max - g.x_min) / (gb_ctx.ni - 1)
+    p = phi[_interior(gb_ctx.ni, gb_ctx.nj)]
+    sign = p / torch.sqrt(p * p + dx * dx)
+    for _ in range(gb_ctx.params.reinit_iterations):
+        phi = ReinitSweep.apply(phi, sign, gb_ctx)
+    return phi
+
+
+def _blend(keep, phi, c0, c1, it):
+    out = phi.clone()
+    out[it] = c0 * keep[it] + c1 * phi[it]
+    return out
+
+
+def levelset_rk3(gb_ctx, phi, ua, va, dt):
+    """The whole level-set update of one order-3 time step (EULERIAN_FLUID_SOLVER_2D.h:1694-1741):
+    the advection TVD-RK3, then the reinitialisation TVD-RK3 of three Reinitialization calls with
+    the interior blends; the forward equals gb2d_levelset_rk3 (to the rounding of S)."""
+    it = _interior(gb_ctx.ni, gb_ctx.nj)
+    b = levelset_rk3_frozen(gb_ctx, phi, ua, va, dt)
+    r = reinitialization(gb_ctx, reinitialization(gb_ctx, b))
+    r = reinitialization(gb_ctx, _blend(b, r, 0.75, 0.25, it))
+    return _blend(b, r, 1 / 3.0, 2 / 3.0, it)
+
+
 def centroid_height(phi, ni, nj, x_max=1.0, y_max=1.0, eps=None):
     """Bubble centroid height  sum y H(-phi) / sum H(-phi)  over the nodes, with the
     smeared Heaviside of width 1.5 dx (a differentiable indicator of phi < 0)."""

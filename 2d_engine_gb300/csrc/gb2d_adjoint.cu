@@ -115,6 +115,90 @@ __global__ void k_weno5_adj_coef(const double* __restrict__ phi_a, const double*
   }
 }
 
+// One reinitialisation sweep (the FP64 form of k_reinit_sweep): phi' = phi - dtau S h on the
+// interior where the Godunov selection yields h = |grad phi| - 1 over the chosen one-sided WENO5
+// derivatives, phi' = phi elsewhere and on the ghost ring.  With the selections held, per
+// interior node: C[m] = -dtau S lam dh/dq_m along x (m = 0..6) and y (7..13), and the
+// cotangent of S, -dtau h lam.  Gathered by k_weno5_adj_gather.
+__global__ void k_reinit_adj_coef(const double* __restrict__ phi_a, const double* __restrict__ S, const double* __restrict__ lam_a,
+                                  double* __restrict__ coef, double* __restrict__ gS, AdjArgs a, double dtau) {
+  const int ni = a.ni, nj = a.nj;
+  const DField phi = dfield((double*)phi_a, 2, ni, nj), lam = dfield((double*)lam_a, 2, ni, nj);
+  const size_t n = (size_t)ni * nj;
+  GB_FOR_IJ(i, j, ni, nj) {
+    const size_t t = (size_t)j * ni + i;
+    double qx[7], qy[7], Jmx[7], Jpx[7], Jmy[7], Jpy[7], mx, px, my, py;
+#pragma unroll
+    for (int m = 0; m < 7; ++m) qx[m] = GB_AT(phi, clamp_line(i - 3 + m, ni), j);
+#pragma unroll
+    for (int m = 0; m < 7; ++m) qy[m] = GB_AT(phi, i, clamp_line(j - 3 + m, nj));
+    weno5_line_grad(qx, a.odx, a.eps, true, mx, Jmx);
+    weno5_line_grad(qx, a.odx, a.eps, false, px, Jpx);
+    weno5_line_grad(qy, a.ody, a.eps, true, my, Jmy);
+    weno5_line_grad(qy, a.ody, a.eps, false, py, Jpy);
+    const double s = S[t], l = GB_AT(lam, i, j);
+    double h = 0.0, dgx = 0.0, dgy = 0.0;  // dh / d(chosen x and y derivatives)
+    const double* Jx = Jmx;
+    const double* Jy = Jmy;
+    bool on = false;
+    {
+      // godunov_h<double>'s choices (ADVECTION_METHOD_2D.h:1505-1655)
+      const double smx = s * mx, spx = s * px, smy = s * my, spy = s * py;
+      int xs = -1, ys = -1;
+      if (gez(spx) && gez(smx))
+        xs = 0;
+      else if (lez(spx) && lez(smx))
+        xs = 1;
+      else if (gtz(spx) && ltz(smx))
+        xs = 2;
+      else if (ltz(spx) && gtz(smx)) {
+        const double sss = s * (fabs(px) - fabs(mx)) / (px - mx);
+        xs = gtz(sss) ? 0 : (ltz(sss) ? 1 : -1);
+      }
+      if (xs >= 0) {
+        if (gez(spy) && gez(smy))
+          ys = 0;
+        else if (lez(spy) && lez(smy))
+          ys = 1;
+        else if (gtz(spy) && ltz(smy))
+          ys = 2;
+        else if (ltz(spy) && gtz(smy)) {
+          const double ss = s * (fabs(py) - fabs(my)) / (py - my);
+          ys = gtz(ss) ? 0 : 1;
+        }
+      }
+      if (xs >= 0 && ys >= 0) {
+        on = true;
+        const double gx = xs == 0 ? mx : px, gy = ys == 0 ? my : py;
+        Jx = xs == 0 ? Jmx : Jpx;
+        Jy = ys == 0 ? Jmy : Jpy;
+        if (xs != 2 && ys != 2) {
+          const double r = sqrt(gx * gx + gy * gy);
+          h = r - 1.0;
+          if (r > 0) dgx = gx / r, dgy = gy / r;
+        } else if (xs != 2) {
+          const double r = sqrt(gx * gx);
+          h = r - 1.0;
+          if (r > 0) dgx = gx / r;
+        } else if (ys != 2) {
+          const double r = sqrt(gy * gy);
+          h = r - 1.0;
+          if (r > 0) dgy = gy / r;
+        } else {
+          h = -1.0;
+        }
+      }
+    }
+    const double w = on ? -dtau * s * l : 0.0;
+#pragma unroll
+    for (int m = 0; m < 7; ++m) {
+      coef[m * n + t] = w * dgx * Jx[m];
+      coef[(7 + m) * n + t] = w * dgy * Jy[m];
+    }
+    gS[t] = on ? -dtau * h * l : 0.0;
+  }
+}
+
 // Sum of the stencil coefficients that land on interior position k of one line:
 // position p of the ghost-filled copy feeds nodes within 3 of it; k = 1 also owns the
 // low ghost positions -1..-3, k = n-2 the high ones n..n+2.
@@ -883,6 +967,22 @@ int eno3_adjoint(gb2d_ctx* c, double dt) {
   }
   k_eno3_adj_face<<<grid_ij(ni + 1, nj + 1), kThreads, 0, c->stream>>>(c->ua, c->va, c->adj_lam_u, c->adj_lam_v, c->adj_eno, a);
   k_eno3_adj_gather<<<grid_ij(ni + 7, nj + 7), kThreads, 0, c->stream>>>(c->adj_eno, c->adj_mu_u, c->adj_mu_v, a);
+  GB_LAUNCHED(2);
+  return GB2D_OK;
+}
+
+
+int reinit_sweep_vjp(gb2d_ctx* c, const double* phi_dev, const double* sign_dev, const double* lam_dev, double* mu_dev, double* gs_dev) {
+  AdjArgs a;
+  a.ni = c->grid.ni;
+  a.nj = c->grid.nj;
+  a.odx = c->base.odx;
+  a.ody = c->base.ody;
+  a.eps = c->prm.weno_epsilon;
+  a.dt = 0.0;
+  const double dtau = c->base.dx / (double)c->prm.reinit_scaling;
+  k_reinit_adj_coef<<<grid_ij(a.ni, a.nj), kThreads, 0, c->stream>>>(phi_dev, sign_dev, lam_dev, c->adj_coef, gs_dev, a, dtau);
+  k_weno5_adj_gather<<<grid_ij(a.ni + 4, a.nj + 4), kThreads, 0, c->stream>>>(lam_dev, c->adj_coef, mu_dev, a);
   GB_LAUNCHED(2);
   return GB2D_OK;
 }

@@ -804,6 +804,34 @@ int gb2d_velocity_advection_adjoint(gb2d_ctx* c, double dt, const double* lam_u,
   return sync_check(c, "velocity_advection_adjoint");
 }
 
+int gb2d_reinit_sweep_apply(gb2d_ctx* c, const double* phi_in, const double* sign, double* phi_out) {
+  if (!c || !phi_in || !sign || !phi_out) return GB2D_ERR_ARG;
+  const size_t ni = c->grid.ni, nj = c->grid.nj, nphi = (ni + 4) * (nj + 4);
+  const int A = spare(c, c->phi_cur), B = spare(c, c->phi_cur, A);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->phi_buf[A], phi_in, nphi * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->sign, sign, ni * nj * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  launch_reinit_sweep(c->stream, c, c->phi_buf[A], c->phi_buf[B], c->sign, c->base.dx / (double)c->prm.reinit_scaling,
+                      c->prm.advection_precision == GB2D_PRECISION_MIXED);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(phi_out, c->phi_buf[B], nphi * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return sync_check(c, "reinit_sweep_apply");
+}
+
+int gb2d_reinit_sweep_adjoint(gb2d_ctx* c, const double* phi_in, const double* sign, const double* lam, double* mu_phi, double* mu_sign) {
+  if (!c || !phi_in || !sign || !lam || !mu_phi || !mu_sign) return GB2D_ERR_ARG;
+  int rc = adjoint_buffers(c);
+  if (rc) return rc;
+  const size_t ni = c->grid.ni, nj = c->grid.nj, nphi = (ni + 4) * (nj + 4);
+  const int A = spare(c, c->phi_cur);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->phi_buf[A], phi_in, nphi * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->sign, sign, ni * nj * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_phi, lam, nphi * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  reinit_sweep_vjp(c, c->phi_buf[A], c->sign, c->adj_lam_phi, c->adj_mu_phi, c->adj_gvel);
+  if ((rc = check_launch(c, "reinit_sweep_adjoint"))) return rc;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_phi, c->adj_mu_phi, nphi * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_sign, c->adj_gvel, ni * nj * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return sync_check(c, "reinit_sweep_adjoint");
+}
+
 int gb2d_projection_phi_gradient(gb2d_ctx* c, double dt, double* d_phi) {
   if (!c || !d_phi || !std::isfinite(dt) || dt == 0.0 || !c->adj_coef) return GB2D_ERR_ARG;
   return phi_gradient(c, dt, d_phi);

@@ -226,6 +226,9 @@ int phi_gradient(gb2d_ctx* c, double dt, double* host_out);
 // VJP of the last velocity advection (the FP64 forms of ENO3) at the current UA, VA: cotangents
 // adj_lam_u / adj_lam_v of the advected U, V -> adj_mu_u / adj_mu_v on UA / VA (ghost 3).
 int eno3_adjoint(gb2d_ctx* c, double dt);
+// VJP of one reinitialisation sweep (FP64 form) at phi (device, ghost 2) and S (device, ni x nj):
+// lam (device, ghost 2) -> mu (device, ghost 2) and the cotangent of S into gs (device, ni x nj).
+int reinit_sweep_vjp(gb2d_ctx* c, const double* phi, const double* sign, const double* lam, double* mu, double* gs);
 
 // ---- gb2d_jump.cu (FP64, compiled without FMA contraction) ----
 int jump_buffers(gb2d_ctx* c);

@@ -275,6 +275,17 @@ int gb2d_projection_phi_gradient(gb2d_ctx* ctx, double dt, double* d_phi);
  * (FillGhostCellsFrom): a caller maps mu_ua, mu_va back onto U, V through that copy's transpose. */
 int gb2d_velocity_advection_adjoint(gb2d_ctx* ctx, double dt, const double* lam_u, const double* lam_v, double* mu_ua,
                                     double* mu_va);
+/* One WENO5-Godunov reinitialisation sweep (the sweep gb2d_reinitialization repeats) of phi_in
+ * (PHI's layout) with the given S (ni x nj, S = phi / sqrt(phi^2 + dx^2) of the level set the
+ * Reinitialization started from) into phi_out, in the context's advection precision; the
+ * context's own PHI is not touched.  With gb2d_reinit_sweep_adjoint, the building block of a
+ * differentiable Reinitialization (the sweeps' S is held, and its own derivative is the
+ * caller's). */
+int gb2d_reinit_sweep_apply(gb2d_ctx* ctx, const double* phi_in, const double* sign, double* phi_out);
+/* VJP of that sweep (FP64 form) at phi_in, sign: lam (PHI's layout) -> mu_phi (PHI's layout) and
+ * mu_sign (ni x nj, the cotangent of S). */
+int gb2d_reinit_sweep_adjoint(gb2d_ctx* ctx, const double* phi_in, const double* sign, const double* lam, double* mu_phi,
+                              double* mu_sign);
 
 /* Batches: many independent simulations of uneven grid sizes on one GPU (no counterpart
  * in the reference, which runs one simulation per process).  Each instance is a full

@@ -455,3 +455,70 @@ def test_time_step_window_gradient(gb):
     fd = (4 * q(h / 2) - q(h)) / 3
     got = float(np.sum(g_u * du))
     assert abs(got - fd) <= 1e-4 * max(abs(fd), 1e-9), ("u", got, fd)
+
+
+def test_reinitialization_sweep_adjoint(gb):
+    """One reinitialisation sweep with S held: its VJP in phi and in S against central
+    differences along random directions (an off-centre bubble, so every Godunov case and both
+    WENO sides occur)."""
+    n = 40
+    case = rising_bubble_case(n, n, seed=21)
+    c = gb.Context(n, n, advection_precision=gb.PRECISION_FP64)
+    rng = np.random.default_rng(22)
+    phi = case["phi"]
+    p = phi[2:2 + n, 2:2 + n]
+    dx = 1.0 / (n - 1)
+    sign = p / np.sqrt(p * p + dx * dx)
+    lam = rng.standard_normal(phi.shape)
+    mu, ms = c.reinit_sweep_adjoint(phi, sign, lam)
+    for k in range(4):
+        d = rng.standard_normal(phi.shape)
+        fd = central(lambda x: float(np.sum(lam * c.reinit_sweep(x, sign))), phi, d, eps=1e-7)
+        ad = float(np.sum(mu * d))
+        assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-3 * np.linalg.norm(mu)), (k, ad, fd)
+        # Between sign changes of S the sweep is linear in S (the Godunov choices depend on S's
+        # sign only), so a wide step has no truncation error and keeps rounding (the step moves
+        # the output by dtau * h * step) well below the tolerance.
+        e = rng.standard_normal(sign.shape)
+        fd = central(lambda x: float(np.sum(lam * c.reinit_sweep(phi, x))), sign, e, eps=1e-5)
+        ad = float(np.sum(ms * e))
+        assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-3 * np.linalg.norm(ms)), (k, ad, fd)
+    c.close()
+
+
+def test_levelset_rk3_with_reinitialization_gradient(gb):
+    """Centroid height after two whole level-set updates (advection TVD-RK3 plus the
+    reinitialisation TVD-RK3, 3 sweeps per Reinitialization): the autograd forward equals
+    gb2d_levelset_rk3, and the gradient in the starting level set matches central
+    differences."""
+    ag = importlib.import_module("2d_engine_gb300.autograd")
+    case, dt = window_case()
+    c = gb.Context(33, 33, reinit_iterations=3)
+    ua, va = torch.from_numpy(case["ua"]), torch.from_numpy(case["va"])
+    c.set(gb.FIELD_PHI, case["phi"])
+    c.set(gb.FIELD_UA, case["ua"])
+    c.set(gb.FIELD_VA, case["va"])
+    c.levelset_rk3(dt)
+    want = c.get(gb.FIELD_PHI)
+    with torch.no_grad():
+        got = ag.levelset_rk3(c, torch.from_numpy(case["phi"].copy()), ua, va, dt).numpy()
+    np.testing.assert_allclose(got[2:-2, 2:-2], want[2:-2, 2:-2], rtol=0, atol=1e-13)
+
+    def loss(p):
+        for _ in range(2):
+            p = ag.levelset_rk3(c, p, ua, va, dt)
+        return ag.centroid_height(p, 33, 33)
+
+    phi0 = torch.from_numpy(case["phi"].copy()).requires_grad_(True)
+    loss(phi0).backward()
+    grad = phi0.grad.numpy().copy()
+    rng = np.random.default_rng(23)
+    with torch.no_grad():
+        f = lambda p: float(loss(torch.from_numpy(p)))
+        for k in range(6):
+            d = rng.standard_normal(case["phi"].shape)
+            d /= np.linalg.norm(d)
+            fd = central(f, case["phi"], d)
+            ad = float(np.sum(grad * d))
+            assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-3 * np.linalg.norm(grad)), (k, ad, fd)
+    c.close()
