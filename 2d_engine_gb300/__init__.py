@@ -115,6 +115,7 @@ def library():
         "gb2d_velocity_advection_adjoint": [vp, d, vp, vp, vp, vp],
         "gb2d_reinit_sweep_apply": [vp, vp, vp, vp],
         "gb2d_reinit_sweep_adjoint": [vp, vp, vp, vp, vp, vp],
+        "gb2d_viscosity_adjoint": [vp, d, vp, vp, vp, vp, vp, vp],
         "gb2d_projection_host": [vp, d, O, vp, vp, vp, vp, vp, vp, vp, S],
         "gb2d_poisson_assemble": [vp, d, vp, vp, vp, vp],
         "gb2d_poisson_apply": [vp, vp, vp],
@@ -432,6 +433,15 @@ class Context:
         mu, ms = np.empty(self.shape(FIELD_PHI)), np.empty((self.nj, self.ni))
         self._check(self.L.gb2d_reinit_sweep_adjoint(self.h, _ptr(phi), _ptr(sign), _ptr(lam), _ptr(mu), _ptr(ms)))
         return mu, ms
+
+    def viscosity_adjoint(self, dt, lam_u, lam_v):
+        """VJP of the sourcing's viscosity at the context's PHI, U, V:
+        (mu_u, mu_v, mu_phi, (dL/d water_density, dL/d air_density))."""
+        lu, lv = (np.ascontiguousarray(x, dtype=np.float64) for x in (lam_u, lam_v))
+        mu, mv, mp = np.empty(self.shape(FIELD_U)), np.empty(self.shape(FIELD_V)), np.empty(self.shape(FIELD_PHI))
+        dd = np.empty(2)
+        self._check(self.L.gb2d_viscosity_adjoint(self.h, dt, _ptr(lu), _ptr(lv), _ptr(mu), _ptr(mv), _ptr(mp), _ptr(dd)))
+        return mu, mv, mp, (float(dd[0]), float(dd[1]))
 
     def projection_phi_gradient(self, dt):
         """dL/dphi (PHI's shape) of the loss of the last projection_adjoint (gb2d_projection_phi_gradient)."""

@@ -367,15 +367,19 @@ class ProjectVelocity(torch.autograd.Function):
         return (torch.from_numpy(dphi), torch.from_numpy(mu), torch.from_numpy(mv), t(dw), t(da), None, None, None, None)
 
 
-def gravity_walls(u, v, dt, gravity=(0.0, -9.8), g=2):
+def gravity_walls(u, v, dt, gravity=(0.0, -9.8), g=2, walls=True, gravity_on=True):
     """The flow stage without viscosity (k_flow with gravity and walls): every interior face
     gains dt * gravity, then the wall-normal faces (U at i = 0 and i = ni, V at j = 0 and
-    j = nj) become zero; ghost faces are left as they are.  Differentiable."""
+    j = nj) become zero; ghost faces are left as they are.  Differentiable.  With viscosity the
+    stage is gravity (walls=False), Viscosity, then the walls (gravity_on=False)."""
     nj, ni1 = u.shape[0] - 2 * g, u.shape[1] - 2 * g
     nj1, ni = v.shape[0] - 2 * g, v.shape[1] - 2 * g
     u2, v2 = u.clone(), v.clone()
-    u2[g:g + nj, g:g + ni1] = u[g:g + nj, g:g + ni1] + dt * gravity[0]
-    v2[g:g + nj1, g:g + ni] = v[g:g + nj1, g:g + ni] + dt * gravity[1]
+    if gravity_on:
+        u2[g:g + nj, g:g + ni1] = u[g:g + nj, g:g + ni1] + dt * gravity[0]
+        v2[g:g + nj1, g:g + ni] = v[g:g + nj1, g:g + ni] + dt * gravity[1]
+    if not walls:
+        return u2, v2
     u2[g:g + nj, g] = 0.0
     u2[g:g + nj, g + ni1 - 1] = 0.0
     v2[g, g:g + ni] = 0.0
@@ -383,19 +387,74 @@ def gravity_walls(u, v, dt, gravity=(0.0, -9.8), g=2):
     return u2, v2
 
 
-def time_step(gb_ls, phi, u, v, ua, va, water, air, dt, make_context, state, opts, gravity=(0.0, -9.8)):
-    """One order-3 AdvanceOneTimeStepThread (EULERIAN_FLUID_SOLVER_2D.h:1694-1794) with the
-    reinitialisation off and no viscosity, as autograd operations: the level-set TVD-RK3 in the
-    advecting copies ua, va of the previous step's last velocity stage, then the velocity
-    TVD-RK3 of three SolveForRK stages (ENO3 advection, gravity and walls, projection).
-    Returns the new (phi, u, v) and the advecting copies the last stage read (the next step's
-    ua, va).  Differentiable in phi, u, v, ua, va and the two densities."""
-    phi = levelset_rk3_frozen(gb_ls, phi, ua, va, dt)
+class Viscosity(torch.autograd.Function):
+    """(u', v') = ApplyViscosity (VISCOSITY_2D.h:460-532) of (u, v) with the level set phi, as
+    gb2d_sourcing applies it (no gravity, no walls); backward gb2d_viscosity_adjoint, in u, v,
+    phi (the smeared viscosities and face densities) and the two densities.  make_context(w, a)
+    returns a context with those densities; flow holds set_flow_params' viscosities."""
+
+    @staticmethod
+    def forward(ctx, phi, u, v, water, air, make_context, flow, dt):
+        c = make_context(float(water), float(air))
+        c.set_flow_params(viscosity=True, **flow)
+        c.set(FIELD_PHI, _np(phi))
+        c.set(FIELD_U, _np(u))
+        c.set(FIELD_V, _np(v))
+        c.sourcing(dt)
+        out = torch.from_numpy(c.get(FIELD_U)), torch.from_numpy(c.get(FIELD_V))
+        c.set(FIELD_U, _np(u))  # the linearisation point: the stage's inputs
+        c.set(FIELD_V, _np(v))
+        ctx.c, ctx.dt = c, dt
+        return out
+
+    @staticmethod
+    def backward(ctx, gu, gv):
+        c = ctx.c
+        mu, mv, mp, (dw, da) = c.viscosity_adjoint(ctx.dt, _np(gu.contiguous()), _np(gv.contiguous()))
+        c.close()
+        t = lambda x: torch.tensor(x, dtype=torch.float64)
+        return torch.from_numpy(mp), torch.from_numpy(mu), torch.from_numpy(mv), t(dw), t(da), None, None, None
+
+
+def extrapolate_ghost1(phi, g=2):
+    """phi with its ghost-1 ring (not the corners) linearly extrapolated from the interior, as the
+    projection's in-place ghost extrapolation leaves it (k_extrapolate: 2 f(0) - f(1) on each
+    side).  Differentiable."""
+    nj, ni = phi.shape[0] - 2 * g, phi.shape[1] - 2 * g
+    out = phi.clone()
+    r = slice(g, g + nj)
+    c = slice(g, g + ni)
+    out[r, g - 1] = 2.0 * phi[r, g] - phi[r, g + 1]
+    out[r, g + ni] = 2.0 * phi[r, g + ni - 1] - phi[r, g + ni - 2]
+    out[g - 1, c] = 2.0 * phi[g, c] - phi[g + 1, c]
+    out[g + nj, c] = 2.0 * phi[g + nj - 1, c] - phi[g + nj - 2, c]
+    return out
+
+
+def time_step(gb_ls, phi, u, v, ua, va, water, air, dt, make_context, state, opts, gravity=(0.0, -9.8), reinit=False,
+              viscosity=None):
+    """One order-3 AdvanceOneTimeStepThread (EULERIAN_FLUID_SOLVER_2D.h:1694-1794) as autograd
+    operations: the level-set TVD-RK3 in the advecting copies ua, va of the previous step's last
+    velocity stage (with reinit, followed by the reinitialisation TVD-RK3 of gb_ls's
+    reinit_iterations sweeps), then the velocity TVD-RK3 of three SolveForRK stages (ENO3
+    advection, gravity, the explicit viscosity when `viscosity` holds set_flow_params'
+    viscosities, walls, projection).  Returns the new (phi, u, v) and the advecting copies the
+    last stage read (the next step's ua, va).  Differentiable in phi, u, v, ua, va and the two
+    densities."""
+    phi = levelset_rk3(gb_ls, phi, ua, va, dt) if reinit else levelset_rk3_frozen(gb_ls, phi, ua, va, dt)
     uk, vk = u, v
     for stage in range(3):
         ua, va = advecting_copy(u), advecting_copy(v)
         u, v = VelocityAdvection.apply(u, v, lambda: make_context(1000.0, 1.0), dt)
-        u, v = gravity_walls(u, v, dt, gravity)
+        if viscosity is None:
+            u, v = gravity_walls(u, v, dt, gravity)
+        else:
+            # Stage 1 reads the level set's ghosts as the level-set update left them; the later
+            # stages read them after the first projection's extrapolation.
+            u, v = gravity_walls(u, v, dt, gravity, walls=False)
+            u, v = Viscosity.apply(phi if stage == 0 else extrapolate_ghost1(phi), u, v, water, air, make_context, viscosity,
+                                   dt)
+            u, v = gravity_walls(u, v, dt, (0.0, 0.0), gravity_on=False)
         u, v = ProjectVelocity.apply(phi, u, v, water, air, make_context, state, dt, opts)
         if stage == 1:
             u, v = 0.75 * uk + 0.25 * u, 0.75 * vk + 0.25 * v

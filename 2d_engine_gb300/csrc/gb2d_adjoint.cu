@@ -780,6 +780,148 @@ __global__ void k_eno3_adj_gather(const double* __restrict__ co, double* __restr
   }
 }
 
+// ---- explicit viscosity adjoint ----
+// ApplyViscosity (VISCOSITY_2D.h:460-532) as k_flow's FP64 viscous branch without gravity and
+// walls (the Sourcing form): each new face value is t0 + coef * (stencil of the old faces), affine
+// in U, V, with coef = dt / rho(H(phi)) and the smeared viscosities mu(H(phi)) depending on phi.
+// Pass 1 stores per face of both MAC grids 13 cotangent-weighted numbers: the 7 velocity
+// coefficients (x-face: +x, -x, +y, -y neighbours, the two cross-term weights, self), 4 phi
+// weights (the two face nodes, the upper / lower (right / left) corner averages' quarter shares)
+// and the face's shares of dL / d rho_water and dL / d rho_air (through coef).
+// Pass 2 gathers them onto every face and node that each stencil read, in a fixed order.
+struct ViscAdjArgs {
+  int ni, nj;
+  double dt, odx, ody, eps, oe;
+  double mu_lo, mu_d, mu_at0, mu_at1, rho_lo, rho_d, coef0, coef1;
+};
+
+__device__ __forceinline__ double visc_mu(double l, const ViscAdjArgs& a) {
+  if (lt_neg(l, a.eps)) return a.mu_at0;
+  if (gt_pos(l, a.eps)) return a.mu_at1;
+  return a.mu_lo + a.mu_d * heaviside_band(l, a.oe);
+}
+// coef = dt / rho(H(l)), its slope in l, and its partials in the water and air densities.
+__device__ __forceinline__ double visc_coef(double l, const ViscAdjArgs& a, double& dcoef, double& dw, double& da) {
+  const double H = lt_neg(l, a.eps) ? 0.0 : (gt_pos(l, a.eps) ? 1.0 : heaviside_band(l, a.oe));
+  const double r = a.rho_lo + a.rho_d * H;
+  dw = -a.dt * H / (r * r);
+  da = -a.dt * (1.0 - H) / (r * r);
+  if (lt_neg(l, a.eps)) return dcoef = 0.0, a.coef0;
+  if (gt_pos(l, a.eps)) return dcoef = 0.0, a.coef1;
+  dcoef = -a.dt * a.rho_d * dheaviside(l, a.eps, a.oe) / (r * r);
+  return a.dt * (1 / r);
+}
+
+__global__ void k_visc_adj_coef(const double* __restrict__ phi_a, const double* __restrict__ u_a, const double* __restrict__ v_a,
+                                const double* __restrict__ lu_a, const double* __restrict__ lv_a, double* __restrict__ C,
+                                ViscAdjArgs a) {
+  const int ni = a.ni, nj = a.nj;
+  const DField phi = dfield((double*)phi_a, 2, ni, nj);
+  const DField u = dfield((double*)u_a, 2, ni + 1, nj), v = dfield((double*)v_a, 2, ni, nj + 1);
+  const DField lu = dfield((double*)lu_a, 2, ni + 1, nj), lv = dfield((double*)lv_a, 2, ni, nj + 1);
+  const size_t nX = (size_t)(ni + 1) * nj, nY = (size_t)ni * (nj + 1);
+  auto tu = [&](int i, int j) -> double { return (i < 0 || i > ni || j < 0 || j >= nj) ? 0.0 : GB_AT(u, i, j); };
+  auto tv = [&](int i, int j) -> double { return (i < 0 || i >= ni || j < 0 || j > nj) ? 0.0 : GB_AT(v, i, j); };
+  auto P = [&](int i, int j) -> double { return GB_AT(phi, i, j); };
+  auto dmu = [&](double l) -> double { return a.mu_d * dheaviside(l, a.eps, a.oe); };
+  const double ox2 = a.odx * a.odx, oy2 = a.ody * a.ody, oxy = a.odx * a.ody;
+  GB_FOR_IJ(i, j, ni + 1, nj + 1) {
+    if (j < nj) {  // x-face (i, j): nodes (i-1, j) and (i, j)
+      double* o = C + (size_t)j * (ni + 1) + i;
+      const double lam = GB_AT(lu, i, j);
+      const double pl = P(i - 1, j), pc = P(i, j);
+      const double cu = 0.25 * (pl + pc + P(i - 1, j + 1) + P(i, j + 1));
+      const double cd = 0.25 * (P(i - 1, j - 1) + P(i, j - 1) + pl + pc);
+      double dcoef, dw, da;
+      const double coef = visc_coef(0.5 * (pl + pc), a, dcoef, dw, da);
+      const double m_cu = visc_mu(cu, a), m_cd = visc_mu(cd, a), m_r = visc_mu(pc, a), m_c = visc_mu(pl, a);
+      const double t0 = tu(i, j);
+      const double dxp = tu(i + 1, j) - t0, dxm = t0 - tu(i - 1, j);
+      const double gup = a.ody * (tu(i, j + 1) - t0) + a.odx * (tv(i, j + 1) - tv(i - 1, j + 1));
+      const double gdn = a.ody * (t0 - tu(i, j - 1)) + a.odx * (tv(i, j) - tv(i - 1, j));
+      const double axp = coef * 2.0 * ox2 * m_r, axm = coef * 2.0 * ox2 * m_c, ayp = coef * oy2 * m_cu, aym = coef * oy2 * m_cd;
+      o[0] = lam * axp;
+      o[nX] = lam * axm;
+      o[2 * nX] = lam * ayp;
+      o[3 * nX] = lam * aym;
+      o[4 * nX] = lam * coef * oxy * m_cu;
+      o[5 * nX] = lam * coef * oxy * m_cd;
+      o[6 * nX] = lam * (1.0 - (axp + axm + ayp + aym));
+      const double F = 2.0 * ox2 * (m_r * dxp - m_c * dxm), G = a.ody * (m_cu * gup - m_cd * gdn);
+      const double wco = lam * (F + G) * dcoef;
+      o[7 * nX] = -lam * coef * 2.0 * ox2 * dxm * dmu(pl) + 0.5 * wco;  // node (i-1, j)
+      o[8 * nX] = lam * coef * 2.0 * ox2 * dxp * dmu(pc) + 0.5 * wco;   // node (i, j)
+      o[9 * nX] = 0.25 * lam * coef * a.ody * gup * dmu(cu);
+      o[10 * nX] = -0.25 * lam * coef * a.ody * gdn * dmu(cd);
+      o[11 * nX] = lam * (F + G) * dw;
+      o[12 * nX] = lam * (F + G) * da;
+    }
+    if (i < ni) {  // y-face (i, j): nodes (i, j-1) and (i, j)
+      double* o = C + 13 * nX + (size_t)j * ni + i;
+      const double lam = GB_AT(lv, i, j);
+      const double pb = P(i, j - 1), pc = P(i, j);
+      const double cu = 0.25 * (pb + P(i + 1, j - 1) + pc + P(i + 1, j));
+      const double cl = 0.25 * (P(i - 1, j - 1) + pb + P(i - 1, j) + pc);
+      double dcoef, dw, da;
+      const double coef = visc_coef(0.5 * (pb + pc), a, dcoef, dw, da);
+      const double m_cu = visc_mu(cu, a), m_cl = visc_mu(cl, a), m_u = visc_mu(pc, a), m_c = visc_mu(pb, a);
+      const double t0 = tv(i, j);
+      const double dyp = tv(i, j + 1) - t0, dym = t0 - tv(i, j - 1);
+      const double grt = a.ody * (tu(i + 1, j) - tu(i + 1, j - 1)) + a.odx * (tv(i + 1, j) - t0);
+      const double glf = a.ody * (tu(i, j) - tu(i, j - 1)) + a.odx * (t0 - tv(i - 1, j));
+      const double ayp = coef * 2.0 * oy2 * m_u, aym = coef * 2.0 * oy2 * m_c, axp = coef * ox2 * m_cu, axm = coef * ox2 * m_cl;
+      o[0] = lam * ayp;
+      o[nY] = lam * aym;
+      o[2 * nY] = lam * axp;
+      o[3 * nY] = lam * axm;
+      o[4 * nY] = lam * coef * oxy * m_cu;
+      o[5 * nY] = lam * coef * oxy * m_cl;
+      o[6 * nY] = lam * (1.0 - (ayp + aym + axp + axm));
+      const double F = 2.0 * oy2 * (m_u * dyp - m_c * dym), G = a.odx * (m_cu * grt - m_cl * glf);
+      const double wco = lam * (F + G) * dcoef;
+      o[7 * nY] = -lam * coef * 2.0 * oy2 * dym * dmu(pb) + 0.5 * wco;  // node (i, j-1)
+      o[8 * nY] = lam * coef * 2.0 * oy2 * dyp * dmu(pc) + 0.5 * wco;   // node (i, j)
+      o[9 * nY] = 0.25 * lam * coef * a.odx * grt * dmu(cu);
+      o[10 * nY] = -0.25 * lam * coef * a.odx * glf * dmu(cl);
+      o[11 * nY] = lam * (F + G) * dw;
+      o[12 * nY] = lam * (F + G) * da;
+    }
+  }
+}
+
+// Over the (ni + 2) x (nj + 2) index space (x, y): the x-face and the y-face (x, y) where they
+// exist, and the node (x - 1, y - 1) of phi's interior and ghost-1 ring.
+__global__ void k_visc_adj_gather(const double* __restrict__ C, double* __restrict__ mu_a, double* __restrict__ mv_a,
+                                  double* __restrict__ mp_a, int ni, int nj) {
+  const size_t nX = (size_t)(ni + 1) * nj, nY = (size_t)ni * (nj + 1);
+  const double* CY = C + 13 * nX;
+  auto X = [&](int k, int I, int J) -> double {
+    return (I < 0 || I > ni || J < 0 || J >= nj) ? 0.0 : C[k * nX + (size_t)J * (ni + 1) + I];
+  };
+  auto Y = [&](int k, int I, int J) -> double {
+    return (I < 0 || I >= ni || J < 0 || J > nj) ? 0.0 : CY[k * nY + (size_t)J * ni + I];
+  };
+  DField mu = dfield(mu_a, 2, ni + 1, nj), mv = dfield(mv_a, 2, ni, nj + 1), mp = dfield(mp_a, 2, ni, nj);
+  GB_FOR_IJ(x, y, ni + 2, nj + 2) {
+    if (x <= ni && y < nj) {
+      const int i = x, j = y;
+      GB_AT(mu, i, j) = X(6, i, j) + X(0, i - 1, j) + X(1, i + 1, j) + X(2, i, j - 1) + X(3, i, j + 1) + Y(4, i - 1, j) -
+                        Y(4, i - 1, j + 1) - Y(5, i, j) + Y(5, i, j + 1);
+    }
+    if (x < ni && y <= nj) {
+      const int i = x, j = y;
+      GB_AT(mv, i, j) = Y(6, i, j) + Y(0, i, j - 1) + Y(1, i, j + 1) + Y(2, i - 1, j) + Y(3, i + 1, j) + X(4, i, j - 1) -
+                        X(4, i + 1, j - 1) - X(5, i, j) + X(5, i + 1, j);
+    }
+    const int i = x - 1, j = y - 1;
+    GB_AT(mp, i, j) = X(8, i, j) + X(7, i + 1, j) + X(9, i, j) + X(9, i + 1, j) + X(9, i, j - 1) + X(9, i + 1, j - 1) +
+                      X(10, i, j) + X(10, i + 1, j) + X(10, i, j + 1) + X(10, i + 1, j + 1) + Y(8, i, j) + Y(7, i, j + 1) +
+                      Y(9, i, j) + Y(9, i - 1, j) + Y(9, i, j + 1) + Y(9, i - 1, j + 1) + Y(10, i, j) + Y(10, i + 1, j) +
+                      Y(10, i, j + 1) + Y(10, i + 1, j + 1);
+  }
+}
+
+
 }  // namespace
 
 int density_gradient(gb2d_ctx* c, double dt, double* d_water, double* d_air) {
@@ -987,5 +1129,50 @@ int reinit_sweep_vjp(gb2d_ctx* c, const double* phi_dev, const double* sign_dev,
   return GB2D_OK;
 }
 
+
+// VJP of the Sourcing viscosity at the context's PHI, U, V: lam_u, lam_v (device, U / V
+// layouts) -> mu_u, mu_v (U / V layouts) and mu_phi (PHI's layout, nonzero on the interior and
+// the ghost-1 ring); d_density (host, may be null) receives dL / d rho_water, dL / d rho_air, the
+// faces' shares added on the host in index order.  The 13 numbers of each face live in adj_eno.
+int viscosity_vjp(gb2d_ctx* c, double dt, const double* lu, const double* lv, double* mu, double* mv, double* mp,
+                  double* d_density) {
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  ViscAdjArgs a;
+  a.ni = ni;
+  a.nj = nj;
+  a.dt = dt;
+  a.odx = c->base.odx;
+  a.ody = c->base.ody;
+  a.eps = 1.5 * c->base.dx;
+  a.oe = 1.0 / a.eps;
+  a.mu_lo = c->flow.air_viscosity;
+  a.mu_d = c->flow.water_viscosity - c->flow.air_viscosity;
+  a.mu_at0 = a.mu_lo + a.mu_d * 0.0;
+  a.mu_at1 = a.mu_lo + a.mu_d * 1.0;
+  a.rho_lo = c->prm.air_density;
+  a.rho_d = c->prm.water_density - c->prm.air_density;
+  a.coef0 = dt * (1 / (a.rho_lo + a.rho_d * 0.0));
+  a.coef1 = dt * (1 / (a.rho_lo + a.rho_d * 1.0));
+  const size_t nu = (size_t)(ni + 5) * (nj + 4), nv = (size_t)(ni + 4) * (nj + 5), np = (size_t)(ni + 4) * (nj + 4);
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(mu, 0, nu * sizeof(double), c->stream));
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(mv, 0, nv * sizeof(double), c->stream));
+  GB2D_CUDA_TRY(c, cudaMemsetAsync(mp, 0, np * sizeof(double), c->stream));
+  k_visc_adj_coef<<<grid_ij(ni + 1, nj + 1), kThreads, 0, c->stream>>>(c->phi_buf[c->phi_cur], c->u, c->v, lu, lv, c->adj_eno, a);
+  k_visc_adj_gather<<<grid_ij(ni + 2, nj + 2), kThreads, 0, c->stream>>>(c->adj_eno, mu, mv, mp, ni, nj);
+  GB_LAUNCHED(2);
+  if (!d_density) return GB2D_OK;
+  const size_t nX = (size_t)(ni + 1) * nj, nY = (size_t)ni * (nj + 1);
+  std::vector<double> h(2 * (nX + nY));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(h.data(), c->adj_eno + 11 * nX, 2 * nX * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(h.data() + 2 * nX, c->adj_eno + 13 * nX + 11 * nY, 2 * nY * sizeof(double),
+                                   cudaMemcpyDeviceToHost, c->stream));
+  GB2D_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  double w = 0.0, a_ = 0.0;
+  for (size_t k = 0; k < nX; ++k) w += h[k], a_ += h[nX + k];
+  for (size_t k = 0; k < nY; ++k) w += h[2 * nX + k], a_ += h[2 * nX + nY + k];
+  d_density[0] = w;
+  d_density[1] = a_;
+  return GB2D_OK;
+}
 
 }  // namespace gb2d

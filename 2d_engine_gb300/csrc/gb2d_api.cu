@@ -832,6 +832,23 @@ int gb2d_reinit_sweep_adjoint(gb2d_ctx* c, const double* phi_in, const double* s
   return sync_check(c, "reinit_sweep_adjoint");
 }
 
+int gb2d_viscosity_adjoint(gb2d_ctx* c, double dt, const double* lam_u, const double* lam_v, double* mu_u, double* mu_v,
+                           double* mu_phi, double* d_density) {
+  if (!c || !lam_u || !lam_v || !mu_u || !mu_v || !mu_phi || !std::isfinite(dt)) return GB2D_ERR_ARG;
+  int rc = adjoint_buffers(c);
+  if (rc) return rc;
+  const size_t ni = c->grid.ni, nj = c->grid.nj;
+  const size_t nu = (ni + 5) * (nj + 4), nv = (ni + 4) * (nj + 5), nphi = (ni + 4) * (nj + 4);
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_u, lam_u, nu * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->adj_lam_v, lam_v, nv * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if ((rc = viscosity_vjp(c, dt, c->adj_lam_u, c->adj_lam_v, c->adj_mu_u, c->adj_mu_v, c->adj_mu_phi, d_density))) return rc;
+  if ((rc = check_launch(c, "viscosity_adjoint"))) return rc;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_u, c->adj_mu_u, nu * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_v, c->adj_mu_v, nv * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(mu_phi, c->adj_mu_phi, nphi * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return sync_check(c, "viscosity_adjoint");
+}
+
 int gb2d_projection_phi_gradient(gb2d_ctx* c, double dt, double* d_phi) {
   if (!c || !d_phi || !std::isfinite(dt) || dt == 0.0 || !c->adj_coef) return GB2D_ERR_ARG;
   return phi_gradient(c, dt, d_phi);

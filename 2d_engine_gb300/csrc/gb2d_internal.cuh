@@ -229,6 +229,8 @@ int eno3_adjoint(gb2d_ctx* c, double dt);
 // VJP of one reinitialisation sweep (FP64 form) at phi (device, ghost 2) and S (device, ni x nj):
 // lam (device, ghost 2) -> mu (device, ghost 2) and the cotangent of S into gs (device, ni x nj).
 int reinit_sweep_vjp(gb2d_ctx* c, const double* phi, const double* sign, const double* lam, double* mu, double* gs);
+int viscosity_vjp(gb2d_ctx* c, double dt, const double* lu, const double* lv, double* mu, double* mv, double* mp,
+                  double* d_density);
 
 // ---- gb2d_jump.cu (FP64, compiled without FMA contraction) ----
 int jump_buffers(gb2d_ctx* c);

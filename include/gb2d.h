@@ -286,6 +286,14 @@ int gb2d_reinit_sweep_apply(gb2d_ctx* ctx, const double* phi_in, const double* s
  * mu_sign (ni x nj, the cotangent of S). */
 int gb2d_reinit_sweep_adjoint(gb2d_ctx* ctx, const double* phi_in, const double* sign, const double* lam, double* mu_phi,
                               double* mu_sign);
+/* VJP of gb2d_sourcing's explicit viscosity (ApplyViscosity, VISCOSITY_2D.h:460-532; FP64 form)
+ * at the context's PHI, U, V (the stage's inputs): lam_u, lam_v (U / V layouts) -> mu_u, mu_v
+ * (U / V layouts) and mu_phi (PHI's layout: the smeared viscosities and the face densities
+ * depend on the level set, read on the interior and the ghost-1 ring) and, if d_density is not
+ * null, d_density[0..1] = dL/d water_density, dL/d air_density (through dt / rho of each face).
+ * Uses gb2d_flow_params' viscosities. */
+int gb2d_viscosity_adjoint(gb2d_ctx* ctx, double dt, const double* lam_u, const double* lam_v, double* mu_u, double* mu_v,
+                           double* mu_phi, double* d_density);
 
 /* Batches: many independent simulations of uneven grid sizes on one GPU (no counterpart
  * in the reference, which runs one simulation per process).  Each instance is a full

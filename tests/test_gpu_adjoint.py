@@ -522,3 +522,114 @@ def test_levelset_rk3_with_reinitialization_gradient(gb):
             ad = float(np.sum(grad * d))
             assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-3 * np.linalg.norm(grad)), (k, ad, fd)
     c.close()
+
+
+def test_viscosity_adjoint(gb):
+    """The sourcing's explicit viscosity (viscosities 1 : 0.01, densities 3 : 1): its VJP in U,
+    V, the level set (interior and ghost-1 ring) and the two densities against central
+    differences of the GPU forward."""
+    n = 30
+    case = rising_bubble_case(n, n, seed=24)
+    rng = np.random.default_rng(25)
+    dt = 0.2 / (n - 1)
+    u0 = case["u"] + 0.3 * rng.standard_normal(case["u"].shape)
+    v0 = case["v"] + 0.3 * rng.standard_normal(case["v"].shape)
+
+    def fwd(phi, u, v, w=3.0, a=1.0):
+        c = gb.Context(n, n, water_density=w, air_density=a)
+        c.set_flow_params(water_viscosity=1.0, air_viscosity=0.01, viscosity=True)
+        for f, x in ((gb.FIELD_PHI, phi), (gb.FIELD_U, u), (gb.FIELD_V, v)):
+            c.set(f, x)
+        c.sourcing(dt)
+        out = c.get(gb.FIELD_U), c.get(gb.FIELD_V)
+        c.close()
+        return out
+
+    lu, lv = rng.standard_normal(u0.shape), rng.standard_normal(v0.shape)
+    L = lambda out: float(np.sum(lu * out[0]) + np.sum(lv * out[1]))
+    c = gb.Context(n, n, water_density=3.0, air_density=1.0)
+    c.set_flow_params(water_viscosity=1.0, air_viscosity=0.01, viscosity=True)
+    for f, x in ((gb.FIELD_PHI, case["phi"]), (gb.FIELD_U, u0), (gb.FIELD_V, v0)):
+        c.set(f, x)
+    mu, mv, mp, (dw, da) = c.viscosity_adjoint(dt, lu, lv)
+    c.close()
+    phi = case["phi"]
+    for k in range(3):
+        du, dv = rng.standard_normal(u0.shape), rng.standard_normal(v0.shape)
+        fd = central(lambda t: L(fwd(phi, u0 + t * du, v0 + t * dv)), 0.0, 1.0, eps=1e-3)  # affine in U, V
+        ad = float(np.sum(mu * du) + np.sum(mv * dv))
+        assert abs(ad - fd) <= 1e-9 * max(abs(fd), 1.0), ("uv", k, ad, fd)
+        dp = rng.standard_normal(phi.shape)
+        fd = central(lambda t: L(fwd(phi + t * dp, u0, v0)), 0.0, 1.0, eps=1e-5)
+        ad = float(np.sum(mp * dp))
+        assert abs(ad - fd) <= GRAD_TOL * max(abs(fd), 1e-3 * np.linalg.norm(mp)), ("phi", k, ad, fd)
+    fd = central(lambda t: L(fwd(phi, u0, v0, w=3.0 + t)), 0.0, 1.0, eps=1e-4)
+    assert abs(dw - fd) <= GRAD_TOL * abs(fd), ("water", dw, fd)
+    fd = central(lambda t: L(fwd(phi, u0, v0, a=1.0 + t)), 0.0, 1.0, eps=1e-4)
+    assert abs(da - fd) <= GRAD_TOL * abs(fd), ("air", da, fd)
+
+
+def test_time_step_with_reinitialization_and_viscosity(gb):
+    """One whole order-3 time step with the reinitialisation (2 sweeps per Reinitialization) and
+    the explicit viscosity on, as autograd operations: the forward equals gb2d_advance_time_step,
+    and the centroid height's gradients in the initial level set, the initial x-velocity and the
+    water density match central differences of the step."""
+    ag = importlib.import_module("2d_engine_gb300.autograd")
+    n = 25
+    case = rising_bubble_case(n, n, seed=26)
+    rng = np.random.default_rng(27)
+    dt = 0.2 / (n - 1)
+    u0 = case["u"] * 5.0 + 0.1 * rng.standard_normal(case["u"].shape)
+    v0 = case["v"] * 5.0 + 0.1 * rng.standard_normal(case["v"].shape)
+    ua0, va0 = ag.advecting_copy(torch.from_numpy(u0)).numpy(), ag.advecting_copy(torch.from_numpy(v0)).numpy()
+    opts = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=1e-13, max_iterations=20000)
+    kw = dict(surface_tension=1.0, advection_precision=gb.PRECISION_FP64, reinit_iterations=2)
+    flow = dict(water_viscosity=0.5, air_viscosity=0.05)
+
+    def make(w, a):
+        return gb.Context(n, n, water_density=w, air_density=a, **kw)
+
+    def step(phi, u, v, w=3.0, grad=False):
+        P, U = (torch.from_numpy(x.copy()).requires_grad_(grad) for x in (phi, u))
+        W, A = torch.tensor(w, dtype=torch.float64, requires_grad=grad), torch.tensor(1.0, dtype=torch.float64)
+        ls = gb.Context(n, n, **kw)
+        state = {"p": case["p"].copy()}
+        p, uu, vv, _, _ = ag.time_step(ls, P, U, torch.from_numpy(v), torch.from_numpy(ua0), torch.from_numpy(va0), W, A, dt, make,
+                                       state, opts, reinit=True, viscosity=flow)
+        L = ag.centroid_height(p, n, n) + 0.01 * (uu[2:2 + n, 2:3 + n] ** 2).sum()
+        out = (float(L), p.detach().numpy().copy(), uu.detach().numpy().copy())
+        if grad:
+            L.backward()
+            out = out + (P.grad.numpy().copy(), U.grad.numpy().copy(), float(W.grad))
+        ls.close()
+        return out
+
+    c = make(3.0, 1.0)
+    c.set_flow_params(viscosity=True, **flow)
+    for f, x in ((gb.FIELD_PHI, case["phi"]), (gb.FIELD_U, u0), (gb.FIELD_V, v0), (gb.FIELD_P, case["p"]), (gb.FIELD_UA, ua0),
+                 (gb.FIELD_VA, va0)):
+        c.set(f, x)
+    c.advance_time_step(dt, opts)
+    _, phi_t, u_t, g_phi, g_u, g_w = step(case["phi"], u0, v0, grad=True)
+    it = (slice(2, 2 + n), slice(2, 2 + n))
+    assert np.abs(phi_t[it] - c.get(gb.FIELD_PHI)[it]).max() <= 1e-11
+    assert np.abs(u_t[2:2 + n, 2:3 + n] - c.get(gb.FIELD_U)[2:2 + n, 2:3 + n]).max() <= 1e-9
+    c.close()
+
+    phi0 = case["phi"]
+    y, x = np.mgrid[0:n, 0:n]
+    d = np.zeros_like(phi0)
+    d[it] = np.sin(2.3 * np.pi * x / n + 0.4) * np.cos(1.7 * np.pi * y / n)
+    h = 2e-2 * float(np.abs(phi0[it]).min())
+    q = lambda s: (step(phi0 + s * d, u0, v0)[0] - step(phi0 - s * d, u0, v0)[0]) / (2 * s)
+    fd = (4 * q(h / 2) - q(h)) / 3
+    got = float(np.sum(g_phi * d))
+    assert abs(got - fd) <= 1e-4 * max(abs(fd), 1e-9), ("phi", got, fd)
+    du = rng.standard_normal(u0.shape)
+    q = lambda s: (step(phi0, u0 + s * du, v0)[0] - step(phi0, u0 - s * du, v0)[0]) / (2 * s)
+    fd = (4 * q(5e-7) - q(1e-6)) / 3
+    got = float(np.sum(g_u * du))
+    assert abs(got - fd) <= 1e-4 * max(abs(fd), 1e-9), ("u", got, fd)
+    q = lambda s: (step(phi0, u0, v0, w=3.0 + s)[0] - step(phi0, u0, v0, w=3.0 - s)[0]) / (2 * s)
+    fd = (4 * q(5e-4) - q(1e-3)) / 3
+    assert abs(g_w - fd) <= 1e-4 * max(abs(fd), 1e-9), ("water", g_w, fd)
