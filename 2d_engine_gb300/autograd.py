@@ -461,3 +461,40 @@ def time_step(gb_ls, phi, u, v, ua, va, water, air, dt, make_context, state, opt
         elif stage == 2:
             u, v = (1 / 3.0) * uk + (2 / 3.0) * u, (1 / 3.0) * vk + (2 / 3.0) * v
     return phi, u, v, ua, va
+
+
+def time_step_window_loss(gb, ni, nj, phi0, u0, v0, water, air, dt, steps, checkpoint_every=10, opts=None, surface_tension=0.0728,
+                          viscosity=None, gravity=(0.0, -9.8), p0=None, x_max=1.0, y_max=1.0):
+    """The bubble's centroid height after `steps` whole order-3 time steps (time_step, the
+    reinitialisation off inside the window) from (phi0, u0, v0) at rest-frame advecting copies of
+    u0, v0, with torch.utils.checkpoint segments of `checkpoint_every` steps, so that only every
+    segment's starting state is kept for the backward pass.  Differentiable in phi0, u0, v0 and
+    the densities water, air (0-d tensors).  viscosity: set_flow_params' viscosities, or None."""
+    opts = solve_opts(precision=0, tolerance=1e-10, max_iterations=20000) if opts is None else opts
+    kw = dict(x_max=x_max, y_max=y_max, surface_tension=surface_tension, reinit_iterations=0, advection_precision=0)
+
+    def make(w, a):
+        return gb.Context(ni, nj, 0.0, 0.0, water_density=w, air_density=a, **kw)
+
+    ls = gb.Context(ni, nj, 0.0, 0.0, **kw)
+    state = {"p": np.zeros(ls.shape(FIELD_P)) if p0 is None else p0.copy()}
+    phi, u, v = phi0, u0, v0
+    ua, va = advecting_copy(u0), advecting_copy(v0)
+    k = 0
+    while k < steps:
+        n = min(checkpoint_every, steps - k)
+
+        def segment(p, uu, vv, aa, bb, w, a, n=n):
+            for _ in range(n):
+                p, uu, vv, aa, bb = time_step(ls, p, uu, vv, aa, bb, w, a, dt, make, state, opts, gravity, viscosity=viscosity)
+            return p, uu, vv, aa, bb
+
+        args = (phi, u, v, ua, va, water, air)
+        if any(isinstance(x, torch.Tensor) and x.requires_grad for x in args):
+            phi, u, v, ua, va = torch.utils.checkpoint.checkpoint(segment, *args, use_reentrant=False)
+        else:
+            phi, u, v, ua, va = segment(*args)
+        k += n
+    # ls stays open: the checkpointed segments run again through it in the backward pass
+    # (Context frees its device state when it is collected).
+    return centroid_height(phi, ni, nj, x_max, y_max)
