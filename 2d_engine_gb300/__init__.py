@@ -46,7 +46,7 @@ class FlowParamsT(ctypes.Structure):
 
 class SolveOptsT(ctypes.Structure):
     _fields_ = [("solver", ctypes.c_int), ("precision", ctypes.c_int), ("tolerance", ctypes.c_double),
-                ("max_iterations", ctypes.c_int), ("mg_smooth", ctypes.c_int), ("inner_tolerance", ctypes.c_double)]
+                ("max_iterations", ctypes.c_int), ("mg_smooth", ctypes.c_int)]
 
 
 class SolveStatsT(ctypes.Structure):
@@ -126,6 +126,7 @@ def library():
         "gb2d_kernel_launches": [ctypes.POINTER(ctypes.c_ulonglong)],
         "gb2d_alu_peaks": [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)],
         "gb2d_solver_layout": [vp, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)],
+        "gb2d_preconditioner_apply": [vp, i, i, vp, vp],
         "gb2d_check_exact_division": [ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)],
         "gb2d_checkpoint_save": [vp],
         "gb2d_checkpoint_restore": [vp],
@@ -174,9 +175,8 @@ def _ptr(a):
     return a.ctypes.data
 
 
-def solve_opts(solver=SOLVER_MGPCG, precision=PRECISION_FP64, tolerance=1e-8, max_iterations=10000, mg_smooth=2,
-               inner_tolerance=1e-4):
-    return SolveOptsT(solver, precision, tolerance, max_iterations, mg_smooth, inner_tolerance)
+def solve_opts(solver=SOLVER_MGPCG, precision=PRECISION_FP64, tolerance=1e-8, max_iterations=10000, mg_smooth=2):
+    return SolveOptsT(solver, precision, tolerance, max_iterations, mg_smooth)
 
 
 class Context:
@@ -254,6 +254,15 @@ class Context:
         lv, top, ctas = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         self._check(self.L.gb2d_solver_layout(self.h, precision, ctypes.byref(lv), ctypes.byref(top), ctypes.byref(ctas)))
         return lv.value, top.value, ctas.value
+
+    def preconditioner_apply(self, r, precision=PRECISION_MIXED, mg_smooth=2):
+        """One V-cycle z = M r of the preconditioner of the last assembled system (r, z: (nj, ni))."""
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        if r.shape != (self.nj, self.ni):
+            raise ValueError(f"r: expected shape {(self.nj, self.ni)}, got {r.shape}")
+        z = np.empty_like(r)
+        self._check(self.L.gb2d_preconditioner_apply(self.h, precision, mg_smooth, _ptr(r), _ptr(z)))
+        return z
 
     def probe_read(self):
         n, ms, by = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()

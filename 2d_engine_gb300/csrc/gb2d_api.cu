@@ -358,6 +358,21 @@ int gb2d_solver_layout(gb2d_ctx* c, int precision, int* levels, int* cluster_top
   return GB2D_OK;
 }
 
+int gb2d_preconditioner_apply(gb2d_ctx* c, int precision, int mg_smooth, const double* r, double* z) {
+  if (!c || !r || !z) return GB2D_ERR_ARG;
+  if (precision != GB2D_PRECISION_FP64 && precision != GB2D_PRECISION_MIXED) return GB2D_ERR_ARG;
+  const size_t n = (size_t)c->grid.ni * c->grid.nj;
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->tmp_a, r, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  // z lands in xw (tmp_b may hold a jump system's diagonal shift)
+  int rc = gb2d::solver_precondition(c, precision == GB2D_PRECISION_MIXED, mg_smooth, c->tmp_a, c->xw);
+  if (rc) {
+    snprintf(c->err, sizeof(c->err), "preconditioner_apply: %s", cudaGetErrorString(cudaGetLastError()));
+    return rc;
+  }
+  GB2D_CUDA_TRY(c, cudaMemcpyAsync(z, c->xw, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  return sync_check(c, "preconditioner_apply");
+}
+
 int gb2d_check_exact_division(unsigned long long n, unsigned long long seed, unsigned long long* mismatches) {
   if (!mismatches) return GB2D_ERR_ARG;
   int err = 0;

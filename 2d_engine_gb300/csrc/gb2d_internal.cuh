@@ -254,6 +254,9 @@ void solver_drop_prebuild(gb2d_ctx* c);
 // ctx->bx/by/diag) and refreshes only the right-hand side.
 void solver_keep_levels(gb2d_ctx* c);
 void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, int* cluster_ctas);
+// One multigrid V-cycle (nu sweeps per side, FP32 levels when prec) of the assembled
+// system in ctx->bx/by/diag applied to r: z = M r (device, compact ni x nj FP64).
+int solver_precondition(gb2d_ctx* c, int prec, int nu, const double* r_dev, double* z_dev);
 
 }  // namespace gb2d
 

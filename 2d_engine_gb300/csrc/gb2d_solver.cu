@@ -1,6 +1,8 @@
 // Pressure solver: multigrid-preconditioned CG on the matrix-free 5-point
-// ghost-fluid operator, in FP64 or as FP64 iterative refinement around an FP32
-// CG + FP32 V-cycle inner solve.
+// ghost-fluid operator.  The CG (x, r, p, A p, every dot product) is FP64 with
+// the reference's own matrix entries; the preconditioner (a symmetric V-cycle,
+// or Jacobi) runs in FP64, or in FP32 on an FP32 copy of r for
+// GB2D_PRECISION_MIXED.
 //
 // Replaces PCG_METHOD::PCGMethod with IC(0) (PCG_METHOD.cpp:176-264) and the
 // reference's constant-coefficient MULTIGRID_METHOD (MULTIGRID_METHOD.cpp:107-332)
@@ -11,21 +13,18 @@
 // preconditioner), piecewise-constant prolongation with averaging restriction,
 // and a dense inverse on the coarsest level (<= 64 cells).
 //
-// Kernel structure of one V-cycle: on every level with more than 64^2 cells a
-// smoothing sweep is ONE launch over 32x16 tiles (the tile plus a halo is staged
-// in shared memory, red and black half sweeps run back to back, halo cells are
-// recomputed redundantly); the last pre-sweep also forms the residual and
-// restricts it, the first post-sweep also prolongs the coarse correction.  All
-// levels from 64^2 down run inside one single-CTA kernel with x and b in shared
-// memory.  One CG iteration is two more kernels, and each iteration is replayed
-// from a CUDA graph.
-//
-// The FP32 inner CG applies the operator in flux form,
-//   (A p)_i = sh_i p_i + sum_faces c_f (p_i - p_nb),
-// whose differences of neighbouring values are exact, so FP32 rounding is
-// relative to the flux rather than to the diagonal; the solution accumulates in
-// FP64 and every dot product accumulates in FP64.  Each FP64 refinement step
-// recomputes r = b - A x with the reference's own matrix entries.
+// Kernel structure of one V-cycle: every level above the cluster tail does each
+// side of its smoothing in ONE tiled launch (the tile plus a halo is staged in
+// shared memory, the red and black half sweeps run back to back, halo cells are
+// recomputed redundantly); the pre-smoothing launch also forms the residual and
+// restricts it, the post-smoothing launch also prolongs the coarse correction.
+// The levels from 128^2 down run in one launch of a 16-CTA thread-block cluster
+// (gb2d_ctail.cuh), neighbour rows read from the other CTAs' shared memory; a
+// single-CTA kernel over the levels from 64^2 down is the fallback.  One CG
+// iteration adds three FP64 kernels (direction, operator product with p.Ap,
+// update with r.r), and each iteration is replayed from a CUDA graph whose
+// kernels use programmatic dependent launch.  The loop around the CG recomputes
+// the true FP64 residual and restarts only if the recursive residual drifted.
 //
 // All reductions are two-stage and deterministic: blocks write partial sums,
 // consumers re-reduce the partials in a fixed order.
@@ -323,6 +322,26 @@ __device__ __forceinline__ void stage_window(const Level<T>& L, const Level<T>& 
   }
 }
 
+// The smoothers' arithmetic, with every rounding stated: one Gauss-Seidel update
+//   x = (b + cxl xl + cxr xr + cyb xb + cyt xt) / dg   (1/dg stored),
+// fused multiply-adds in that order, and the residual
+//   b - (dg x - cxl xl - cxr xr - cyb xb - cyt xt).
+// Written with the rounding intrinsics so that every kernel that smooths a level
+// (tiled or streaming) computes each value with the same operations, whatever
+// the compiler would contract.
+__device__ __forceinline__ float fmad(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fmad(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mulr(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mulr(double a, double b) { return __dmul_rn(a, b); }
+template <typename T>
+__device__ __forceinline__ T gs_update(T b, T cxl, T xl, T cxr, T xr, T cyb, T xb, T cyt, T xt, T idg) {
+  return mulr(fmad(cyt, xt, fmad(cyb, xb, fmad(cxr, xr, fmad(cxl, xl, b)))), idg);
+}
+template <typename T>
+__device__ __forceinline__ T gs_residual(T b, T dg, T x, T cxl, T xl, T cxr, T xr, T cyb, T xb, T cyt, T xt) {
+  return b - fmad(-cyt, xt, fmad(-cyb, xb, fmad(-cxr, xr, fmad(-cxl, xl, mulr(dg, x)))));
+}
+
 // Half sweep of one colour over the window shrunk by R cells per side: the
 // colour's RH x RW/2 cells are enumerated flat over the block's threads.
 template <typename T, int H, int R, int SH>
@@ -348,7 +367,7 @@ __device__ __forceinline__ void window_half(T* sm, int i0, int j0, int nI, int n
       if (gi < 0 || gi >= nI || gj < 0 || gj >= nJ) continue;
     }
     const int s = c + r * W;
-    xs[s] = (bs[s] + cxs[s] * xs[s - 1] + cxs[s + 1] * xs[s + 1] + cys[s] * xs[s - W] + cys[s + W] * xs[s + W]) * is[s];
+    xs[s] = gs_update(bs[s], cxs[s], xs[s - 1], cxs[s + 1], xs[s + 1], cys[s], xs[s - W], cys[s + W], xs[s + W], is[s]);
   }
 }
 
@@ -464,8 +483,8 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C,
         const int s = (ti + H) + (tj + H) * W;
         xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
         if (!((gi + gj) & 1)) {  // red cells: black residuals are zero after the black half sweep
-          T ax = diag_of(is[s]) * xs[s] - cxs[s] * xs[s - 1] - cxs[s + 1] * xs[s + 1] - cys[s] * xs[s - W] - cys[s + W] * xs[s + W];
-          acc += bs[s] - ax;
+          acc += gs_residual(bs[s], diag_of(is[s]), xs[s], cxs[s], xs[s - 1], cxs[s + 1], xs[s + 1], cys[s], xs[s - W], cys[s + W],
+                             xs[s + W]);
         }
       }
     const int I = i0 / 2 + qx, J = j0 / 2 + qy;
@@ -516,6 +535,8 @@ __global__ void __launch_bounds__(BXT* BYT) k_post_smooth(Level<T> L, Level<T> C
     if (last_block_sum(acc.value(), part_rz, gridDim.x * gridDim.y, counter, &rz)) publish_rz(sc, rz);
   }
 }
+
+#include "gb2d_stream.cuh"
 
 // ---- single-CTA tail: the coarse levels, coefficients resident in shared memory ---
 
@@ -1230,6 +1251,88 @@ void launch_post(cudaStream_t s, int sh, const Level<T>& L, const Level<T>& C, T
     launch_post_sh<T, NS, 3>(s, L, C, xo, prz, S);
 }
 
+// ---- streaming smoother launches (gb2d_stream.cuh) ----
+
+// Whether the levels above the tail use the streaming smoother (GB2D_SMOOTHER=stream)
+// or the tiled one (the default; GB2D_SMOOTHER=tiled).  The test that the two give
+// bit-identical V-cycles runs both.
+inline bool stream_smoother() {
+  static const bool on = [] {
+    const char* e = getenv("GB2D_SMOOTHER");
+    return e && strcmp(e, "stream") == 0;
+  }();
+  return on;
+}
+
+// Rows per segment: S = 32 m - 2 EXTRA (so that the S + 2 EXTRA steps of a block fill
+// whole unrolled passes over the coefficient ring), the largest that still gives the
+// launch `target` blocks (one per strip and segment), at least 16 rows (below that the
+// vertical halo would exceed the work).
+struct StreamPlan {
+  int S, nsteps, blocks;
+};
+inline StreamPlan stream_plan(int nI, int nJ, int ns, bool post) {
+  static const int target = [] {
+    const char* e = getenv("GB2D_STREAM_TARGET_BLOCKS");
+    return e && atoi(e) > 0 ? atoi(e) : 3 * 152;
+  }();
+  const int out = post ? st::W - 4 * ns : st::W - 2 - 4 * ns;
+  const int extra = post ? 4 * ns : 4 * ns + 2;
+  const int nstrips = post ? (nI + 1 + out - 1) / out : (nI + out - 1) / out;
+  int best = -1;
+  for (int m = 1; m <= 64; ++m) {
+    const int S = st::CRING * m - 2 * extra;
+    if (S < 16) continue;
+    if (best < 0) best = S;  // the smallest admissible S
+    if ((long long)nstrips * ((nJ + S - 1) / S) >= target) best = S;
+    if (S >= nJ) break;
+  }
+  StreamPlan p;
+  p.S = best;
+  p.nsteps = best + 2 * extra;
+  p.blocks = nstrips * ((nJ + best - 1) / best);
+  return p;
+}
+
+template <typename T, int NS, bool POST>
+void launch_stream_ns(cudaStream_t s, const Level<T>& L, const Level<T>& C, T* xo, double* prz, Solver* S) {
+  const StreamPlan p = stream_plan(L.nI, L.nJ, NS, POST);
+  const dim3 grid(p.blocks), block(32 * st::Geo<NS, POST>::WARPS);
+  const size_t smem = st::smem_bytes<T, NS, POST>();
+  if (L.ld % 2 == 0)
+    pdl_launch(s, grid, block, smem, k_stream<T, NS, POST, true>, L, C, xo, p.S, p.nsteps, prz, S->counter + 3, S->sc,
+               (const int*)S->done);
+  else
+    pdl_launch(s, grid, block, smem, k_stream<T, NS, POST, false>, L, C, xo, p.S, p.nsteps, prz, S->counter + 3, S->sc,
+               (const int*)S->done);
+}
+template <typename T, bool POST>
+void launch_stream(cudaStream_t s, int nu, const Level<T>& L, const Level<T>& C, T* xo, double* prz, Solver* S) {
+  if (nu == 1)
+    launch_stream_ns<T, 1, POST>(s, L, C, xo, prz, S);
+  else if (nu == 2)
+    launch_stream_ns<T, 2, POST>(s, L, C, xo, prz, S);
+  else
+    launch_stream_ns<T, 3, POST>(s, L, C, xo, prz, S);
+}
+
+template <typename T, int NS>
+cudaError_t set_stream_smem_ns() {
+  const auto a = cudaFuncAttributeMaxDynamicSharedMemorySize;
+  cudaError_t e = cudaFuncSetAttribute(k_stream<T, NS, false, true>, a, (int)st::smem_bytes<T, NS, false>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_stream<T, NS, false, false>, a, (int)st::smem_bytes<T, NS, false>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_stream<T, NS, true, true>, a, (int)st::smem_bytes<T, NS, true>());
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_stream<T, NS, true, false>, a, (int)st::smem_bytes<T, NS, true>());
+  return e;
+}
+template <typename T>
+cudaError_t set_stream_smem() {
+  cudaError_t e = set_stream_smem_ns<T, 1>();
+  if (e == cudaSuccess) e = set_stream_smem_ns<T, 2>();
+  if (e == cudaSuccess) e = set_stream_smem_ns<T, 3>();
+  return e;
+}
+
 inline bool probe_begin(Probe* pr, cudaStream_t s) {
   bool on = pr && pr->on && pr->n < pr->cap;
   if (on) cudaEventRecord(pr->ev[2 * pr->n], s);
@@ -1256,7 +1359,9 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
     Level<T>& L = H.L[l];
     const int sh = H.shape[l];
     bool on = l == 0 && probe_begin(pr, s);
-    if (nu == 1)
+    if (stream_smoother())
+      launch_stream<T, false>(s, nu, L, H.L[l + 1], L.xa, nullptr, S);
+    else if (nu == 1)
       launch_pre<T, 1>(s, sh, L, H.L[l + 1], L.xa, done);
     else if (nu == 2)
       launch_pre<T, 2>(s, sh, L, H.L[l + 1], L.xa, done);
@@ -1288,7 +1393,9 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
     Lin.x = L.xa;
     double* prz = l == 0 ? P_rz : nullptr;
     bool on = l == 0 && probe_begin(pr, s);
-    if (nu == 1)
+    if (stream_smoother())
+      launch_stream<T, true>(s, nu, Lin, H.L[l + 1], L.x, prz, S);
+    else if (nu == 1)
       launch_post<T, 1>(s, sh, Lin, H.L[l + 1], L.x, prz, S);
     else if (nu == 2)
       launch_post<T, 2>(s, sh, Lin, H.L[l + 1], L.x, prz, S);
@@ -1605,6 +1712,8 @@ Solver* solver_create(int ni, int nj, char* err, size_t errlen) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&S->ev[1], cudaEventDisableTiming);
   if (e == cudaSuccess) e = set_smooth_smem<float>();
   if (e == cudaSuccess) e = set_smooth_smem<double>();
+  if (e == cudaSuccess) e = set_stream_smem<float>();
+  if (e == cudaSuccess) e = set_stream_smem<double>();
   // The attribute is per kernel for the whole process: only ever raise it.
   static size_t tail_smem_set[2] = {0, 0};
   if (e == cudaSuccess && S->h64.tail_smem > tail_smem_set[0]) {
@@ -1658,6 +1767,43 @@ void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, in
     *cluster_top = S->h64.ctail;
     *cluster_ctas = S->h64.ctail >= 0 ? S->h64.ct_P : 0;
   }
+}
+
+namespace {
+// Padded level layout <- compact FP64 host-order array (the preconditioner's input r,
+// narrowed as the solver narrows its FP32 copy of r).
+template <typename T>
+__global__ void k_load_padded(const double* __restrict__ src, T* __restrict__ dst, int ni, int nj, int ld) {
+  GB_FOR_IJ(i, j, ni, nj) dst[(size_t)(i + 1) + (size_t)(j + 1) * ld] = in_prec(src[(size_t)j * ni + i], T());
+}
+template <typename T>
+__global__ void k_store_compact(const T* __restrict__ src, double* __restrict__ dst, int ni, int nj, int ld) {
+  GB_FOR_IJ(i, j, ni, nj) dst[(size_t)j * ni + i] = widen(src[(size_t)(i + 1) + (size_t)(j + 1) * ld]);
+}
+
+template <typename T>
+int precondition_once(gb2d_ctx* c, Hierarchy<T>& H, double* ainv, int nu, const double* r_dev, double* z_dev) {
+  Solver* S = c->solver;
+  cudaStream_t s = c->stream;
+  const int ni = c->grid.ni, nj = c->grid.nj;
+  build_hierarchy<T>(s, H, c, sizeof(T) == 8 ? S->b64 : nullptr, ainv);
+  k_load_padded<T><<<grid_ij(ni, nj), kThreads, 0, s>>>(r_dev, H.r, ni, nj, H.L[0].ld);
+  GB_LAUNCHED(1);
+  if (cudaMemsetAsync(S->done, 0, sizeof(int), s) != cudaSuccess) return GB2D_ERR_CUDA;
+  vcycle<T>(s, S, H, ainv, nu, nullptr);
+  k_store_compact<T><<<grid_ij(ni, nj), kThreads, 0, s>>>(H.L[0].x, z_dev, ni, nj, H.L[0].ld);
+  GB_LAUNCHED(1);
+  S->keep = false;  // the next solve rebuilds its levels from the system it is given
+  return cudaGetLastError() == cudaSuccess ? GB2D_OK : GB2D_ERR_CUDA;
+}
+}  // namespace
+
+int solver_precondition(gb2d_ctx* c, int prec, int nu, const double* r_dev, double* z_dev) {
+  Solver* S = c->solver;
+  if (!S) return GB2D_ERR_ARG;
+  nu = nu > 0 ? (nu > 3 ? 3 : nu) : 2;
+  return prec ? precondition_once<float>(c, S->h32, S->ainv32, nu, r_dev, z_dev)
+              : precondition_once<double>(c, S->h64, S->ainv64, nu, r_dev, z_dev);
 }
 
 void solver_prebuild(gb2d_ctx* c, const gb2d_solve_opts* o) {

@@ -106,7 +106,6 @@ typedef struct {
   double tolerance;     /* stop at ||b - A p||_2 / ||b||_2 <= tolerance */
   int max_iterations;   /* cap on Krylov iterations (all restarts together) */
   int mg_smooth;        /* red-black Gauss-Seidel sweeps before and after each coarse correction (0 = 2) */
-  double inner_tolerance; /* reserved (no inner solve in the current scheme); ignored */
 } gb2d_solve_opts;
 
 typedef struct {
@@ -164,6 +163,14 @@ int gb2d_check_exact_division(unsigned long long n, unsigned long long seed, uns
  * single-CTA tail is used instead) and that cluster's CTA count.  No counterpart
  * in the reference (diagnostics). */
 int gb2d_solver_layout(gb2d_ctx* ctx, int precision, int* levels, int* cluster_top, int* cluster_ctas);
+
+/* One multigrid V-cycle of the pressure solver's preconditioner, z = M r, for the
+ * system last assembled on this context (gb2d_poisson_assemble or a projection):
+ * precision GB2D_PRECISION_FP64 or GB2D_PRECISION_MIXED (FP32 levels, r narrowed
+ * to FP32 as the solver does), mg_smooth red-black sweeps per side (0 = 2).  r, z:
+ * host ni x nj, row-major, no ghosts.  No counterpart in the reference
+ * (diagnostics: the smoothing kernels are compared through it). */
+int gb2d_preconditioner_apply(gb2d_ctx* ctx, int precision, int mg_smooth, const double* r, double* z);
 
 /* Device-resident checkpoint of the step state (PHI with its ghosts, U, V, UA,
  * VA, P): save copies it to a second set of device buffers (allocated on the
@@ -365,8 +372,11 @@ int gb2d_poisson_solve(gb2d_ctx* ctx, const double* rhs, double* x, const gb2d_s
  * about 2.1 MB that every GPU loading the library keeps until exit; at most
  * GB2D_NOALLOC_MAX_CELLS unknowns, larger sizes return GB2D_ERR_TOO_LARGE.  The
  * first call on a device looks up the array's address with that device current
- * (make it before any stream capture).  All calls share the array and keep the
- * last call's contents, so calls that overlap on the GPU race. */
+ * (make it before any stream capture) and keeps it for the process: after a
+ * cudaDeviceReset, or from another context on that device, do not call it again.
+ * A warm start that already meets the tolerance returns GB2D_OK after zero
+ * iterations with x unchanged.  All calls share the array and keep the last
+ * call's contents, so calls that overlap on the GPU race. */
 #define GB2D_NOALLOC_MAX_CELLS 65536
 int gb2d_poisson_solve_noalloc(int ni, int nj, double dx, double dy, const double* bx, const double* by, const double* diag,
                                const double* rhs, double* x, double tolerance, int max_iterations, void* stream, int* iterations,
