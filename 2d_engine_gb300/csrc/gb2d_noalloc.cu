@@ -15,8 +15,12 @@
 //   * the array (about 2.1 MB) stays resident on every GPU that loads this library
 //     until the process exits;
 //   * the first call on a device looks up the array's device address with that
-//     device current (cudaGetSymbolAddress) and caches it; make that first call
-//     before any stream capture;
+//     device current (cudaGetSymbolAddress) and caches it per device ordinal for
+//     the life of the process; make that first call before any stream capture.
+//     The cached address belongs to the context that was current at that first
+//     call (normally the device's primary context): after cudaDeviceReset, or
+//     from a different context on the same device, the array lives elsewhere and
+//     this entry point must not be called again in that process;
 //   * every call shares the one array and keeps the previous call's contents:
 //     calls whose work overlaps on the GPU (other streams or threads) race and
 //     must be serialised by the caller.
@@ -80,11 +84,11 @@ __device__ double sum_parts(const double* part) {
   return block_sum(v);
 }
 
-// r = b - A x, z = r/dg, p = z; partials r.z (slot 0) and b.b (slot 1).
+// r = b - A x, z = r/dg, p = z; partials r.z (slot 0), b.b (slot 1) and r.r (slot 2).
 __global__ void k_init(Sys s, const double* __restrict__ x, double* scr) {
   double *r = scr, *z = scr + kVec, *p = scr + 2 * kVec, *part = scr + kPartOff;
   size_t n = (size_t)s.ni * s.nj;
-  double rz = 0, bb = 0;
+  double rz = 0, bb = 0, rr = 0;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
     int i = (int)(t % s.ni), j = (int)(t / s.ni);
     double rv = s.rhs[t] - apply(s, x, i, j);
@@ -94,24 +98,27 @@ __global__ void k_init(Sys s, const double* __restrict__ x, double* scr) {
     p[t] = zv;
     rz += rv * zv;
     bb += s.rhs[t] * s.rhs[t];
+    rr += rv * rv;
   }
   rz = block_sum(rz);
   bb = block_sum(bb);
+  rr = block_sum(rr);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = rz;
     part[kBlocks + blockIdx.x] = bb;
+    part[2 * kBlocks + blockIdx.x] = rr;
   }
 }
 
-// Scalars: [0] r.z, [1] b.b, [2] r.r of the latest update.
+// Scalars: [0] r.z, [1] b.b, [2] r.r (of the starting guess, then of the latest update).
 __global__ void k_init_scalars(double* scr) {
   double* part = scr + kPartOff;
   double* sc = scr + kScalOff;
-  double rz = sum_parts(part), bb = sum_parts(part + kBlocks);
+  double rz = sum_parts(part), bb = sum_parts(part + kBlocks), rr = sum_parts(part + 2 * kBlocks);
   if (threadIdx.x == 0) {
     sc[0] = rz;
     sc[1] = bb;
-    sc[2] = 0;
+    sc[2] = rr;
   }
 }
 
@@ -134,7 +141,9 @@ __global__ void k_apply(Sys s, double* scr) {
 __global__ void k_update(Sys s, double* __restrict__ x, double* scr) {
   double *r = scr, *z = scr + kVec, *p = scr + 2 * kVec, *ap = scr + 3 * kVec, *part = scr + kPartOff;
   const double* sc = scr + kScalOff;
-  double alpha = sc[0] / sum_parts(part + 2 * kBlocks);
+  // p.ap is zero only when p is: r.z was zero too, and the step is none.
+  const double pap = sum_parts(part + 2 * kBlocks);
+  double alpha = pap != 0.0 ? sc[0] / pap : 0.0;
   size_t n = (size_t)s.ni * s.nj;
   double rz = 0, rr = 0;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
@@ -159,7 +168,7 @@ __global__ void k_direction(Sys s, double* scr) {
   double *z = scr + kVec, *p = scr + 2 * kVec, *part = scr + kPartOff;
   double* sc = scr + kScalOff;
   double rz_new = sum_parts(part), rr = sum_parts(part + kBlocks);
-  double beta = rz_new / sc[0];
+  double beta = sc[0] != 0.0 ? rz_new / sc[0] : 0.0;
   size_t n = (size_t)s.ni * s.nj;
   for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) p[t] = z[t] + beta * p[t];
   // Other blocks may still be reading the old r.z in sc[0]: the new one goes to
@@ -197,19 +206,23 @@ extern "C" int gb2d_poisson_solve_noalloc(int ni, int nj, double dx, double dy, 
   Sys sys{ni, nj, 1.0 / (dx * dx), 1.0 / (dy * dy), bx, by, diag, rhs};
   k_init<<<kBlocks, kThreads, 0, s>>>(sys, x, scr);
   k_init_scalars<<<1, kThreads, 0, s>>>(scr);
+  if (cudaGetLastError() != cudaSuccess) return GB2D_ERR_CUDA;
   double sc[4] = {0, 0, 0, 0};
   if (cudaMemcpyAsync(sc, scr + kScalOff, 3 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return GB2D_ERR_CUDA;
   if (cudaStreamSynchronize(s) != cudaSuccess) return GB2D_ERR_CUDA;
   double bb = sc[1], thr2 = tolerance * tolerance * bb;
   int it = 0;
-  double rr = 0;
-  if (!std::isfinite(bb)) return GB2D_ERR_NONFINITE;
-  if (bb > 0) {
+  double rr = sc[2];
+  if (!std::isfinite(bb) || !std::isfinite(rr)) return GB2D_ERR_NONFINITE;
+  // A starting guess that already meets the tolerance (a warm start from the
+  // solution) is returned unchanged after zero iterations.
+  if (bb > 0 && rr > thr2) {
     for (it = 1; it <= max_iterations; ++it) {
       k_apply<<<kBlocks, kThreads, 0, s>>>(sys, scr);
       k_update<<<kBlocks, kThreads, 0, s>>>(sys, x, scr);
       k_direction<<<kBlocks, kThreads, 0, s>>>(sys, scr);
       k_swap<<<1, 1, 0, s>>>(scr);
+      if (cudaGetLastError() != cudaSuccess) return GB2D_ERR_CUDA;
       if (cudaMemcpyAsync(sc, scr + kScalOff, 4 * sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess) return GB2D_ERR_CUDA;
       if (cudaStreamSynchronize(s) != cudaSuccess) return GB2D_ERR_CUDA;
       rr = sc[2];

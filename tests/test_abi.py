@@ -79,3 +79,15 @@ def test_field_density_extent(gb):
     a, b = ctypes.c_int(), ctypes.c_int()
     assert gb.library().gb2d_field_extent(ctypes.byref(g), gb.FIELD_DENSITY, ctypes.byref(a), ctypes.byref(b)) == 0
     assert (a.value, b.value) == (37, 21)
+
+
+def test_create_rejects_non_positive_densities(gb):
+    """The face weights divide by both densities (POISSON_SOLVER.cpp:743-746 with
+    v = 1/rho): zero, negative or NaN densities are rejected before any device work."""
+    lib = gb.library()
+    h = ctypes.c_void_p()
+    g = gb.GridT(10, 10, 0, 0, 1, 1)
+    for water, air in ((0.0, 1.0), (1000.0, 0.0), (-1.0, 1.0), (float("nan"), 1.0), (1000.0, float("nan"))):
+        p = gb.ParamsT(water, air, 0.07, 1e-6, 25, 5, 0)
+        assert lib.gb2d_create(ctypes.byref(g), ctypes.byref(p), ctypes.byref(h)) == -1, (water, air)
+        assert not h.value
