@@ -567,16 +567,42 @@ static void ic0_apply(const ic0_t* L, const double* b, double* x, double* y, dou
   }
 }
 
-int or_pcg_ic0(const or_grid* gr, const or_params* pr, const double* bx, const double* by, const double* diag, const double* rhs, double* x, or_stats* st) {
-  if (!gr || !pr || !bx || !by || !diag || !rhs || !x) return OR_BAD_ARG;
+/* The PCG state between calls, so that a solve can run in slices of iterations
+ * (the CPU baseline times a full solve split over benchmark steps); the arithmetic
+ * and its order are those of one uninterrupted PCGMethod call. */
+typedef struct {
+  const double *bx, *by, *diag;
+  const or_grid* gr;
+  double* x;
+  double *buf, *r, *p, *Ap, *sv, *y, *summ;
+  ic0_t L;
+  double res_new, sqr_tol, rel_thr2;
+  int it, max_it, done;
+} pcg_run;
+
+/* ComputeResidual, IncompleteCholeskyDecomposition, the first M^-1 r and r.z
+ * (PCG_METHOD.cpp:192-212). */
+static int pcg_begin(pcg_run* R, const or_grid* gr, const or_params* pr, const double* bx, const double* by, const double* diag,
+                     const double* rhs, double* x) {
   int ni = gr->ni, nj = gr->nj;
   size_t n = (size_t)ni * nj;
   space_t s = base_space(gr);
   double idx2 = 1.0 / (s.dx * s.dx), idy2 = 1.0 / (s.dy * s.dy);
-  double* buf = zalloc(9 * n);
-  if (!buf) return OR_NO_MEMORY;
-  ic0_t L = {buf, buf + n, buf + 2 * n, ni, nj};
-  double *r = buf + 3 * n, *p = buf + 4 * n, *Ap = buf + 5 * n, *sv = buf + 6 * n, *y = buf + 7 * n, *summ = buf + 8 * n;
+  memset(R, 0, sizeof(*R));
+  R->buf = zalloc(9 * n);
+  if (!R->buf) return OR_NO_MEMORY;
+  R->gr = gr;
+  R->bx = bx;
+  R->by = by;
+  R->diag = diag;
+  R->x = x;
+  ic0_t L = {R->buf, R->buf + n, R->buf + 2 * n, ni, nj};
+  R->r = R->buf + 3 * n;
+  R->p = R->buf + 4 * n;
+  R->Ap = R->buf + 5 * n;
+  R->sv = R->buf + 6 * n;
+  R->y = R->buf + 7 * n;
+  R->summ = R->buf + 8 * n;
   for (size_t k = 0; k < n; ++k) {
     int i = (int)(k % ni), j = (int)(k / ni);
     double sum = 0;
@@ -592,51 +618,77 @@ int or_pcg_ic0(const or_grid* gr, const or_params* pr, const double* bx, const d
     }
     L.dg[k] = (k == 0) ? sqrt(diag[k]) : sqrt(diag[k] - sum);
   }
-  or_poisson_apply(gr, bx, by, diag, x, Ap);
-  for (size_t k = 0; k < n; ++k) r[k] = rhs[k] - Ap[k];
-  ic0_apply(&L, r, p, y, summ);
+  R->L = L;
+  or_poisson_apply(gr, bx, by, diag, x, R->Ap);
+  for (size_t k = 0; k < n; ++k) R->r[k] = rhs[k] - R->Ap[k];
+  ic0_apply(&R->L, R->r, R->p, R->y, R->summ);
   double res_new = 0;
-  for (size_t k = 0; k < n; ++k) res_new += r[k] * p[k];
-  double sqr_tol = pr->pcg_tolerance * pr->pcg_tolerance;
-  double rel_thr2 = 0;
+  for (size_t k = 0; k < n; ++k) res_new += R->r[k] * R->p[k];
+  R->res_new = res_new;
+  R->sqr_tol = pr->pcg_tolerance * pr->pcg_tolerance;
+  R->rel_thr2 = 0;
   if (pr->pcg_rel_residual > 0) {
     double bb = 0;
     for (size_t k = 0; k < n; ++k) bb += rhs[k] * rhs[k];
-    rel_thr2 = pr->pcg_rel_residual * pr->pcg_rel_residual * bb;
+    R->rel_thr2 = pr->pcg_rel_residual * pr->pcg_rel_residual * bb;
   }
-  int it = 0;
-  while (1) {
-    or_poisson_apply(gr, bx, by, diag, p, Ap);
+  R->max_it = pr->pcg_max_iterations;
+  return OR_OK;
+}
+
+/* Up to `count` iterations of the PCGMethod loop (PCG_METHOD.cpp:214-258); sets
+ * done once a stop test holds.  Returns the iterations run. */
+static int pcg_iterate(pcg_run* R, int count) {
+  size_t n = (size_t)R->gr->ni * R->gr->nj;
+  double *x = R->x, *r = R->r, *p = R->p, *Ap = R->Ap, *sv = R->sv;
+  int k0 = 0;
+  for (; k0 < count && !R->done; ++k0) {
+    or_poisson_apply(R->gr, R->bx, R->by, R->diag, p, Ap);
     double dot = 0;
     for (size_t k = 0; k < n; ++k) dot += p[k] * Ap[k];
-    double alpha = res_new / dot;
+    double alpha = R->res_new / dot;
     for (size_t k = 0; k < n; ++k) {
       x[k] += alpha * p[k];
       r[k] -= alpha * Ap[k];
     }
-    ic0_apply(&L, r, sv, y, summ);
-    double res_old = res_new;
-    res_new = 0;
+    ic0_apply(&R->L, r, sv, R->y, R->summ);
+    double res_old = R->res_new;
+    double res_new = 0;
     for (size_t k = 0; k < n; ++k) res_new += r[k] * sv[k];
+    R->res_new = res_new;
     double beta = res_new / res_old;
     for (size_t k = 0; k < n; ++k) {
       p[k] *= beta;
       p[k] += sv[k];
     }
-    it++;
-    if (it > pr->pcg_max_iterations) break;
-    if (res_new < sqr_tol) break;
-    if (rel_thr2 > 0) {
+    R->it++;
+    if (R->it > R->max_it || res_new < R->sqr_tol) {
+      R->done = 1;
+    } else if (R->rel_thr2 > 0) {
       double rr = 0;
       for (size_t k = 0; k < n; ++k) rr += r[k] * r[k];
-      if (rr <= rel_thr2) break;
+      if (rr <= R->rel_thr2) R->done = 1;
     }
   }
+  return k0;
+}
+
+static void pcg_end(pcg_run* R, or_stats* st) {
   if (st) {
-    st->iterations = it;
-    st->residual = sqrt(res_new);
+    st->iterations = R->it;
+    st->residual = sqrt(R->res_new);
   }
-  free(buf);
+  free(R->buf);
+  R->buf = NULL;
+}
+
+int or_pcg_ic0(const or_grid* gr, const or_params* pr, const double* bx, const double* by, const double* diag, const double* rhs, double* x, or_stats* st) {
+  if (!gr || !pr || !bx || !by || !diag || !rhs || !x) return OR_BAD_ARG;
+  pcg_run R;
+  int rc = pcg_begin(&R, gr, pr, bx, by, diag, rhs, x);
+  if (rc) return rc;
+  while (!R.done) pcg_iterate(&R, 1 << 30);
+  pcg_end(&R, st);
   return OR_OK;
 }
 
@@ -651,28 +703,82 @@ static double heaviside(double phi, double eps) {
 }
 
 /* a9-a14: PROJECTION_2D::Solve(dt, tid) (PROJECTION_2D.h:244-257) for
- * air_bubble_rising with Neumann walls and use_delta_function_formulation. */
-int or_projection(const or_grid* gr, const or_params* pr, double* phi_a, double* u_a, double* v_a, double* p_a, double* kappa, double dt, or_stats* st) {
-  if (!gr || !pr || !phi_a || !u_a || !v_a || !p_a || !kappa || gr->ni < 4 || gr->nj < 4) return OR_BAD_ARG;
+ * air_bubble_rising with Neumann walls and use_delta_function_formulation, as
+ * three calls: or_projection_begin (curvature, assembly, IC(0) factor),
+ * or_projection_iterate (slices of PCG iterations) and or_projection_finish
+ * (VectorToGrid, velocity update).  or_projection runs the three in one call. */
+struct or_projection_run {
+  or_grid gr;
+  or_params pr;
+  double *phi_a, *u_a, *v_a, *p_a, *kappa;
+  double dt;
+  double *bx, *by, *dg, *rhs, *x;
+  pcg_run pcg;
+  int pcg_open;
+};
+
+int or_projection_begin(const or_grid* gr, const or_params* pr, double* phi_a, double* u_a, double* v_a, double* p_a, double* kappa,
+                        double dt, or_projection_run** out) {
+  if (!gr || !pr || !phi_a || !u_a || !v_a || !p_a || !kappa || !out || gr->ni < 4 || gr->nj < 4) return OR_BAD_ARG;
+  *out = NULL;
   int ni = gr->ni, nj = gr->nj, rc;
   size_t n = (size_t)ni * nj;
-  space_t s = base_space(gr);
-  double* bx = zalloc((size_t)(ni + 1) * nj);
-  double* by = zalloc((size_t)ni * (nj + 1));
-  double* dg = zalloc(n);
-  double* rhs = zalloc(n);
-  double* x = zalloc(n);
-  if (!bx || !by || !dg || !rhs || !x) {
+  or_projection_run* P = (or_projection_run*)calloc(1, sizeof(or_projection_run));
+  if (!P) return OR_NO_MEMORY;
+  P->gr = *gr;
+  P->pr = *pr;
+  P->phi_a = phi_a;
+  P->u_a = u_a;
+  P->v_a = v_a;
+  P->p_a = p_a;
+  P->kappa = kappa;
+  P->dt = dt;
+  P->bx = zalloc((size_t)(ni + 1) * nj);
+  P->by = zalloc((size_t)ni * (nj + 1));
+  P->dg = zalloc(n);
+  P->rhs = zalloc(n);
+  P->x = zalloc(n);
+  if (!P->bx || !P->by || !P->dg || !P->rhs || !P->x) {
     rc = OR_NO_MEMORY;
-    goto out;
+    goto fail;
   }
   /* DetermineJumpConditionField -> ComputeCurvaturesThread fills phi's ghosts first. */
-  if ((rc = or_curvature(gr, phi_a, kappa))) goto out;
-  if ((rc = or_poisson_assemble(gr, pr, phi_a, u_a, v_a, kappa, dt, bx, by, dg, rhs))) goto out;
-  fld phi = F(phi_a, 2, ni, nj), u = F(u_a, 2, ni + 1, nj), v = F(v_a, 2, ni, nj + 1), p = F(p_a, 1, ni, nj);
-  for (int j = 0; j < nj; ++j)
-    for (int i = 0; i < ni; ++i) x[i + (size_t)j * ni] = AT(p, i, j); /* warm start (:974) */
-  if ((rc = or_pcg_ic0(gr, pr, bx, by, dg, rhs, x, st))) goto out;
+  if ((rc = or_curvature(&P->gr, phi_a, kappa))) goto fail;
+  if ((rc = or_poisson_assemble(&P->gr, &P->pr, phi_a, u_a, v_a, kappa, dt, P->bx, P->by, P->dg, P->rhs))) goto fail;
+  {
+    fld p = F(p_a, 1, ni, nj);
+    for (int j = 0; j < nj; ++j)
+      for (int i = 0; i < ni; ++i) P->x[i + (size_t)j * ni] = AT(p, i, j); /* warm start (:974) */
+  }
+  if ((rc = pcg_begin(&P->pcg, &P->gr, &P->pr, P->bx, P->by, P->dg, P->rhs, P->x))) goto fail;
+  P->pcg_open = 1;
+  *out = P;
+  return OR_OK;
+fail:
+  or_projection_free(P);
+  return rc;
+}
+
+int or_projection_iterate(or_projection_run* P, int count, int* done) {
+  if (!P || !P->pcg_open || count < 0) return OR_BAD_ARG;
+  int k = pcg_iterate(&P->pcg, count);
+  if (done) *done = P->pcg.done;
+  return k;
+}
+
+int or_projection_finish(or_projection_run* P, or_stats* st) {
+  if (!P || !P->pcg_open) return OR_BAD_ARG;
+  while (!P->pcg.done) pcg_iterate(&P->pcg, 1 << 30);
+  pcg_end(&P->pcg, st);
+  P->pcg_open = 0;
+  const or_grid* gr = &P->gr;
+  const or_params* pr = &P->pr;
+  int ni = gr->ni, nj = gr->nj;
+  double dt = P->dt;
+  const double* kappa = P->kappa;
+  const double* x = P->x;
+  space_t s = base_space(gr);
+  fld phi = F(P->phi_a, 2, ni, nj), u = F(P->u_a, 2, ni + 1, nj), v = F(P->v_a, 2, ni, nj + 1), p = F(P->p_a, 1, ni, nj);
   for (int j = 0; j < nj; ++j)
     for (int i = 0; i < ni; ++i) AT(p, i, j) = x[i + (size_t)j * ni]; /* VectorToGrid */
 
@@ -731,13 +837,26 @@ int or_projection(const or_grid* gr, const or_params* pr, double* phi_a, double*
       st->max_velocity_y = mvy;
     }
   }
-  rc = OR_OK;
-out:
-  free(bx);
-  free(by);
-  free(dg);
-  free(rhs);
-  free(x);
+  return OR_OK;
+}
+
+void or_projection_free(or_projection_run* P) {
+  if (!P) return;
+  if (P->pcg_open) pcg_end(&P->pcg, NULL);
+  free(P->bx);
+  free(P->by);
+  free(P->dg);
+  free(P->rhs);
+  free(P->x);
+  free(P);
+}
+
+int or_projection(const or_grid* gr, const or_params* pr, double* phi_a, double* u_a, double* v_a, double* p_a, double* kappa, double dt, or_stats* st) {
+  or_projection_run* P = NULL;
+  int rc = or_projection_begin(gr, pr, phi_a, u_a, v_a, p_a, kappa, dt, &P);
+  if (rc) return rc;
+  rc = or_projection_finish(P, st);
+  or_projection_free(P);
   return rc;
 }
 

@@ -85,6 +85,17 @@ int or_velocity_advection(const or_grid* gr, const or_params* pr, double* u, dou
 int or_curvature(const or_grid* gr, double* phi, double* kappa);
 /* a9-a14: one PROJECTION_2D::Solve(dt, tid); p is the warm start and the result. */
 int or_projection(const or_grid* gr, const or_params* pr, double* phi, double* u, double* v, double* p, double* kappa, double dt, or_stats* st);
+/* The same projection as three calls, so that its PCG can run in slices of
+ * iterations: begin (curvature, assembly, IC(0) factor, first residual), iterate
+ * (at most `count` PCG iterations; returns how many ran, *done = 1 once a stop
+ * test holds), finish (remaining iterations, VectorToGrid, velocity update).  The
+ * arrays passed to begin must stay valid until finish; free releases the run. */
+typedef struct or_projection_run or_projection_run;
+int or_projection_begin(const or_grid* gr, const or_params* pr, double* phi, double* u, double* v, double* p, double* kappa, double dt,
+                        or_projection_run** run);
+int or_projection_iterate(or_projection_run* run, int count, int* done);
+int or_projection_finish(or_projection_run* run, or_stats* st);
+void or_projection_free(or_projection_run* run);
 
 /* Rest of SolveForRK (EULERIAN_FLUID_SOLVER_2D.h:1857-1879). */
 int or_apply_gravity(const or_grid* gr, const or_flow* fl, double* u, double* v, double dt);

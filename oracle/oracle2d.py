@@ -67,6 +67,11 @@ def lib():
         L.or_poisson_assemble.argtypes = [G, R, P, P, P, P, d, P, P, P, P]
         L.or_poisson_apply.argtypes = [G, P, P, P, P, P]
         L.or_pcg_ic0.argtypes = [G, R, P, P, P, P, P, S]
+        L.or_projection_begin.argtypes = [G, R, P, P, P, P, P, d, ctypes.POINTER(ctypes.c_void_p)]
+        L.or_projection_iterate.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.or_projection_finish.argtypes = [ctypes.c_void_p, S]
+        L.or_projection_free.argtypes = [ctypes.c_void_p]
+        L.or_projection_free.restype = None
         L.or_fill_ghost_extrapolate.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         W = ctypes.POINTER(Flow)
         L.or_cfl_time_step.argtypes = [G, R, W, P, P, P, d, P]
@@ -83,6 +88,7 @@ def lib():
         L.or_time_step.argtypes = [G, R, W, P, P, P, P, P, P, P, P, d, S]
         for f in ("or_levelset_advection", "or_reinitialization", "or_levelset_rk3", "or_velocity_advection",
                   "or_curvature", "or_projection", "or_poisson_assemble", "or_pcg_ic0", "or_apply_gravity",
+                  "or_projection_begin", "or_projection_iterate", "or_projection_finish",
                   "or_sourcing", "or_solve_for_rk", "or_time_step"):
             getattr(L, f).restype = ctypes.c_int
         _lib = L
@@ -134,6 +140,46 @@ def projection(g, pr, phi, u, v, p, kappa, dt):
     st = Stats()
     _check(lib().or_projection(ctypes.byref(g), ctypes.byref(pr), _p(phi), _p(u), _p(v), _p(p), _p(kappa), dt, ctypes.byref(st)), "projection")
     return st
+
+
+class ProjectionRun:
+    """or_projection split into slices: begin (curvature, assembly, IC(0) factor) at
+    construction, iterate(count) runs at most `count` PCG iterations and returns how many
+    ran, finish() runs the rest and the velocity update.  The arrays are updated in place
+    and must stay alive until finish()."""
+
+    def __init__(self, g, pr, phi, u, v, p, kappa, dt):
+        self._keep = (g, pr, phi, u, v, p, kappa)
+        h = ctypes.c_void_p()
+        _check(lib().or_projection_begin(ctypes.byref(g), ctypes.byref(pr), _p(phi), _p(u), _p(v), _p(p), _p(kappa), dt,
+                                         ctypes.byref(h)), "projection_begin")
+        self.h = h
+        self.done = False
+
+    def iterate(self, count):
+        d = ctypes.c_int(0)
+        k = lib().or_projection_iterate(self.h, count, ctypes.byref(d))
+        if k < 0:
+            raise RuntimeError(f"oracle projection_iterate failed with status {k}")
+        self.done = bool(d.value)
+        return k
+
+    def finish(self):
+        st = Stats()
+        _check(lib().or_projection_finish(self.h, ctypes.byref(st)), "projection_finish")
+        self.close()
+        return st
+
+    def close(self):
+        if self.h:
+            lib().or_projection_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def poisson_assemble(g, pr, phi, u, v, kappa, dt):
