@@ -467,9 +467,16 @@ def time_step_window_loss(gb, ni, nj, phi0, u0, v0, water, air, dt, steps, check
                           viscosity=None, gravity=(0.0, -9.8), p0=None, x_max=1.0, y_max=1.0):
     """The bubble's centroid height after `steps` whole order-3 time steps (time_step, the
     reinitialisation off inside the window) from (phi0, u0, v0) at rest-frame advecting copies of
-    u0, v0, with torch.utils.checkpoint segments of `checkpoint_every` steps, so that only every
-    segment's starting state is kept for the backward pass.  Differentiable in phi0, u0, v0 and
-    the densities water, air (0-d tensors).  viscosity: set_flow_params' viscosities, or None."""
+    u0, v0, with torch.utils.checkpoint segments of `checkpoint_every` steps.  Differentiable in
+    phi0, u0, v0 and the densities water, air (0-d tensors).  viscosity: set_flow_params'
+    viscosities, or None.
+
+    Memory: the segments run their forward without building a graph (re-entrant checkpoint),
+    so the GPU contexts that the velocity-advection, viscosity and projection operations hold
+    for their backward exist only while one segment is recomputed and differentiated; between
+    segments only each segment's starting state and its starting warm-start pressure are kept.
+    The recompute starts every projection from the same warm start as the first forward did, so
+    it repeats that forward exactly."""
     opts = solve_opts(precision=0, tolerance=1e-10, max_iterations=20000) if opts is None else opts
     kw = dict(x_max=x_max, y_max=y_max, surface_tension=surface_tension, reinit_iterations=0, advection_precision=0)
 
@@ -484,14 +491,15 @@ def time_step_window_loss(gb, ni, nj, phi0, u0, v0, water, air, dt, steps, check
     while k < steps:
         n = min(checkpoint_every, steps - k)
 
-        def segment(p, uu, vv, aa, bb, w, a, n=n):
+        def segment(p, uu, vv, aa, bb, w, a, n=n, p_start=state["p"].copy()):
+            state["p"] = p_start.copy()  # the warm start this segment began from, also when recomputed
             for _ in range(n):
                 p, uu, vv, aa, bb = time_step(ls, p, uu, vv, aa, bb, w, a, dt, make, state, opts, gravity, viscosity=viscosity)
             return p, uu, vv, aa, bb
 
         args = (phi, u, v, ua, va, water, air)
-        if any(isinstance(x, torch.Tensor) and x.requires_grad for x in args):
-            phi, u, v, ua, va = torch.utils.checkpoint.checkpoint(segment, *args, use_reentrant=False)
+        if torch.is_grad_enabled() and any(isinstance(x, torch.Tensor) and x.requires_grad for x in args):
+            phi, u, v, ua, va = torch.utils.checkpoint.checkpoint(segment, *args, use_reentrant=True)
         else:
             phi, u, v, ua, va = segment(*args)
         k += n
