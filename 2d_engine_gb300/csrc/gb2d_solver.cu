@@ -1264,10 +1264,9 @@ inline bool stream_smoother() {
   return on;
 }
 
-// Rows per segment: S = 32 m - 2 EXTRA (so that the S + 2 EXTRA steps of a block fill
-// whole unrolled passes over the coefficient ring), the largest that still gives the
-// launch `target` blocks (one per strip and segment), at least 16 rows (below that the
-// vertical halo would exceed the work).
+// Rows per segment: an even S that gives the launch about `target` blocks (one per
+// strip and segment), at least 16 rows (below that the vertical halo would exceed
+// the work) and at most 256.  A block takes S + 2 EXTRA steps.
 struct StreamPlan {
   int S, nsteps, blocks;
 };
@@ -1279,18 +1278,14 @@ inline StreamPlan stream_plan(int nI, int nJ, int ns, bool post) {
   const int out = post ? st::W - 4 * ns : st::W - 2 - 4 * ns;
   const int extra = post ? 4 * ns : 4 * ns + 2;
   const int nstrips = post ? (nI + 1 + out - 1) / out : (nI + out - 1) / out;
-  int best = -1;
-  for (int m = 1; m <= 64; ++m) {
-    const int S = st::CRING * m - 2 * extra;
-    if (S < 16) continue;
-    if (best < 0) best = S;  // the smallest admissible S
-    if ((long long)nstrips * ((nJ + S - 1) / S) >= target) best = S;
-    if (S >= nJ) break;
-  }
+  const int segs = (target + nstrips - 1) / nstrips;
+  int S = (nJ + segs - 1) / segs;
+  S += S & 1;
+  S = S < 16 ? 16 : S > 256 ? 256 : S;
   StreamPlan p;
-  p.S = best;
-  p.nsteps = best + 2 * extra;
-  p.blocks = nstrips * ((nJ + best - 1) / best);
+  p.S = S;
+  p.nsteps = S + 2 * extra;
+  p.blocks = nstrips * ((nJ + S - 1) / S);
   return p;
 }
 

@@ -106,55 +106,70 @@ struct StCtx {
   bool ain, bin, out_a, out_b;
 };
 
-// Stage array a of row r into coefficient slot `slot` (the row's index from rs, mod CRING).
-template <typename T, bool POST, bool VEC>
-__device__ __forceinline__ void stage_array(const StCtx<T>& c, int a, int slot, int r) {
-  constexpr int NA = Arr<POST>::N;
-  T* d = c.cring + (size_t)slot * NA * W + a * W + 2 * c.lane;
-  const bool rin = r >= 0 && r < c.L.nJ;
-  if (POST && a == kXc) {  // the coarse correction each fine cell receives (piecewise-constant prolongation)
-    const T* g = c.C.x + (long long)((r >> 1) + 1) * c.C.ld + 1;
-    if (rin && c.ain)
-      cp_async_n<sizeof(T)>(d, g + (c.ca >> 1));
-    else
-      d[0] = T(0);
-    if (rin && c.bin)
-      cp_async_n<sizeof(T)>(d + 1, g + (c.cb >> 1));
-    else
-      d[1] = T(0);
-    return;
-  }
-  const T* src = a == kB ? c.L.b : a == kId ? c.L.idg : a == kCx ? c.L.cx : a == kCy ? c.L.cy : c.L.x;
-  stage_pair<T, VEC>(d, src + (long long)(c.ca + 1) + (long long)(r + 1) * c.L.ld, rin, c.ain, c.bin);
-}
-
-// The step loop of one warp role, unrolled over the coefficient ring so that every
-// ring slot is a compile-time offset: row rs + k lives in coefficient slot k mod
-// CRING and x slot k mod XRING.  ROLE < 2NS: half sweep ROLE + 1 (the last one also
-// writes the finished rows); ROLE == 2NS (pre-smoothing): residual and restriction.
-// Every role passes the block barrier once per step.
-template <typename T, int NS, bool POST, bool VEC, int ROLE>
-__device__ __forceinline__ void role_loop(const StCtx<T>& c, Acc<T>& acc, bool rz) {
+// The step loop, one body for every warp (a warp's role is a runtime value, so
+// the code stays small enough for the instruction cache).  role < 2NS: half sweep
+// role + 1 (the last one also writes the finished rows); role == 2NS
+// (pre-smoothing): residual and restriction.  Row rs + k lives in coefficient slot
+// k mod CRING and x slot k mod XRING.  The loop is unrolled by two so that every
+// row parity is a compile-time value; each warp passes the block barrier once per
+// step.
+template <typename T, int NS, bool POST, bool VEC>
+__device__ __forceinline__ void stream_loop(const StCtx<T>& c, int role, Acc<T>& acc, bool rz) {
   using G = Geo<NS, POST>;
-  constexpr int NA = Arr<POST>::N;
+  constexpr int NA = Arr<POST>::N, ROW = NA * W;
   constexpr int RS_ODD = POST ? 0 : 1;  // rs = r0 - BELOW with r0 even
+  constexpr int MAXA = (NA + G::WARPS - 1) / G::WARPS;
   const int lane = c.lane;
-  T qacc = T(0);
-  for (int base = 0; base < c.nsteps; base += CRING) {
+  // This warp's staged arrays: their source at column ca of row rs + AHEAD, advanced
+  // by one row per step (the coarse correction is addressed per row instead).
+  const T* gsrc[MAXA];
+  int aoff[MAXA];
 #pragma unroll
-    for (int j = 0; j < CRING; ++j) {
-      const int i = base + j;  // step: row rs + i enters the pipeline
+  for (int m = 0; m < MAXA; ++m) {
+    const int a = role + m * G::WARPS;
+    aoff[m] = a < NA ? a * W + 2 * lane : -1;
+    const T* src = a == kB ? c.L.b : a == kId ? c.L.idg : a == kCx ? c.L.cx : a == kCy ? c.L.cy : c.L.x;
+    gsrc[m] = src + (long long)(c.ca + 1) + (long long)(c.rs + AHEAD + 1) * c.L.ld;
+  }
+  const int s = role + 1;  // half sweep of a sweeping role
+  const int color = POST ? (s & 1) : ((s - 1) & 1);  // red first from zero, black first after the correction
+  T qacc = T(0);
+  for (int i0 = 0; i0 < c.nsteps; i0 += 2) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = i0 + h;  // step: row rs + i enters the pipeline
       cp_wait<AHEAD - 1>();
       asm volatile("bar.sync 0;" ::: "memory");  // row rs + i staged everywhere; the previous step done everywhere
       {
-        const int k = i + AHEAD;
-        if (k <= c.nrows)  // one row beyond the last: its cy is the last row's top face
-          for (int a = ROLE; a < NA; a += G::WARPS) stage_array<T, POST, VEC>(c, a, (j + AHEAD) & (CRING - 1), c.rs + k);
+        const int k = i + AHEAD, r = c.rs + k;
+        if (k <= c.nrows) {  // one row beyond the last: its cy is the last row's top face
+          T* row = c.cring + (size_t)(k & (CRING - 1)) * ROW;
+          const bool rin = r >= 0 && r < c.L.nJ;
+#pragma unroll
+          for (int m = 0; m < MAXA; ++m) {
+            if (aoff[m] < 0) continue;
+            T* d = row + aoff[m];
+            if (POST && aoff[m] - 2 * lane == kXc * W) {  // the coarse correction (piecewise-constant prolongation)
+              const T* g = c.C.x + (long long)((r >> 1) + 1) * c.C.ld + 1;
+              if (rin && c.ain)
+                cp_async_n<sizeof(T)>(d, g + (c.ca >> 1));
+              else
+                d[0] = T(0);
+              if (rin && c.bin)
+                cp_async_n<sizeof(T)>(d + 1, g + (c.cb >> 1));
+              else
+                d[1] = T(0);
+            } else {
+              stage_pair<T, VEC>(d, gsrc[m], rin, c.ain, c.bin);
+            }
+            gsrc[m] += c.L.ld;
+          }
+        }
         cp_commit();
       }
-      if (ROLE == 0 && i < c.nrows) {  // x of row rs + i before the sweeps
-        const T* R = c.cring + (size_t)j * NA * W + 2 * lane;
-        T* X = c.xring + (size_t)(j & (XRING - 1)) * W + 2 * lane;
+      if (role == 0 && i < c.nrows) {  // x of row rs + i before the sweeps
+        const T* R = c.cring + (size_t)(i & (CRING - 1)) * ROW + 2 * lane;
+        T* X = c.xring + (size_t)(i & (XRING - 1)) * W + 2 * lane;
         if (POST) {
           X[0] = R[kXa * W] + R[kXc * W];
           X[1] = R[kXa * W + 1] + R[kXc * W + 1];
@@ -162,24 +177,20 @@ __device__ __forceinline__ void role_loop(const StCtx<T>& c, Acc<T>& acc, bool r
           X[0] = X[1] = T(0);
         }
       }
-      if (ROLE < 2 * NS) {
-        constexpr int S = ROLE + 1;  // half sweep of this role
-        const int k = i - 2 * S;     // row rs + k
+      if (role < 2 * NS) {
+        const int k = i - 2 * s;  // row rs + k: its parity is that of rs + h
         if (k >= 0 && k < c.nrows) {
-          constexpr int COLOR = POST ? (S & 1) : ((S - 1) & 1);  // red first from zero, black first after the correction
           // Cell (col, r) has colour (col + r) & 1; ca is odd, cb = ca + 1 even.
-          const int jr = (j - 2 * S) & (CRING - 1);
-          const bool upd_b = ((RS_ODD + j - 2 * S) & 1) == COLOR;  // compile-time after unrolling
-          const int col = 2 * lane + (upd_b ? 1 : 0);
-          T* X0 = c.xring + (size_t)(jr & (XRING - 1)) * W;
-          const T* Xm = c.xring + (size_t)((jr - 1) & (XRING - 1)) * W;
-          const T* Xp = c.xring + (size_t)((jr + 1) & (XRING - 1)) * W;
-          const T* C0 = c.cring + (size_t)jr * NA * W;
-          const T* C1 = c.cring + (size_t)((jr + 1) & (CRING - 1)) * NA * W;
+          const int col = 2 * lane + (((RS_ODD + h) & 1) == color ? 1 : 0);
+          T* X0 = c.xring + (size_t)(k & (XRING - 1)) * W;
+          const T* Xm = c.xring + (size_t)((k - 1) & (XRING - 1)) * W;
+          const T* Xp = c.xring + (size_t)((k + 1) & (XRING - 1)) * W;
+          const T* C0 = c.cring + (size_t)(k & (CRING - 1)) * ROW;
+          const T* C1 = c.cring + (size_t)((k + 1) & (CRING - 1)) * ROW;
           const int cl = col > 0 ? col - 1 : 0, cr = col < W - 1 ? col + 1 : W - 1;  // strip edges: halo, any value
           X0[col] = gs_update(C0[kB * W + col], C0[kCx * W + col], X0[cl], C0[kCx * W + cr], X0[cr], C0[kCy * W + col], Xm[col],
                               C1[kCy * W + col], Xp[col], C0[kId * W + col]);
-          if (S == 2 * NS) {  // row rs + k is final: write it (and, after the correction, add its r.z)
+          if (s == 2 * NS) {  // row rs + k is final: write it (and, after the correction, add its r.z)
             const int r = c.rs + k;
             if (r >= c.r0 && r < c.r1 && r < c.L.nJ) {
               __syncwarp();
@@ -198,18 +209,17 @@ __device__ __forceinline__ void role_loop(const StCtx<T>& c, Acc<T>& acc, bool r
         // Residual of row q = rs + k (its final x: rows q - 1 .. q + 1), restricted by row
         // pairs: coarse cell (I, J) averages the red cells (2I, 2J) and (2I + 1, 2J + 1),
         // in that order.
-        const int k = i - 4 * NS - 2;
+        const int k = i - 4 * NS - 2;  // q has the parity of rs + h
         if (k >= 0 && k < c.nrows - 1) {
           const int q = c.rs + k;
-          const int jq = (j - 4 * NS - 2) & (CRING - 1);
-          const bool even = ((RS_ODD + j - 4 * NS - 2) & 1) == 0;  // compile-time after unrolling
-          const int col = even ? 2 * lane + 1 : 2 * lane;           // red: cb on even rows, ca on odd rows
-          const bool inside = q >= 0 && q < c.L.nJ && (even ? (c.cb >= 0 && c.cb < c.L.nI) : (c.ca >= 0 && c.ca < c.L.nI));
-          const T* X0 = c.xring + (size_t)(jq & (XRING - 1)) * W;
-          const T* Xm = c.xring + (size_t)((jq - 1) & (XRING - 1)) * W;
-          const T* Xp = c.xring + (size_t)((jq + 1) & (XRING - 1)) * W;
-          const T* C0 = c.cring + (size_t)jq * NA * W;
-          const T* C1 = c.cring + (size_t)((jq + 1) & (CRING - 1)) * NA * W;
+          const bool even = ((RS_ODD + h) & 1) == 0;
+          const int col = even ? 2 * lane + 1 : 2 * lane;  // red: cb on even rows, ca on odd rows
+          const bool inside = q >= 0 && q < c.L.nJ && (even ? c.bin : c.ain);
+          const T* X0 = c.xring + (size_t)(k & (XRING - 1)) * W;
+          const T* Xm = c.xring + (size_t)((k - 1) & (XRING - 1)) * W;
+          const T* Xp = c.xring + (size_t)((k + 1) & (XRING - 1)) * W;
+          const T* C0 = c.cring + (size_t)(k & (CRING - 1)) * ROW;
+          const T* C1 = c.cring + (size_t)((k + 1) & (CRING - 1)) * ROW;
           const int cl = col > 0 ? col - 1 : 0, cr = col < W - 1 ? col + 1 : W - 1;
           const T res = gs_residual(C0[kB * W + col], diag_of(C0[kId * W + col]), X0[col], C0[kCx * W + col], X0[cl], C0[kCx * W + cr],
                                     X0[cr], C0[kCy * W + col], Xm[col], C1[kCy * W + col], Xp[col]);
@@ -229,16 +239,6 @@ __device__ __forceinline__ void role_loop(const StCtx<T>& c, Acc<T>& acc, bool r
   }
 }
 
-template <typename T, int NS, bool POST, bool VEC, int ROLE>
-__device__ __forceinline__ void run_role(int warp, const StCtx<T>& c, Acc<T>& acc, bool rz) {
-  if constexpr (ROLE < Geo<NS, POST>::WARPS) {
-    if (warp == ROLE)
-      role_loop<T, NS, POST, VEC, ROLE>(c, acc, rz);
-    else
-      run_role<T, NS, POST, VEC, ROLE + 1>(warp, c, acc, rz);
-  }
-}
-
 }  // namespace st
 
 // One V-cycle side on one level (see the comment at the top of this file).  One
@@ -246,7 +246,7 @@ __device__ __forceinline__ void run_role(int warp, const StCtx<T>& c, Acc<T>& ac
 // xout, the coarse right-hand side to C.b.  POST = true: x = L.x + prolonged C.x,
 // NS sweeps black first, x to xout; with part_rz (the finest level) r.z is reduced
 // and beta published.  S: output rows per segment (even); nsteps: steps per block,
-// a multiple of CRING, at least S + 2 EXTRA.
+// even, at least S + 2 EXTRA.
 template <typename T, int NS, bool POST, bool VEC>
 __global__ void __launch_bounds__(32 * st::Geo<NS, POST>::WARPS)
     k_stream(Level<T> L, Level<T> C, T* __restrict__ xout, int S, int nsteps, double* __restrict__ part_rz,
@@ -284,13 +284,32 @@ __global__ void __launch_bounds__(32 * st::Geo<NS, POST>::WARPS)
   c.out_b = c.bin && c.cb >= olo && c.cb < ohi;
 
   for (int q = threadIdx.x; q < XRING * W; q += blockDim.x) c.xring[q] = T(0);
-  // Prologue: rows rs .. rs + AHEAD - 1 (AHEAD < S + EXTRA for every admissible S).
+  // Prologue: rows rs .. rs + AHEAD - 1 (AHEAD < S + EXTRA for every admissible S),
+  // warp w copying arrays w, w + WARPS, ...
   for (int k = 0; k < AHEAD; ++k) {
-    for (int a = warp; a < NA; a += G::WARPS) stage_array<T, POST, VEC>(c, a, k, c.rs + k);
+    const int r = c.rs + k;
+    const bool rin = r >= 0 && r < L.nJ;
+    for (int a = warp; a < NA; a += G::WARPS) {
+      T* d = c.cring + (size_t)k * NA * W + a * W + 2 * c.lane;
+      if (POST && a == kXc) {
+        const T* g = C.x + (long long)((r >> 1) + 1) * C.ld + 1;
+        if (rin && c.ain)
+          cp_async_n<sizeof(T)>(d, g + (c.ca >> 1));
+        else
+          d[0] = T(0);
+        if (rin && c.bin)
+          cp_async_n<sizeof(T)>(d + 1, g + (c.cb >> 1));
+        else
+          d[1] = T(0);
+      } else {
+        const T* src = a == kB ? L.b : a == kId ? L.idg : a == kCx ? L.cx : a == kCy ? L.cy : L.x;
+        stage_pair<T, VEC>(d, src + (long long)(c.ca + 1) + (long long)(r + 1) * L.ld, rin, c.ain, c.bin);
+      }
+    }
     cp_commit();
   }
   Acc<T> acc;
-  run_role<T, NS, POST, VEC, 0>(warp, c, acc, part_rz != nullptr);
+  stream_loop<T, NS, POST, VEC>(c, warp, acc, part_rz != nullptr);
   cp_wait<0>();
   if (POST && part_rz) {
     double rz;

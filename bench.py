@@ -223,33 +223,58 @@ def cpu_baseline(case, sample_iterations):
 BATCH_INSTANCES, BATCH_FRAMES, BATCH_SEED = 256, 10, 3
 
 
-def run_rayleigh_taylor(gb, stream, n=2048, frames=4):
+def run_rayleigh_taylor(gb, stream, n=2048, frames=500, every=50):
     """Rayleigh-Taylor on 2048 x 2048 nodes over [0,1] x [0,2] (dy = 2 dx, the reference's
     dx-only diagonal): interface y = 1 + 0.05 cos(2 pi x), densities 3 over 1, viscosity 1e-3,
     no surface tension; mixed precision (FP32 WENO5 / reinit / ENO3 fluxes, FP32 V-cycles),
-    CFL time steps.  One untimed frame, then `frames` timed with CUDA events."""
+    CFL time steps, 500 frames, each timed with CUDA events.  Every 50 frames the state is
+    also restarted for one frame on the FP64 path (untimed) and the frame's results compared
+    (tests/test_gpu_rt_long.py holds the FP64 path to the CPU oracle on the same trajectory
+    at 512^2)."""
+    import numpy as np
     import torch
     from tests.golden.cases import rayleigh_taylor_level_set
-    c = gb.Context(n, n, 0.0, 0.0, 1.0, 2.0, water_density=3.0, air_density=1.0, surface_tension=0.0,
-                   advection_precision=gb.PRECISION_MIXED)
-    c.set_stream(stream.cuda_stream)
-    c.set_flow_params(water_viscosity=1e-3, air_viscosity=1e-3, gravity=(0.0, -9.8), viscosity=True, cfl_number=0.5)
+    mk = lambda prec: gb.Context(n, n, 0.0, 0.0, 1.0, 2.0, water_density=3.0, air_density=1.0, surface_tension=0.0,
+                                 advection_precision=prec)
+    c, c64 = mk(gb.PRECISION_MIXED), mk(gb.PRECISION_FP64)
+    for x in (c, c64):
+        x.set_stream(stream.cuda_stream)
+        x.set_flow_params(water_viscosity=1e-3, air_viscosity=1e-3, gravity=(0.0, -9.8), viscosity=True, cfl_number=0.5)
     c.set(gb.FIELD_PHI, rayleigh_taylor_level_set(n, n))
     opts = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=TOL)
-    dt, _ = c.advance_frame(cfl=1.0, prev_dt=0.0, opts=opts, allow_max_iters=True)
-    ms, its = [], []
-    for _ in range(frames):
+    o64 = gb.solve_opts(precision=gb.PRECISION_FP64, tolerance=1e-10, max_iterations=2000)
+    ids = (gb.FIELD_PHI, gb.FIELD_U, gb.FIELD_V, gb.FIELD_UA, gb.FIELD_VA, gb.FIELD_P)
+    inner = (slice(2, 2 + n), slice(2, 2 + n))
+    dt = 0.0
+    ms, its, worst = [], [], {}
+    for f in range(1, frames + 1):
+        check = f % every == 0
+        if check:
+            for fid in ids:
+                c64.set(fid, c.get(fid))
         with torch.cuda.stream(stream):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            dt, st = c.advance_frame(cfl=1.0, prev_dt=dt, opts=opts, allow_max_iters=True)
+            dt_new, st = c.advance_frame(cfl=1.0, prev_dt=dt, opts=opts, allow_max_iters=True)
             e1.record(stream)
         e1.synchronize()
         ms.append(e0.elapsed_time(e1))
         its.append(st.iterations / 3.0)
+        if check:
+            c64.advance_frame(cfl=1.0, prev_dt=dt, opts=o64, allow_max_iters=True)
+            for name, fid in (("phi", gb.FIELD_PHI), ("u", gb.FIELD_U), ("v", gb.FIELD_V), ("p", gb.FIELD_P)):
+                a, b = c.get(fid), c64.get(fid)
+                if name == "phi":
+                    a, b = a[inner], b[inner]
+                e = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+                worst[name] = max(worst.get(name, 0.0), e)
+        dt = dt_new
     c.close()
+    c64.close()
     return {"nodes": [n, n], "domain": [1.0, 2.0], "frames_timed": frames, "ms_per_frame": statistics.mean(ms),
-            "cg_iterations_per_projection": statistics.mean(its), "last_dt": dt, "precision": "mixed"}
+            "ms_per_frame_first_50": statistics.mean(ms[:50]), "ms_per_frame_last_50": statistics.mean(ms[-50:]),
+            "cg_iterations_per_projection": statistics.mean(its), "last_dt": dt, "precision": "mixed",
+            "one_frame_restarts_every": every, "max_rel_l2_mixed_vs_fp64_frame": worst}
 
 
 def run_batch(gb, n, frames, cpu=True, dist=None, rank=0, ws=1):

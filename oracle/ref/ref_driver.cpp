@@ -272,9 +272,40 @@ struct RefPoisson {
   POISSON_EQUATION_TEST test;
 };
 
+/* Test 8's interface as SIMULATION_WORLD builds it (SIMULATION_WORLD.h:945-1070): the
+ * distance to 8000 samples of the five-petal curve r = 0.5 + 0.2 sin(5 theta) about
+ * (0.02 sqrt 5, 0.02 sqrt 5), signed by comparing the node with that curve at the
+ * node's own polar angle about the origin (the reference's test, kept as it is). */
+static T star_levelset(T x, T y) {
+  const int samples = 8000;
+  const T c = (T)0.02 * sqrt((T)5);
+  T best = 0;
+  for (int p = 0; p < samples; ++p) {
+    const T th = (T)2 * PI * p / samples;
+    const T px = c + ((T)0.5 + (T)0.2 * sin(5 * th)) * cos(th);
+    const T py = c + ((T)0.5 + (T)0.2 * sin(5 * th)) * sin(th);
+    const T d = sqrt(POW2(x - px) + POW2(y - py));
+    if (p == 0 || d <= best) best = d;
+  }
+  const T ratio = y / x;
+  T ang;
+  if (x >= (T)0 && y >= (T)0)
+    ang = atan(ratio);
+  else if (x <= (T)0 && y >= (T)0)
+    ang = PI + atan(ratio);
+  else if (x <= (T)0 && y <= (T)0)
+    ang = PI + atan(ratio);
+  else
+    ang = 2 * PI + atan(ratio);
+  const T side = POW2(x - 0.02 * sqrt(5)) + POW2(y - 0.02 * sqrt(5)) - POW2(0.5 + 0.2 * sin(5 * ang));
+  if (side > 0) return best;
+  if (side < 0) return -best;
+  return 0;  // on the curve, or a NaN test (the origin's angle): the reference leaves 0
+}
+
 void* ref_poisson_create(int test_number, int n, double tolerance, int max_iteration) {
   std::cout.rdbuf(&g_null);
-  if (test_number != 3 && test_number != 5) return 0;
+  if (test_number != 3 && test_number != 5 && test_number != 8) return 0;
   RefPoisson* r = new RefPoisson;
   r->mt.Initialize(1);
   r->world.poisson_equation_with_jump_condition_test = true;
@@ -299,8 +330,10 @@ void* ref_poisson_create(int test_number, int n, double tolerance, int max_itera
       T x = g.x_min + i * g.dx, y = g.y_min + j * g.dy;
       if (test_number == 3)
         ls(i, j) = sqrt(POW2(x - (T)0.5) + POW2(y - (T)0.5)) - (T)0.25;
-      else
+      else if (test_number == 5)
         ls(i, j) = sqrt(POW2(x) + POW2(y)) - (T)0.5;
+      else
+        ls(i, j) = star_levelset(x, y);
     }
   ls.FillGhostCellsFromThreaded(&(ls.phi), false);
   return r;

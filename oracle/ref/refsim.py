@@ -130,7 +130,7 @@ class RefSim:
 
 
 class RefPoissonTest:
-    """POISSON_EQUATION_TEST of the reference (tests 3 and 5: jump-condition Poisson on
+    """POISSON_EQUATION_TEST of the reference (tests 3, 5 and 8: jump-condition Poisson on
     [-1,1]^2 with n x n nodes, Dirichlet boundaries, PCG)."""
 
     FIELDS = dict(solution=0, true_solution=1, beta=2, rhs=3, jc_on_solution=4, jc_on_derivative=5, bc=6, levelset=7,
@@ -149,7 +149,7 @@ class RefPoissonTest:
         self.L = L
         self.h = L.ref_poisson_create(test_number, n, tolerance, max_iteration)
         if not self.h:
-            raise ValueError("test number must be 3 or 5")
+            raise ValueError("test number must be 3, 5 or 8")
 
     def solve(self):
         return self.L.ref_poisson_solve(self.h)

@@ -23,9 +23,9 @@ tests/golden/cases.py and stores inputs and outputs:
   fast sweeping       FastSweepingMethodOriginal with 1 and 4 sweeps
 and, in rising_bubble_128_frames.npz, 100 frames of the 128^2 rising bubble
 (SIMULATION_WORLD::AdvanceOneFrame: curvature, CFL time step, time step); in
-poisson_test{3,5}_61.npz, POISSON_EQUATION_TEST's jump-condition problems 3 and 5.
+poisson_test{3,5,8}_61.npz, POISSON_EQUATION_TEST's jump-condition problems 3, 5 and 8.
 
-Usage:  python tests/golden/make_golden.py   (needs the reference sources)
+Usage:  python tests/golden/make_golden.py [name ...]   (needs the reference sources)
 """
 import os
 import sys
@@ -214,17 +214,25 @@ def make_poisson_test(name, test_number, n):
     print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB, CG {its} iterations, L2 error {l2:.3e}")
 
 
+FIXTURES = {
+    "bubbles_17": lambda: make_case("bubbles_17", bubbles_case(17, seed=1), 0.5 / 16, 1e-13),
+    "bubbles_33": lambda: make_case("bubbles_33", bubbles_case(33, seed=2), 0.5 / 32, 1e-13),
+    "rising_bubble_40x24": lambda: make_case("rising_bubble_40x24", rising_bubble_case(40, 24, seed=3), 0.01, 1e-13),
+    "tall_24x40": lambda: make_case("tall_24x40", bubbles_case(24, 40, seed=4, x_max=1.0, y_max=2.0), 0.02, 1e-13),
+    "bubbles_65": lambda: make_case("bubbles_65", bubbles_case(65, seed=5), 0.5 / 64, 1e-12, flow=False),
+    "rising_bubble_128_frames": lambda: make_rising_bubble_run("rising_bubble_128_frames"),
+    "poisson_test3_61": lambda: make_poisson_test("poisson_test3_61", 3, 61),
+    "poisson_test5_61": lambda: make_poisson_test("poisson_test5_61", 5, 61),
+    "poisson_test8_61": lambda: make_poisson_test("poisson_test8_61", 8, 61),
+}
+
+
 def main():
+    """python tests/golden/make_golden.py [name ...]: the named fixtures, or all of them."""
     if not R.available():
         sys.exit("oracle/_ref/libref2d.so missing: run `make -C oracle/ref` where the reference sources are present")
-    make_case("bubbles_17", bubbles_case(17, seed=1), 0.5 / 16, 1e-13)
-    make_case("bubbles_33", bubbles_case(33, seed=2), 0.5 / 32, 1e-13)
-    make_case("rising_bubble_40x24", rising_bubble_case(40, 24, seed=3), 0.01, 1e-13)
-    make_case("tall_24x40", bubbles_case(24, 40, seed=4, x_max=1.0, y_max=2.0), 0.02, 1e-13)
-    make_case("bubbles_65", bubbles_case(65, seed=5), 0.5 / 64, 1e-12, flow=False)
-    make_rising_bubble_run("rising_bubble_128_frames")
-    make_poisson_test("poisson_test3_61", 3, 61)
-    make_poisson_test("poisson_test5_61", 5, 61)
+    for name in sys.argv[1:] or list(FIXTURES):
+        FIXTURES[name]()
 
 
 if __name__ == "__main__":

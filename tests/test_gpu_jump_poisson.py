@@ -1,14 +1,18 @@
 """Known-answer jump-condition Poisson problems of the reference's POISSON_EQUATION_TEST
-(tests 3 and 5 on [-1,1]^2, 61 x 61 nodes, Dirichlet boundaries) through
+(tests 3, 5 and 8 on [-1,1]^2, 61 x 61 nodes, Dirichlet boundaries) through
 gb2d_jump_poisson_solve: normals bit-exact, the solution against the reference's own,
-and the discretisation error against the exact solutions equal to the reference's."""
+and, for tests 3 and 5, the discretisation error against the exact solutions equal to
+the reference's.  Test 8 (a five-petal interface r = 0.5 + 0.2 sin 5 theta, coefficient
+1 inside and 0.1 outside, both jumps; POISSON_EQUATION_TEST.h:441-456, 566-583, 635-652)
+states no exact solution the test checks (the reference reports an error for tests 0
+and 3 only, :296-306): it is pinned on the reference's own solution."""
 import numpy as np
 import pytest
 
 from conftest import load_golden
 
 pytestmark = pytest.mark.gpu
-NAMES = ["poisson_test3_61", "poisson_test5_61"]
+NAMES = ["poisson_test3_61", "poisson_test5_61", "poisson_test8_61"]
 
 
 def rel_l2(a, b):
@@ -48,6 +52,8 @@ def test_fp64_matches_reference(gb, name):
     np.testing.assert_array_equal(nx[1:-1, 1:-1], g["normal_x"][1:-1, 1:-1])
     np.testing.assert_array_equal(ny[1:-1, 1:-1], g["normal_y"][1:-1, 1:-1])
     assert rel_l2(sol, g["solution"]) <= 1e-10
+    if int(g["test_number"]) == 8:
+        return
     # the known answer: the same discretisation error as the reference's solution
     e_ref, e = l2_error(g, g["solution"]), l2_error(g, sol)
     assert abs(e - e_ref) <= 1e-6 * e_ref

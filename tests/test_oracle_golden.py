@@ -176,7 +176,7 @@ def test_rising_bubble_frames(oracle):
         np.testing.assert_array_equal(got, g[key])
 
 
-@pytest.mark.parametrize("name", ["poisson_test3_61", "poisson_test5_61"])
+@pytest.mark.parametrize("name", ["poisson_test3_61", "poisson_test5_61", "poisson_test8_61"])
 def test_jump_poisson_system(oracle, name):
     """POISSON_EQUATION_TEST's jump problems: the oracle's normals, right-hand side and
     operator equal the reference's system bit for bit; its IC(0)-PCG solution agrees with
