@@ -105,6 +105,9 @@ struct RefSim {
   WORLD_DISCRETIZATION_2D world;
   EULERIAN_FLUID_SOLVER_2D solver;
   SCRIPT_BLOCK block;
+#ifdef REF_GPU
+  ~RefSim() { delete solver.gpu_step; }
+#endif
 };
 
 ARRAY_2D<T>* field(RefSim* s, int id) {
@@ -415,6 +418,39 @@ int ref_poisson_system(void* h, int* n, int* nnz, int* row_ptr, int* col, double
   if (x) for (int k = 0; k < ps.x.num_dimension; ++k) x[k] = ps.x[k];
   return 0;
 }
+#ifdef REF_GPU
+/* The drop-in (built by `make -C oracle/ref gpu` on a copy of EULERIAN_FLUID_SOLVER_2D.h
+ * with the hooks of oracle/ref/patch_gpu_step.py, linked against libgb2d.so): the
+ * solver's GB2D_FLUID_STEP is built from its own grid and script constants, as
+ * INTEGRATION.md shows a maintainer doing at the end of InitializeFromScriptBlock, and
+ * loaded with the solver's current state; from then on AdvanceOneTimeStepThread,
+ * CFLOneTimeStep and the four step members run on the GPU.  ref_gpu_download copies the
+ * device state back into the reference's arrays. */
+int ref_enable_gpu(void* h, int mixed, double tolerance) {
+  RefSim* s = static_cast<RefSim*>(h);
+  EULERIAN_FLUID_SOLVER_2D& f = s->solver;
+  const GRID_STRUCTURE_2D& g = f.base_grid;
+  const int prec = mixed ? GB2D_PRECISION_MIXED : GB2D_PRECISION_FP64;
+  gb2d_grid gg = {g.i_res, g.j_res, g.x_min, g.y_min, g.x_max, g.y_max};
+  gb2d_params p = {f.water_density, f.air_density, f.surface_tension, f.advecting_field_variables->epsilon,
+                   f.iteration_number_for_reinitialization, f.scaling_number_for_reinitialization, prec};
+  gb2d_solve_opts o = {GB2D_SOLVER_MGPCG, prec, tolerance, 100000, 2};
+  delete f.gpu_step;
+  f.gpu_step = new GB2D_FLUID_STEP(gg, p, o, [s](int tid) { s->mt.Sync(tid); });
+  gb2d_flow_params fl = {f.water_viscosity, f.air_viscosity, f.gravity.x, f.gravity.y, f.cfl_number,
+                         f.viscosity_solver->use_delta_function_formulation ? 1 : 0};
+  f.gpu_step->SetFlowParams(fl);
+  for (int id = 0; id <= 5; ++id) f.gpu_step->Upload(id, field(s, id)->values);
+  return 0;
+}
+int ref_gpu_download(void* h) {
+  RefSim* s = static_cast<RefSim*>(h);
+  if (!s->solver.gpu_step) return -1;
+  for (int id = 0; id <= 5; ++id) s->solver.gpu_step->Download(id, field(s, id)->values);
+  return 0;
+}
+#endif
+
 int ref_pcg_info(void* h, int* iterations, double* residual) {
   LINEAR_SOLVER* ls = static_cast<RefSim*>(h)->solver.water_projection->poisson_solver.linear_solver;
   *iterations = ls->num_iteration;

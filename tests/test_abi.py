@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from conftest import ROOT
 
 
@@ -91,3 +93,28 @@ def test_create_rejects_non_positive_densities(gb):
         p = gb.ParamsT(water, air, 0.07, 1e-6, 25, 5, 0)
         assert lib.gb2d_create(ctypes.byref(g), ctypes.byref(p), ctypes.byref(h)) == -1, (water, air)
         assert not h.value
+
+
+def test_reference_solver_links_with_the_dropin(gb):
+    """The drop-in in the reference's own solver class: oracle/ref/patch_gpu_step.py applies
+    the member hooks INTEGRATION.md describes to a copy of EULERIAN_FLUID_SOLVER_2D.h, and the
+    headless reference build links that class against libgb2d.so with no undefined symbol.
+    Runs where the reference sources are (it needs them to build); calling it needs a GPU
+    and those sources together, which no machine of this project has."""
+    import shutil
+    import subprocess
+    ref = os.environ.get("REFERENCE", "/root/reference")
+    if not os.path.exists(os.path.join(ref, "EULERIAN_FLUID_SOLVER_2D.h")) or shutil.which("make") is None:
+        pytest.skip("reference sources not present")
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "gpu", f"REFERENCE={ref}"], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    so = os.path.join(ROOT, "oracle", "_ref", "libref2d_gpu.so")
+    lib = ctypes.CDLL(so)
+    for name in ("ref_create", "ref_enable_gpu", "ref_gpu_download", "ref_step", "ref_cfl_dt"):
+        assert hasattr(lib, name), name
+    nm = subprocess.run(["nm", "-D", "--undefined-only", so], capture_output=True, text=True).stdout
+    for name in ("gb2d_create", "gb2d_advance_time_step", "gb2d_cfl_time_step", "gb2d_projection", "gb2d_levelset_advection"):
+        assert name in nm, name
+    patched = open(os.path.join(ROOT, "oracle", "_ref", "patched", "EULERIAN_FLUID_SOLVER_2D.h")).read()
+    assert patched.count("if (gpu_step)") == 6
