@@ -109,6 +109,8 @@ def library():
         "gb2d_batch_context": [vp, i, ctypes.POINTER(vp)],
         "gb2d_batch_autotune": [vp, d, O, vp],
         "gb2d_batch_advance": [vp, i, d, vp, O, ctypes.POINTER(BatchStatsT)],
+        "gb2d_batch_run_graph": [vp, i, d, vp, O, ctypes.POINTER(BatchStatsT)],
+        "gb2d_batch_schedule": [vp, i, ctypes.POINTER(i), ctypes.POINTER(i)],
         "gb2d_jump_poisson_solve": [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, O, S],
         "gb2d_projection_density_gradient": [vp, d, ctypes.POINTER(d), ctypes.POINTER(d)],
         "gb2d_projection_phi_gradient": [vp, d, vp],
@@ -121,6 +123,7 @@ def library():
         "gb2d_poisson_apply": [vp, vp, vp],
         "gb2d_poisson_solve": [vp, vp, vp, O, S],
         "gb2d_set_stream": [vp, vp],
+        "gb2d_set_tile_plan": [vp, i],
         "gb2d_probe_enable": [vp, i],
         "gb2d_probe_read": [vp, ctypes.POINTER(i), ctypes.POINTER(d), ctypes.POINTER(d)],
         "gb2d_kernel_launches": [ctypes.POINTER(ctypes.c_ulonglong)],
@@ -234,6 +237,10 @@ class Context:
     def set_stream(self, stream_handle):
         """Use a caller's CUDA stream (integer cudaStream_t, e.g. torch.cuda.Stream().cuda_stream); None = own."""
         self._check(self.L.gb2d_set_stream(self.h, ctypes.c_void_p(stream_handle) if stream_handle else None))
+
+    def set_tile_plan(self, plan):
+        """Tile shape of the solver's smoothing levels: -1 the per-level rule, 0-3 one shape for all."""
+        self._check(self.L.gb2d_set_tile_plan(self.h, plan))
 
     def device_ptr(self, field):
         p = ctypes.c_void_p()
@@ -552,6 +559,22 @@ class Batch:
         if rc != 0 and not (allow_max_iters and rc == -4):
             self._check(rc)
         return dts, st
+
+    def run_graph(self, frames, cfl=1.0, dts=None, opts=None, allow_max_iters=False):
+        """advance() as one graph launch (gb2d_batch_run_graph)."""
+        opts = opts or solve_opts(precision=PRECISION_MIXED)
+        dts = np.zeros(self.n) if dts is None else np.ascontiguousarray(dts, dtype=np.float64)
+        st = BatchStatsT()
+        rc = self.L.gb2d_batch_run_graph(self.h, frames, cfl, _ptr(dts), ctypes.byref(opts), ctypes.byref(st))
+        if rc != 0 and not (allow_max_iters and rc == -4):
+            self._check(rc)
+        return dts, st
+
+    def schedule(self, k):
+        """(sweeps, tile plan) of instance k (gb2d_batch_schedule)."""
+        sw, tp = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.gb2d_batch_schedule(self.h, k, ctypes.byref(sw), ctypes.byref(tp)))
+        return sw.value, tp.value
 
     def close(self):
         if getattr(self, "h", None):

@@ -147,6 +147,7 @@ void free_ctx(gb2d_ctx* c) {
   if (c->ev_join2) cudaEventDestroy(c->ev_join2);
   if (c->ev_pre0) cudaEventDestroy(c->ev_pre0);
   if (c->xfer) cudaStreamDestroy(c->xfer);
+  if (c->body_stream) cudaStreamDestroy(c->body_stream);
   if (c->ev_xfer0) cudaEventDestroy(c->ev_xfer0);
   if (c->ev_xfer) cudaEventDestroy(c->ev_xfer);
   delete c;
@@ -200,6 +201,7 @@ int gb2d_create(const gb2d_grid* grid, const gb2d_params* params, gb2d_ctx** out
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_pre0, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->body_stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_xfer0, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_xfer, cudaEventDisableTiming);
   struct A {
@@ -284,6 +286,14 @@ int gb2d_set_stream(gb2d_ctx* c, void* stream) {
   int rc = sync_check(c, "set_stream");
   if (rc) return rc;
   c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return GB2D_OK;
+}
+
+int gb2d_set_tile_plan(gb2d_ctx* c, int plan) {
+  if (!c || plan > 3) return GB2D_ERR_ARG;
+  int rc = sync_check(c, "set_tile_plan");
+  if (rc) return rc;
+  solver_set_tile_plan(c, plan);
   return GB2D_OK;
 }
 
@@ -479,9 +489,11 @@ int gb2d_velocity_advection(gb2d_ctx* c, double dt) {
   return check_launch(c, "velocity_advection");
 }
 
+// Detections (c->sc->flag) clear at every host-driven call; a device-driven run keeps
+// them for the whole run, which reads them at its end.
 static int curvature_impl(gb2d_ctx* c) {
   double* phi = c->phi_buf[c->phi_cur];
-  GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->flag, 0, sizeof(int), c->stream));
+  if (!c->graph_mode) GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->flag, 0, sizeof(int), c->stream));
   launch_extrapolate_ghosts(c->stream, phi, 2, c->grid.ni, c->grid.nj);
   launch_curvature(c->stream, c, phi, c->kappa, &c->sc->flag);
   return check_launch(c, "curvature");
@@ -512,7 +524,7 @@ int gb2d_curvature(gb2d_ctx* c) {
 // them on a third stream, and the right-hand side follows the curvature.
 static int curvature_and_assemble(gb2d_ctx* c, double dt, const gb2d_solve_opts* prebuild, cudaEvent_t inputs = nullptr) {
   double* phi = c->phi_buf[c->phi_cur];
-  GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->flag, 0, sizeof(int), c->stream));
+  if (!c->graph_mode) GB2D_CUDA_TRY(c, cudaMemsetAsync(&c->sc->flag, 0, sizeof(int), c->stream));
   launch_extrapolate_ghosts(c->stream, phi, 2, c->grid.ni, c->grid.nj);
   GB2D_CUDA_TRY(c, cudaEventRecord(c->ev_fork, c->stream));
   GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->side, c->ev_fork, 0));
@@ -588,6 +600,7 @@ static int projection_run(gb2d_ctx* c, double dt, const gb2d_solve_opts* o, gb2d
   if (io && io->v_out)
     GB2D_CUDA_TRY(c, cudaMemcpyAsync(io->v_out, c->v, field_bytes(c, GB2D_FIELD_V), cudaMemcpyDeviceToHost, c->stream));
   if (p_out) GB2D_CUDA_TRY(c, cudaStreamWaitEvent(c->stream, c->ev_xfer, 0));
+  if (c->graph_mode) return check_launch(c, "projection");
   if ((rc = read_flag(c))) return rc;
   const Scalars* h = (const Scalars*)c->host_stage;
   double mu, mv;
@@ -713,6 +726,56 @@ int gb2d_advance_frame(gb2d_ctx* c, double cfl, double* dt, const gb2d_solve_opt
   *dt = d;
   return gb2d_advance_time_step(c, d, o, st);
 }
+
+}  // extern "C"
+
+namespace gb2d {
+
+// One gb2d_advance_frame captured on c->stream for the device (gb2d_batch_run_graph):
+// the curvature, the CFL time step formed on the device (launch_frame_dt), and the order-3
+// time step with every kernel reading that step (c->dt_dev) and every solve looping on the
+// device (c->graph_mode); nothing is read back.  The buffers a frame rotates (the four
+// level-set buffers, U/V and their alternates) are copied back to where the frame found
+// them, so that the captured frame can run again.
+int frame_capture(gb2d_ctx* c, double cfl, const gb2d_solve_opts* o) {
+  const int phi0 = c->phi_cur;
+  double *u0 = c->u, *v0 = c->v;
+  c->graph_mode = 1;
+  c->dt_dev = &c->sc->dt_frame;
+  int rc = curvature_impl(c);
+  if (rc == GB2D_OK) {
+    launch_cfl(c->stream, c);
+    launch_frame_dt(c->stream, c, cfl);
+    rc = check_launch(c, "frame time step");
+  }
+  if (rc == GB2D_OK) rc = gb2d_advance_time_step(c, 1.0 /* read on the device */, o, nullptr);
+  if (rc == GB2D_OK) {
+    const size_t ni = c->grid.ni, nj = c->grid.nj;
+    const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+    if (c->phi_cur != phi0) {
+      GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->phi_buf[phi0], c->phi_buf[c->phi_cur], (ni + 4) * (nj + 4) * sizeof(double), d2d, c->stream));
+      c->phi_cur = phi0;
+    }
+    if (c->u != u0) {
+      GB2D_CUDA_TRY(c, cudaMemcpyAsync(u0, c->u, (ni + 5) * (nj + 4) * sizeof(double), d2d, c->stream));
+      c->u_alt = c->u;
+      c->u = u0;
+    }
+    if (c->v != v0) {
+      GB2D_CUDA_TRY(c, cudaMemcpyAsync(v0, c->v, (ni + 4) * (nj + 5) * sizeof(double), d2d, c->stream));
+      c->v_alt = c->v;
+      c->v = v0;
+    }
+    rc = check_launch(c, "frame");
+  }
+  c->graph_mode = 0;
+  c->dt_dev = nullptr;
+  return rc;
+}
+
+}  // namespace gb2d
+
+extern "C" {
 
 int gb2d_weno5_adjoint(gb2d_ctx* c, double dt, const double* lam_phi, double* mu_phi, double* mu_ua, double* mu_va) {
   if (!c || !lam_phi || !mu_phi || !std::isfinite(dt)) return GB2D_ERR_ARG;

@@ -98,8 +98,9 @@ struct LSArgs {
 // ghosts to the caller's extrapolation).
 template <bool MIXED>
 __global__ void k_weno5_advect(const double* __restrict__ src_a, double* __restrict__ dst_a, const double* __restrict__ ua_a,
-                               const double* __restrict__ va_a, LSArgs a, double dt) {
+                               const double* __restrict__ va_a, LSArgs a, DtArg dt_arg) {
   int ni = a.ni, nj = a.nj;
+  const double dt = dt_arg.get();
   int W = ni + 4, H = nj + 4;
   int ix = blockIdx.x * blockDim.x + threadIdx.x, jy = blockIdx.y * blockDim.y + threadIdx.y;
   if (ix >= W || jy >= H) return;
@@ -258,8 +259,9 @@ struct EnoArgs {
 // face velocities and the update in FP64).
 template <bool MIXED>
 __global__ void k_eno3(double* __restrict__ u_a, double* __restrict__ v_a, const double* __restrict__ ua_a, const double* __restrict__ va_a,
-                       EnoArgs a, double dt) {
+                       EnoArgs a, DtArg dt_arg) {
   int ni = a.ni, nj = a.nj;
+  const double dt = dt_arg.get();
   DField ua = dfield((double*)ua_a, 3, ni + 1, nj), va = dfield((double*)va_a, 3, ni, nj + 1);
   auto face = [&](bool xc, int i, int j) {
     const DField& g = xc ? ua : va;
@@ -347,6 +349,7 @@ struct AsmArgs {
   Space s;
   double water, air, sigma, one_over_dt, inv_dxdx, inv_dydy;
   double inv_water, inv_air;  // 1/water, 1/air: IEEE quotients taken once on the host
+  const double* dtp;          // non-null: the time step is read here (one_over_dt = 1 / *dtp, IEEE)
   double oeh, oev;            // 1 / (1.5 dx), 1 / (1.5 dy): smeared-Heaviside scales
 };
 
@@ -437,6 +440,7 @@ __global__ void k_rhs(const double* __restrict__ phi_a, const double* __restrict
                       const double* __restrict__ v_a, const double* __restrict__ bx, const double* __restrict__ by, double* __restrict__ rhs,
                       AsmArgs a) {
   int ni = a.ni, nj = a.nj;
+  const double one_over_dt = a.dtp ? 1.0 / *a.dtp : a.one_over_dt;
   DField phi = dfield((double*)phi_a, 2, ni, nj);
   DField u = dfield((double*)u_a, 2, ni + 1, nj), v = dfield((double*)v_a, 2, ni, nj + 1);
   GB_FOR_IJ(i, j, ni, nj) {
@@ -450,7 +454,7 @@ __global__ void k_rhs(const double* __restrict__ phi_a, const double* __restrict
     double FB = arm_flux(pc, GB_AT(phi, i, j - 1), jcc, kappa, i, j - 1, bb, a.s.ody2, a);
     double FT = arm_flux(pc, GB_AT(phi, i, j + 1), jcc, kappa, i, j + 1, bt, a.s.ody2, a);
     double div = a.s.odx * (GB_AT(u, i + 1, j) - GB_AT(u, i, j)) + a.s.ody * (GB_AT(v, i, j + 1) - GB_AT(v, i, j));
-    div *= a.one_over_dt;
+    div *= one_over_dt;
     double FX = FL + FR, FY = FB + FT;
     rhs[t] = -div - FX - FY;
   }
@@ -476,8 +480,9 @@ __global__ void k_apply_exact(const double* __restrict__ bx, const double* __res
 // smeared-Heaviside density of the face-averaged phi (eps = 1.5 dx) and the
 // |phi|-weighted jump.  Pressure ghosts are zero; wall faces (bc < 0) are skipped.
 __global__ void k_velocity_update(const double* __restrict__ phi_a, const double* __restrict__ p_a, const double* __restrict__ kappa,
-                                  double* __restrict__ u_a, double* __restrict__ v_a, AsmArgs a, double dt, Scalars* sc) {
+                                  double* __restrict__ u_a, double* __restrict__ v_a, AsmArgs a, DtArg dt_arg, Scalars* sc) {
   int ni = a.ni, nj = a.nj;
+  const double dt = dt_arg.get();
   DField phi = dfield((double*)phi_a, 2, ni, nj), p = dfield((double*)p_a, 1, ni, nj);
   DField u = dfield(u_a, 2, ni + 1, nj), v = dfield(v_a, 2, ni, nj + 1);
   const double odx = a.s.odx, ody = a.s.ody;  // 1 / dx, 1 / dy, taken on the host
@@ -597,6 +602,7 @@ AsmArgs asm_args(const gb2d_ctx* c, double dt) {
   a.air = c->prm.air_density;
   a.sigma = c->prm.surface_tension;
   a.one_over_dt = 1.0 / dt;
+  a.dtp = c->dt_dev;
   a.inv_dxdx = 1.0 / (c->base.dx * c->base.dx);
   a.inv_dydy = 1.0 / (c->base.dy * c->base.dy);
   a.inv_water = 1.0 / a.water;
@@ -664,9 +670,9 @@ void launch_weno5_advect(cudaStream_t s, const gb2d_ctx* c, const double* src, d
   dim3 blk(32, 8);
   dim3 grd = grid2d(c->grid.ni + 4, c->grid.nj + 4, blk);
   if (mixed)
-    k_weno5_advect<true><<<grd, blk, 0, s>>>(src, dst, c->ua, c->va, ls_args(c), dt);
+    k_weno5_advect<true><<<grd, blk, 0, s>>>(src, dst, c->ua, c->va, ls_args(c), DtArg{dt, c->dt_dev});
   else
-    k_weno5_advect<false><<<grd, blk, 0, s>>>(src, dst, c->ua, c->va, ls_args(c), dt);
+    k_weno5_advect<false><<<grd, blk, 0, s>>>(src, dst, c->ua, c->va, ls_args(c), DtArg{dt, c->dt_dev});
   GB_LAUNCHED(1);
 }
 
@@ -714,9 +720,9 @@ void launch_eno3(cudaStream_t s, const gb2d_ctx* c, double dt) {
     a.o3[g][1] = q.ody / 3;
   }
   if (c->prm.advection_precision == GB2D_PRECISION_MIXED)
-    k_eno3<true><<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, dt);
+    k_eno3<true><<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, DtArg{dt, c->dt_dev});
   else
-    k_eno3<false><<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, dt);
+    k_eno3<false><<<grid_ij(c->grid.ni + 1, c->grid.nj + 1), kThreads, 0, s>>>(c->u, c->v, c->ua, c->va, a, DtArg{dt, c->dt_dev});
   GB_LAUNCHED(1);
 }
 
@@ -753,7 +759,7 @@ void launch_poisson_apply_exact(cudaStream_t s, const gb2d_ctx* c, const double*
 
 void launch_velocity_update(cudaStream_t s, const gb2d_ctx* c, const double* phi, double dt, Scalars* sc) {
   AsmArgs a = asm_args(c, dt);
-  k_velocity_update<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, c->p, c->kappa, c->u, c->v, a, dt, sc);
+  k_velocity_update<<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(phi, c->p, c->kappa, c->u, c->v, a, DtArg{dt, c->dt_dev}, sc);
   GB_LAUNCHED(1);
 }
 

@@ -40,6 +40,10 @@ struct FlowArgs {
   Smear rho, mu;       // face density and viscosity
   double coef0, coef1; // dt * (1 / rho.at0), dt * (1 / rho.at1)
   double air, water;   // node densities of DetermineDensity
+  // Non-null: the time step is read here when the kernel runs, and the dt-derived fields
+  // above are formed from it as the host forms them (g_x, g_y: gravity; inv_rho0/1 = 1 / rho.at0/1).
+  const double* dtp;
+  double g_x, g_y, inv_rho0, inv_rho1;
   // FP32 viscous-flux path
   float odx_f, ody_f, eps_f, oe_f, dt_f, coef0_f, coef1_f;
   SmearF rho_f, mu_f;
@@ -75,6 +79,18 @@ __device__ __forceinline__ float face_coef_f(float l, const FlowArgs& a) {
   return __fdividef(a.dt_f, a.rho_f.lo + a.rho_f.d * heaviside_band_f(l, a.oe_f));
 }
 
+// The dt-dependent fields of FlowArgs, as launch_flow forms them on the host.
+__host__ __device__ __forceinline__ void with_time_step(FlowArgs& a, double dt) {
+  a.gx = dt * a.g_x;
+  a.gy = dt * a.g_y;
+  a.dt = dt;
+  a.coef0 = dt * a.inv_rho0;
+  a.coef1 = dt * a.inv_rho1;
+  a.dt_f = (float)dt;
+  a.coef0_f = (float)a.coef0;
+  a.coef1_f = (float)a.coef1;
+}
+
 // One pass over the (ni+1) x (nj+1) face index space: x-face (i, j), i <= ni,
 // j < nj; y-face (i, j), i < ni, j <= nj; node (i, j) for the density.
 //   VISC = false: gravity and wall conditions in place (u_out may equal u_in).
@@ -88,6 +104,7 @@ __device__ __forceinline__ float face_coef_f(float l, const FlowArgs& a) {
 template <bool VISC, bool MIXED>
 __global__ void k_flow(const double* __restrict__ phi_a, const double* u_in_a, const double* v_in_a, double* u_out_a,
                        double* v_out_a, double* __restrict__ dens_a, FlowArgs a) {
+  if (a.dtp) with_time_step(a, *a.dtp);
   const int ni = a.ni, nj = a.nj;
   const DField phi = dfield((double*)phi_a, 2, ni, nj);
   const DField ui = dfield((double*)u_in_a, 2, ni + 1, nj), vi = dfield((double*)v_in_a, 2, ni, nj + 1);
@@ -253,7 +270,20 @@ __global__ void k_cfl_final(CflArgs a, Scalars* sc) {
   sc->cfl[4] = s_f;
 }
 
+// The frame's time step: DetermineTimeStep keeps the previous step when the CFL rate is
+// zero (SIMULATION_WORLD.h:1201-1204), then the frame's CFL factor.
+__global__ void k_frame_dt(Scalars* sc, double cfl) {
+  double d = sc->cfl[0];
+  if (d == 0) d = sc->dt_frame;
+  sc->dt_frame = d * cfl;
+}
+
 }  // namespace
+
+void launch_frame_dt(cudaStream_t s, gb2d_ctx* c, double cfl) {
+  k_frame_dt<<<1, 1, 0, s>>>(c->sc, cfl);
+  GB_LAUNCHED(1);
+}
 
 void launch_cfl(cudaStream_t s, gb2d_ctx* c) {
   const int ni = c->grid.ni, nj = c->grid.nj;
@@ -284,26 +314,24 @@ void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int
   a.nj = nj;
   a.grav = grav;
   a.bc = bc;
-  a.gx = dt * c->flow.gravity_x;
-  a.gy = dt * c->flow.gravity_y;
-  a.dt = dt;
+  a.g_x = c->flow.gravity_x;
+  a.g_y = c->flow.gravity_y;
   a.odx = c->base.odx;
   a.ody = c->base.ody;
   a.eps = 1.5 * c->base.dx;
   a.oe = 1.0 / a.eps;
   a.rho = make_smear(c->prm.air_density, c->prm.water_density);
   a.mu = make_smear(c->flow.air_viscosity, c->flow.water_viscosity);
-  a.coef0 = dt * (1 / a.rho.at0);
-  a.coef1 = dt * (1 / a.rho.at1);
+  a.inv_rho0 = 1 / a.rho.at0;
+  a.inv_rho1 = 1 / a.rho.at1;
+  a.dtp = c->dt_dev;
+  with_time_step(a, dt);
   a.air = c->prm.air_density;
   a.water = c->prm.water_density;
   a.odx_f = (float)a.odx;
   a.ody_f = (float)a.ody;
   a.eps_f = (float)a.eps;
   a.oe_f = (float)a.oe;
-  a.dt_f = (float)dt;
-  a.coef0_f = (float)a.coef0;
-  a.coef1_f = (float)a.coef1;
   a.rho_f = SmearF{(float)a.rho.lo, (float)a.rho.d, (float)a.rho.at0, (float)a.rho.at1};
   a.mu_f = SmearF{(float)a.mu.lo, (float)a.mu.d, (float)a.mu.at0, (float)a.mu.at1};
   const double* phi = c->phi_buf[c->phi_cur];

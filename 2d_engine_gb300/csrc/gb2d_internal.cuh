@@ -111,6 +111,22 @@ struct Scalars {
   unsigned long long maxu_bits, maxv_bits;  // max |u|, |v| of the velocity update
   unsigned long long cfl_bits[3];           // max |u|, |v|, |kappa| for the CFL time step
   double cfl[5];                            // CFL dt, c_f, g_f, v_f, s_f
+  // Frames run on the device (gb2d_batch_run_graph): the time step of the running frame,
+  // which the kernels read in place of a host value, and the instance's totals.
+  double dt_frame;
+  double g_rr, g_bb;               // true ||r||^2 and ||b||^2 of the latest solve
+  double g_rel2_max;               // largest ||r||^2 / ||b||^2 at the end of a solve
+  unsigned long long g_iters;      // CG iterations of every solve
+  int g_frames;                    // frames of the current run so far
+  int g_capped;                    // a solve stopped at its iteration cap
+};
+
+// A time step given by value, or (p non-null) read on the device when the kernel runs: the
+// frame's CFL step computed on the GPU.
+struct DtArg {
+  double v;
+  const double* p;
+  __device__ __forceinline__ double get() const { return p ? *p : v; }
 };
 
 struct Solver;  // defined in gb2d_solver.cu
@@ -145,6 +161,11 @@ struct gb2d_ctx {
   cudaEvent_t ev_fork2, ev_join2, ev_pre0;  // ev_pre0: the FP64 finest level is built
   int device_loop;                // run each CG solve as one graph launch (a device-side WHILE loop)
   int asm_reuse;                  // the next projection keeps the phi-dependent assembly and solver levels
+  // While a device-driven frame is captured (gb2d_batch_run_graph): the kernels take the time
+  // step from dt_dev, nothing reads back to the host, and each solve loops on the device.
+  const double* dt_dev;
+  int graph_mode;
+  cudaStream_t body_stream;       // captures the bodies of the device loops (created on first use)
   cudaStream_t xfer;              // host copies that overlap the projection (gb2d_projection_host)
   cudaEvent_t ev_xfer0, ev_xfer;
   gb2d::Probe probe;
@@ -209,6 +230,13 @@ void launch_flow(cudaStream_t s, gb2d_ctx* c, double dt, int grav, int visc, int
 void launch_face_blend(cudaStream_t s, gb2d_ctx* c, double c0, double c1);
 // CFLOneTimeStep into c->sc->cfl (dt, c_f, g_f, v_f, s_f).
 void launch_cfl(cudaStream_t s, gb2d_ctx* c);
+// The frame's time step on the device, as gb2d_advance_frame forms it on the host:
+// c->sc->dt_frame = (CFL step, or the previous dt_frame when that is zero) * cfl.
+void launch_frame_dt(cudaStream_t s, gb2d_ctx* c, double cfl);
+
+// ---- gb2d_api.cu ----
+// One gb2d_advance_frame captured on c->stream for the device (no host reads; see gb2d_api.cu).
+int frame_capture(gb2d_ctx* c, double cfl, const gb2d_solve_opts* o);
 
 // ---- gb2d_adjoint.cu ----
 int adjoint_buffers(gb2d_ctx* c);
@@ -254,6 +282,10 @@ void solver_drop_prebuild(gb2d_ctx* c);
 // ctx->bx/by/diag) and refreshes only the right-hand side.
 void solver_keep_levels(gb2d_ctx* c);
 void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, int* cluster_ctas);
+// Tile shapes of the smoothing levels: < 0 the default per-level rule, 0-3 one shape for all.
+void solver_set_tile_plan(gb2d_ctx* c, int plan);
+// Kernels of one CG iteration in the loop body of the latest device-driven solve capture.
+unsigned long long solver_body_nodes(const gb2d_ctx* c);
 // One multigrid V-cycle (nu sweeps per side, FP32 levels when prec) of the assembled
 // system in ctx->bx/by/diag applied to r: z = M r (device, compact ni x nj FP64).
 int solver_precondition(gb2d_ctx* c, int prec, int nu, const double* r_dev, double* z_dev);

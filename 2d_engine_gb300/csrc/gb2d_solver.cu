@@ -887,6 +887,47 @@ __global__ void k_loop_cond(cudaGraphConditionalHandle h, Scalars* sc, const int
   cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+// Start of one pass of a solve inside a device-driven frame: the pass's threshold and
+// done flag from the true residual and ||b||^2 in the frame scalars fs (g_rr, g_bb), as
+// solver_solve's host loop decides them (a non-finite norm marks fs->flag bit 4 and ends
+// the solve), the pass's iteration cap (what the solve's earlier passes left of max_it),
+// and the WHILE node's condition.  first: the solve's first pass.
+__global__ void k_begin_device(cudaGraphConditionalHandle h, Scalars* sc, int* done, Scalars* fs, double tol2, int max_it, int first) {
+  const double rr = fs->g_rr, bb = fs->g_bb;
+  if (first) fs->iters = 0;  // the frame scalars' iters count this solve's iterations
+  const double thr2 = tol2 * bb;
+  int d = 0;
+  if (!isfinite(rr) || !isfinite(bb)) {
+    d = 1;
+    fs->flag |= 4;
+  } else if (rr <= thr2 || bb == 0.0) {
+    d = 1;
+  }
+  const int cap = max_it - fs->iters;
+  if (cap <= 0) d = 1;
+  *done = d;
+  sc->thr2 = thr2;
+  sc->rz_cur = 1.0;
+  sc->iters = 0;
+  sc->max_it = cap;
+  cudaGraphSetConditional(h, d ? 0u : 1u);
+}
+
+// End of a pass (after the true residual is in fs->g_rr / g_bb): the pass's iterations join
+// the solve's and the instance's totals, a non-finite ||r||^2 of the CG marks fs->flag.
+// last: the solve's last pass, whose residual is the solve's result.
+__global__ void k_end_device(const Scalars* sc, Scalars* fs, int last) {
+  fs->iters += sc->iters;
+  fs->g_iters += (unsigned long long)sc->iters;
+  if (sc->flag & 1) fs->flag |= 4;
+  if (!last) return;
+  const double rr = fs->g_rr, bb = fs->g_bb;
+  if (!isfinite(rr) || !isfinite(bb)) fs->flag |= 4;
+  const double rel2 = bb > 0 ? rr / bb : 0.0;
+  if (rel2 > fs->g_rel2_max) fs->g_rel2_max = rel2;
+  if (!(rr <= sc->thr2) && bb != 0.0) fs->g_capped = 1;
+}
+
 }  // namespace
 
 // ---- host side -------------------------------------------------------------------
@@ -934,6 +975,7 @@ struct Solver {
   // Graphs per (precision, solver, smoothing sweeps) and the x they update.
   GraphSet graphs[2][2][3];
   double* graph_x[2][2][3] = {};
+  unsigned long long body_nodes = 0;  // kernels of one CG iteration in a device-driven frame's loop body
 };
 
 // Block-partial slots (nparts_cap doubles each).
@@ -1764,6 +1806,25 @@ void solver_layout(const Solver* S, int mixed, int* levels, int* cluster_top, in
   }
 }
 
+// Tile shapes of the tiled smoothing levels: plan < 0 restores the default rule
+// (plan_shapes), 0-3 give every tiled level that shape (64x16, 32x16, 32x8, 32x32).  The
+// cached CG graphs hold the old launches and are captured again on their next use.
+void solver_set_tile_plan(gb2d_ctx* c, int plan) {
+  Solver* S = c->solver;
+  if (!S) return;
+  int dev = 0, nsm = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  plan_shapes(S->h64, nsm);
+  plan_shapes(S->h32, nsm);
+  if (plan >= 0 && plan < kTileShapes)
+    for (int l = 0; l < kMaxLevels; ++l) S->h64.shape[l] = S->h32.shape[l] = plan;
+  for (auto& a : S->graphs)
+    for (auto& b : a)
+      for (auto& g : b) g.ok = false;
+}
+
+unsigned long long solver_body_nodes(const gb2d_ctx* c) { return c->solver ? c->solver->body_nodes : 0; }
+
 namespace {
 // Padded level layout <- compact FP64 host-order array (the preconditioner's input r,
 // narrowed as the solver narrows its FP32 copy of r).
@@ -1841,6 +1902,96 @@ void solver_drop_prebuild(gb2d_ctx* c) {
   S->prebuilt = false;
 }
 
+// Append to the capture running on s a WHILE node whose body (captured on body) is one CG
+// iteration followed by k_loop_cond, with the handle h (created on the capturing graph).
+template <typename T>
+bool append_cg_loop(cudaStream_t s, cudaStream_t body, cudaGraphConditionalHandle h, Solver* S, Hierarchy<T>& H, const double* ainv,
+                    double* x64, int use_mg, int nu) {
+  cudaStreamCaptureStatus st;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess || st != cudaStreamCaptureStatusActive) return false;
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp) != cudaSuccess) return false;
+  if (cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess) return false;
+  if (cudaStreamBeginCaptureToGraph(body, cp.conditional.phGraph_out[0], nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+      cudaSuccess)
+    return false;
+  unsigned long long* outer = t_capture_count;  // the body's launches count per iteration, apart
+  unsigned long long nb = 0;
+  t_capture_count = &nb;
+  enqueue_iter<T>(body, S, H, ainv, x64, use_mg, nu, 0, nullptr);
+  pdl_launch(body, dim3(1), dim3(1), 0, k_loop_cond, h, S->sc, (const int*)S->done, S->host + 2);
+  GB_LAUNCHED(1);
+  t_capture_count = outer;
+  S->body_nodes = nb;
+  cudaGraph_t out = nullptr;
+  return cudaStreamEndCapture(body, &out) == cudaSuccess;
+}
+
+// The solve of a device-driven frame (ctx->graph_mode, captured on ctx->stream): the true
+// residual and ||b||^2 into the frame scalars, then two passes of [threshold and done flag
+// on the device, CG init, WHILE over one iteration, true residual] -- the host loop's first
+// pass and the restart it takes when the recursive residual has drifted above the
+// tolerance (a pass whose start is converged runs no iteration).  Nothing is read back.
+template <typename T>
+int solve_on_device(gb2d_ctx* c, Solver* S, Hierarchy<T>& H, const double* ainv, double* x, int use_mg, int nu, double tol,
+                    int max_it, cudaEvent_t join_ev, bool joined) {
+  cudaStream_t s = c->stream;
+  const unsigned G = (unsigned)S->G;
+  double* P_rr = slot(S, kSlotRr);
+  double* P_bb = slot(S, kSlotBb);
+  const bool mixed = sizeof(T) == 4;
+  auto residual = [&]() {
+    if (mixed)
+      k_residual64<float><<<G, kThreads, 0, s>>>(S->h64.L[0], x, S->b64, S->h64.r, S->h32.r, P_rr, P_bb);
+    else
+      k_residual64<double><<<G, kThreads, 0, s>>>(S->h64.L[0], x, S->b64, S->h64.r, nullptr, P_rr, P_bb);
+    k_reduce_two<<<1, kThreads, 0, s>>>(P_rr, P_bb, G, &c->sc->g_rr);
+    GB_LAUNCHED(2);
+  };
+  residual();
+  if (!joined) cudaStreamWaitEvent(s, join_ev, 0);
+  cudaMemsetAsync(&S->sc->flag, 0, sizeof(int), s);
+  for (int pass = 0; pass < 2; ++pass) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamGetCaptureInfo(s, &st, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess || st != cudaStreamCaptureStatusActive) {
+      snprintf(c->err, sizeof(c->err), "device-driven solve: the stream is not capturing");
+      return GB2D_ERR_CUDA;
+    }
+    cudaGraphConditionalHandle h;
+    if (cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) {
+      cudaGetLastError();
+      snprintf(c->err, sizeof(c->err), "device-driven solve: conditional handle refused");
+      return GB2D_ERR_CUDA;
+    }
+    k_begin_device<<<1, 1, 0, s>>>(h, S->sc, S->done, c->sc, tol * tol, max_it, pass == 0);
+    GB_LAUNCHED(1);
+    enqueue_init<T>(s, S, H, ainv, use_mg, nu, nullptr);
+    if (!append_cg_loop<T>(s, c->body_stream, h, S, H, ainv, x, use_mg, nu)) {
+      cudaGetLastError();
+      snprintf(c->err, sizeof(c->err), "device-driven solve: the CG loop node was refused");
+      return GB2D_ERR_CUDA;
+    }
+    residual();
+    k_end_device<<<1, 1, 0, s>>>(S->sc, c->sc, pass == 1);
+    GB_LAUNCHED(1);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(c->err, sizeof(c->err), "device-driven solve: %s", cudaGetErrorString(e));
+    return GB2D_ERR_CUDA;
+  }
+  return GB2D_OK;
+}
+
 // x: padded FP64 solution (warm start in, result out); the system is ctx->bx/by/diag/rhs.
 // FP64 CG throughout; the preconditioner runs in FP64 or, for
 // GB2D_PRECISION_MIXED, in FP32.  The loop around the CG recomputes the true
@@ -1897,6 +2048,11 @@ int solver_solve(gb2d_ctx* c, const double* /*rhs*/, double* x, const gb2d_solve
     k_build_level0<float><<<grid_ij(c->grid.ni, c->grid.nj), kThreads, 0, s>>>(c->bx, c->by, c->diag, c->rhs, c->sys_shift,
                                                                                                 S->h32.L[0], nullptr, idx2, idy2);
     GB_LAUNCHED(1);
+  }
+  if (c->graph_mode) {
+    if (prec)
+      return solve_on_device<float>(c, S, S->h32, S->ainv32, x, use_mg, nu, tol, max_it, join_ev, joined);
+    return solve_on_device<double>(c, S, S->h64, S->ainv64, x, use_mg, nu, tol, max_it, join_ev, joined);
   }
   int total = 0, outer = 0;
   double rr = 0, bb = 0;

@@ -279,16 +279,18 @@ def run_rayleigh_taylor(gb, stream, n=2048, frames=500, every=50):
 
 def run_batch(gb, n, frames, cpu=True, dist=None, rank=0, ws=1):
     """Independent rising bubbles of uneven sizes (64^2 to 512^2) advanced together by the
-    batched runtime (mixed precision, relative residual 1e-8, autotuned V-cycles), with
-    the same instances on one worker thread for comparison and the reference's solver
-    (the oracle) timed on a bounded sample and extrapolated."""
+    batched runtime (mixed precision, relative residual 1e-8, autotuned V-cycle sweeps and
+    tile plans): the whole run as one graph launch (gb2d_batch_run_graph; its capture timed
+    apart), the same frames driven by host worker threads and by one worker for
+    comparison, and the reference's solver (the oracle) timed for one frame of a sampled
+    instance of every size."""
     import numpy as np
     from tests.golden.cases import batched_bubbles
     grids, phis, params, flows = batched_bubbles(n, seed=BATCH_SEED)
     for p in params:
         p["advection_precision"] = gb.PRECISION_MIXED
     mine = shard(n, rank, ws)  # with N ranks each GPU runs every N-th instance
-    all_grids, all_params, all_flows = grids, params, flows
+    all_grids, all_phis, all_params, all_flows = grids, phis, params, flows
     grids, phis, params, flows = ([a[k] for k in mine] for a in (grids, phis, params, flows))
     n_all, n = n, len(mine)
     opts = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=TOL)
@@ -310,36 +312,51 @@ def run_batch(gb, n, frames, cpu=True, dist=None, rank=0, ws=1):
         walls[workers] = wall_ms / f
         if workers == 0:
             cells = sum(g[0] * g[1] for g in all_grids)
-            out.update({"workers": b.workers, "create_s": t1 - t0, "autotune_s": t2 - t1, "wall_ms": wall_ms,
-                        "ms_per_frame_all_instances": wall_ms / f, "instance_frames_per_s": n_all * f / (wall_ms * 1e-3),
-                        "cell_frames_per_s": cells * f / (wall_ms * 1e-3), "cells": cells,
-                        "cg_iterations_per_projection": st.cg_iterations / (3.0 * n * f), "max_rel_residual": st.max_rel_residual,
-                        "mg_smooth_by_size": {str(g[0]): smooth[k] for k, g in enumerate(grids)}})
+            out.update({"workers": b.workers, "create_s": t1 - t0, "autotune_s": t2 - t1,
+                        "host_threads": {"wall_ms": wall_ms, "ms_per_frame_all_instances": wall_ms / f,
+                                         "cg_iterations_per_projection": st.cg_iterations / (3.0 * n * f)},
+                        "cells": cells,
+                        "schedule_by_size": {str(g[0]): dict(zip(("sweeps", "tile_plan"), b.schedule(k)))
+                                             for k, g in enumerate(grids)}})
+            # the same instances continue as one graph launch per run: the first call captures
+            # the graph (timed apart), the second reuses it
+            t3 = time.perf_counter()
+            dts, st = b.run_graph(f, cfl=1.0, dts=dts, opts=opts, allow_max_iters=True)
+            capture_s = time.perf_counter() - t3 - st.wall_ms * 1e-3
+            barrier(dist)
+            dts, st = b.run_graph(f, cfl=1.0, dts=dts, opts=opts, allow_max_iters=True)
+            gwall = max_over_ranks(dist, st.wall_ms)
+            out.update({"graph_capture_s": capture_s, "wall_ms": gwall, "ms_per_frame_all_instances": gwall / f,
+                        "instance_frames_per_s": n_all * f / (gwall * 1e-3), "cell_frames_per_s": cells * f / (gwall * 1e-3),
+                        "cg_iterations_per_projection": st.cg_iterations / (3.0 * n * f),
+                        "max_rel_residual": st.max_rel_residual,
+                        "path": "gb2d_batch_run_graph: one graph launch per run, every instance a WHILE node over its frames"})
         b.close()
     out["one_worker_ms_per_frame_all_instances"] = walls[1]
-    out["speedup_vs_one_worker"] = walls[1] / walls[0]
+    out["graph_speedup_vs_one_worker"] = walls[1] / out["ms_per_frame_all_instances"]
+    out["graph_speedup_vs_host_threads"] = walls[0] / out["ms_per_frame_all_instances"]
     if cpu:
-        out["cpu_reference"] = batch_cpu_estimate(all_grids, all_params, all_flows, frames)
+        out["cpu_reference"] = batch_cpu_estimate(all_grids, all_phis, all_params, all_flows, frames)
     return out
 
 
-def batch_cpu_estimate(grids, params, flows, frames):
+def batch_cpu_estimate(grids, phis, params, flows, frames):
     """The reference's solver (the oracle: IC(0)-PCG to the same relative residual,
-    single-threaded) timed for one frame of a 64^2 and a 128^2 instance of the batch;
-    the per-frame cost is fitted as c N^a and summed over the batch."""
+    single-threaded) timed for one frame of the first instance of every size in the batch
+    (its level set, density and viscosity, from rest); the batch's CPU time is that
+    per-size frame time summed over the batch's instances and frames."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import oracle2d
-    from tests.golden.cases import bubble_level_set
     oracle2d.build()
     ms = {}
-    for N in (64, 128):
+    for N in sorted({g[0] for g in grids}):
         k = next(i for i, g in enumerate(grids) if g[0] == N)
         gr = oracle2d.grid(N, N)
         pr = oracle2d.params(water_density=params[k]["water_density"], air_density=1.0, pcg_tolerance=0.0,
                              pcg_max_iterations=100000, pcg_rel_residual=TOL)
-        fl = oracle2d.flow(water_viscosity=flows[k]["water_viscosity"], air_viscosity=0.01, viscosity=True)
-        phi = bubble_level_set(N, N, 1.0, 0.5, 0.3, 0.15)
+        fl = oracle2d.flow(water_viscosity=flows[k]["water_viscosity"], air_viscosity=flows[k]["air_viscosity"], viscosity=True)
+        phi = phis[k].copy()
         u, v = np.zeros((N + 4, N + 5)), np.zeros((N + 5, N + 4))
         ua, va = np.zeros((N + 6, N + 7)), np.zeros((N + 7, N + 6))
         p, kap = np.zeros((N + 2, N + 2)), np.zeros((N, N))
@@ -348,12 +365,11 @@ def batch_cpu_estimate(grids, params, flows, frames):
         dt, _ = oracle2d.cfl_time_step(gr, pr, fl, u, v, kap, 0.5)
         oracle2d.time_step(gr, pr, fl, phi, u, v, ua, va, p, kap, None, dt)
         ms[N] = (time.perf_counter() - t0) * 1e3
-    a = np.log(ms[128] / ms[64]) / np.log(2.0)
-    total_ms = sum(ms[64] * (g[0] / 64.0) ** a for g in grids) * frames
-    return {"kind": "port", "cores": 1, "ms_per_frame_64": ms[64], "ms_per_frame_128": ms[128], "exponent": a,
+    total_ms = sum(ms[g[0]] for g in grids) * frames
+    return {"kind": "port", "cores": 1, "ms_per_frame_by_size": {str(N): t for N, t in ms.items()},
             "estimated_s_for_batch": total_ms * 1e-3,
-            "sample": "oracle frame (level-set RK3, reinit, 3 SolveForRK with IC(0)-PCG to 1e-8) at 64^2 and 128^2, "
-                      "fitted c N^a and summed over the batch's instances and frames"}
+            "sample": "one oracle frame (level-set RK3, reinit, 3 SolveForRK with IC(0)-PCG to 1e-8) of the first "
+                      "instance of each size, from rest, times the batch's instances of that size and its frames"}
 
 
 def run_reference(args):

@@ -134,6 +134,11 @@ int gb2d_synchronize(gb2d_ctx* ctx);
 /* Run the context's work on a caller-owned CUDA stream (a cudaStream_t passed as
  * void*); NULL returns to the context's own stream. */
 int gb2d_set_stream(gb2d_ctx* ctx, void* stream);
+/* Tile shape of the pressure solver's tiled smoothing levels (a tuning knob; no
+ * counterpart in the reference): plan < 0 the per-level rule, 0-3 one shape for every
+ * tiled level (64x16, 32x16, 32x8, 32x32 cells).  Different plans sum the preconditioner's
+ * dot products in different orders, so their results differ by rounding. */
+int gb2d_set_tile_plan(gb2d_ctx* ctx, int plan);
 
 /* Kernel probe for roofline measurement: while enabled, the pressure solver
  * brackets every launch of its finest-level smoother (one launch = every red-black
@@ -325,13 +330,26 @@ const char* gb2d_batch_last_error(const gb2d_batch* batch);
 int gb2d_batch_size(const gb2d_batch* batch, int* n, int* workers);
 int gb2d_batch_context(gb2d_batch* batch, int k, gb2d_ctx** ctx);
 /* Autotuner: for each distinct grid size, time one frame (gb2d_advance_frame with cfl)
- * with 1, 2 and 3 red-black sweeps per V-cycle side from the instance's current state
- * (restored afterwards), keep the fastest for every instance of that size (smooth_out[k],
- * may be NULL) and re-place the instances on the workers by the measured times. */
+ * with 1, 2 and 3 red-black sweeps per V-cycle side under each of four tile plans (the
+ * per-level rule, 32x16, 32x8 and 64x16 tiles on every tiled level) from the instance's
+ * current state (restored afterwards), keep the fastest schedule for every instance of that
+ * size (sweeps in smooth_out[k], may be NULL; both through gb2d_batch_schedule) and re-place
+ * the instances on the workers by the measured times. */
 int gb2d_batch_autotune(gb2d_batch* batch, double cfl, const gb2d_solve_opts* opts, int* smooth_out);
 /* gb2d_advance_frame for every instance, frames times.  dts[k]: instance k's previous time
  * step in, its last step out.  opts' mg_smooth is replaced per instance by the tuned value. */
 int gb2d_batch_advance(gb2d_batch* batch, int frames, double cfl, double* dts, const gb2d_solve_opts* opts, gb2d_batch_stats* stats);
+/* The same run as gb2d_batch_advance in one graph launch: every instance is an independent
+ * branch of one CUDA graph, a WHILE node over its frames whose body is the instance's frame
+ * run on the device (the CFL step formed on the GPU, each CG solve a nested WHILE node), so
+ * the host takes part only before and after the run.  The graph is captured on the first
+ * call and again when frames, cfl, opts or the tuned schedules change (stats->wall_ms
+ * excludes the capture).  The instances' fields and dts equal gb2d_batch_advance's bit for
+ * bit (each solve takes at most the host loop's first pass and one restart). */
+int gb2d_batch_run_graph(gb2d_batch* batch, int frames, double cfl, double* dts, const gb2d_solve_opts* opts, gb2d_batch_stats* stats);
+/* Instance k's tuned schedule: red-black sweeps per V-cycle side and tile plan (-1: the
+ * per-level rule; 0-3: one tile shape, 64x16, 32x16, 32x8 or 32x32, for every tiled level). */
+int gb2d_batch_schedule(const gb2d_batch* batch, int k, int* sweeps, int* tile_plan);
 
 /* The general jump-condition Poisson problem (a15; POISSON_SOLVER::Solve with density, bc,
  * div, levelset, jc_on_solution, jc_on_derivative, POISSON_SOLVER.cpp:127-145, and its
