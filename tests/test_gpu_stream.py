@@ -1,6 +1,6 @@
-"""The streaming smoother (gb2d_stream.cuh, the default) performs exactly the red-black
-Gauss-Seidel sweeps, residual restriction and prolongation of the tiled smoother
-(GB2D_SMOOTHER=tiled): one V-cycle of the preconditioner gives bit-identical z on grids
+"""The streaming smoother (gb2d_stream.cuh, GB2D_SMOOTHER=stream) performs exactly the
+red-black Gauss-Seidel sweeps, residual restriction and prolongation of the tiled smoother
+(the default, GB2D_SMOOTHER=tiled): one V-cycle of the preconditioner gives bit-identical z on grids
 with even and odd row lengths, 1, 2 and 3 sweeps per side, FP64 and FP32 levels, with the
 cluster tail and with the single-CTA tail (which leaves the 128^2 level to the smoother).
 Each variant runs in a child process (the library reads the switches once)."""
