@@ -109,3 +109,26 @@ def test_graph_run_fp64_under_tuned_schedules(gb):
         for f, w in zip(fields, want[k]):
             np.testing.assert_array_equal(b.context(k).get(f), w)
     b.close()
+
+
+def test_graph_run_reports_nonfinite_instance(gb):
+    """A NaN put into one instance's level set on the host: the graph run still finishes (each
+    solve's loop sees the non-finite residual and stops), the other instances advance as in a
+    host-driven run, and the call returns GB2D_ERR_NONFINITE naming the instance."""
+    sizes, phis, params = setup()
+    sizes, phis, params = sizes[:3], phis[:3], params[:3]
+    flows = dict(water_viscosity=1.0, air_viscosity=0.01, viscosity=True)
+    opts = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=1e-8)
+    host, graph = _batch(gb, sizes, phis, params, flows), _batch(gb, sizes, phis, params, flows)
+    bad = phis[1].copy()
+    bad[2 + sizes[1][1] // 2, 2 + sizes[1][0] // 2] = np.nan
+    graph.context(1).set(gb.FIELD_PHI, bad)
+    with pytest.raises(gb.GB2DError) as e:
+        graph.run_graph(2, cfl=1.0, opts=opts)
+    assert e.value.code == -3 and "instance 1" in str(e.value)
+    host.advance(2, cfl=1.0, opts=opts)
+    for k in (0, 2):
+        for f in (gb.FIELD_PHI, gb.FIELD_U, gb.FIELD_V, gb.FIELD_P):
+            np.testing.assert_array_equal(graph.context(k).get(f), host.context(k).get(f))
+    host.close()
+    graph.close()
