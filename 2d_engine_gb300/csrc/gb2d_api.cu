@@ -739,7 +739,7 @@ namespace gb2d {
 // them, so that the captured frame can run again.
 int frame_capture(gb2d_ctx* c, double cfl, const gb2d_solve_opts* o) {
   const int phi0 = c->phi_cur;
-  double *u0 = c->u, *v0 = c->v;
+  double *u0 = c->u, *v0 = c->v, *ua0 = c->u_alt, *va0 = c->v_alt;
   c->graph_mode = 1;
   c->dt_dev = &c->sc->dt_frame;
   int rc = curvature_impl(c);
@@ -752,21 +752,34 @@ int frame_capture(gb2d_ctx* c, double cfl, const gb2d_solve_opts* o) {
   if (rc == GB2D_OK) {
     const size_t ni = c->grid.ni, nj = c->grid.nj;
     const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
+    cudaError_t e = cudaSuccess;
     if (c->phi_cur != phi0) {
-      GB2D_CUDA_TRY(c, cudaMemcpyAsync(c->phi_buf[phi0], c->phi_buf[c->phi_cur], (ni + 4) * (nj + 4) * sizeof(double), d2d, c->stream));
+      e = cudaMemcpyAsync(c->phi_buf[phi0], c->phi_buf[c->phi_cur], (ni + 4) * (nj + 4) * sizeof(double), d2d, c->stream);
       c->phi_cur = phi0;
     }
     if (c->u != u0) {
-      GB2D_CUDA_TRY(c, cudaMemcpyAsync(u0, c->u, (ni + 5) * (nj + 4) * sizeof(double), d2d, c->stream));
+      if (e == cudaSuccess) e = cudaMemcpyAsync(u0, c->u, (ni + 5) * (nj + 4) * sizeof(double), d2d, c->stream);
       c->u_alt = c->u;
       c->u = u0;
     }
     if (c->v != v0) {
-      GB2D_CUDA_TRY(c, cudaMemcpyAsync(v0, c->v, (ni + 4) * (nj + 5) * sizeof(double), d2d, c->stream));
+      if (e == cudaSuccess) e = cudaMemcpyAsync(v0, c->v, (ni + 4) * (nj + 5) * sizeof(double), d2d, c->stream);
       c->v_alt = c->v;
       c->v = v0;
     }
-    rc = check_launch(c, "frame");
+    if (e != cudaSuccess) {
+      snprintf(c->err, sizeof(c->err), "frame capture: %s", cudaGetErrorString(e));
+      rc = GB2D_ERR_CUDA;
+    } else {
+      rc = check_launch(c, "frame");
+    }
+  }
+  if (rc != GB2D_OK) {  // nothing captured runs: the buffers keep their roles
+    c->phi_cur = phi0;
+    c->u = u0;
+    c->v = v0;
+    c->u_alt = ua0;
+    c->v_alt = va0;
   }
   c->graph_mode = 0;
   c->dt_dev = nullptr;

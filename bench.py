@@ -695,6 +695,28 @@ def profile_step():
     print(json.dumps({"frames": 2, "dt": dt, "cg_iterations_last_frame": st.iterations}))
 
 
+def profile_batch(n):
+    """A batch of n rising bubbles of 64^2-512^2 (the batch leg's distributions) as one graph
+    launch, one frame captured and run twice, mixed precision: the workload of the batch's
+    whole-graph capture in profiles/ (kernel nodes under conditional nodes are profiled as
+    the whole graph)."""
+    import importlib
+    from tests.golden.cases import batched_bubbles
+    gb = importlib.import_module("2d_engine_gb300")
+    grids, phis, params, flows = batched_bubbles(n, seed=BATCH_SEED)
+    for p in params:
+        p["advection_precision"] = gb.PRECISION_MIXED
+    b = gb.Batch(grids, params=params, flows=flows)
+    for k in range(len(grids)):
+        b.context(k).set(gb.FIELD_PHI, phis[k])
+    opts = gb.solve_opts(precision=gb.PRECISION_MIXED, tolerance=TOL)
+    dts, st = b.run_graph(1, cfl=1.0, opts=opts, allow_max_iters=True)
+    dts, st = b.run_graph(1, cfl=1.0, dts=dts, opts=opts, allow_max_iters=True)
+    print(json.dumps({"instances": len(grids), "frames": 1, "wall_ms": st.wall_ms, "cg_iterations": st.cg_iterations,
+                      "max_rel_residual": st.max_rel_residual}))
+    b.close()
+
+
 def profile_projection():
     """The headline workload alone: 4 mixed-precision projections of the 1024^2 state (3 warm-up,
     1 as timed), each restored from a device checkpoint, then 1 FP64 projection: the workload of
@@ -730,7 +752,12 @@ def main():
                     help="only run the 1024^2 projections (4 mixed, 1 FP64), for profilers")
     ap.add_argument("--profile-step", action="store_true",
                     help="only run two mixed-precision frames (CFL time steps, viscous term on) of the 1024^2 state, for profilers")
+    ap.add_argument("--profile-batch", type=int, nargs="?", const=16, default=0, metavar="N",
+                    help="only run an N-instance batch (default 16) as one graph launch (two one-frame runs), for profilers")
     args = ap.parse_args()
+    if args.profile_batch:
+        profile_batch(args.profile_batch)
+        return
     if args.profile_projection:
         profile_projection()
         return
