@@ -1063,11 +1063,13 @@ bool plan_ctail(Hierarchy<T>& H, int P) {
   const int nl = H.nlev;
   const char* env = getenv("GB2D_CTAIL_TOP_CELLS");  // tuning override of kCtMaxTopCells
   const long top_cells = env && atol(env) > 0 ? atol(env) : kCtMaxTopCells;
+  const char* env_rows = getenv("GB2D_CTAIL_MIN_ROWS");  // tuning override of kCtMinRows
+  const int min_rows = env_rows && atoi(env_rows) > 0 ? atoi(env_rows) : kCtMinRows;
   for (int top = 0; top < nl - 1; ++top) {
     if (nl - top > kCtMaxLevels) continue;
     if ((long)H.L[top].nI * H.L[top].nJ > top_cells) continue;
     int lb = top - 1;
-    while (lb + 1 < nl - 1 && H.L[lb + 1].nJ >= P * kCtMinRows) ++lb;
+    while (lb + 1 < nl - 1 && H.L[lb + 1].nJ >= P * min_rows) ++lb;
     if (lb < top || H.L[lb].nJ > kCtOwnerRows) continue;
     CtArgs<T> a;
     memset(&a, 0, sizeof a);
@@ -1128,7 +1130,8 @@ bool plan_ctail(Hierarchy<T>& H, int P) {
 }
 
 // Cluster size the part can co-schedule for the cluster tail (16, else 8), or 0.
-// GB2D_CLUSTER_TAIL=0 in the environment selects the single-CTA tail instead.
+// GB2D_CLUSTER_TAIL=0 in the environment selects the single-CTA tail instead;
+// GB2D_CLUSTER_CTAS=P (2-16) asks for P CTAs, for tuning.
 int ctail_cluster_size() {
   const char* env = getenv("GB2D_CLUSTER_TAIL");
   if (env && env[0] == '0') return 0;
@@ -1143,7 +1146,10 @@ int ctail_cluster_size() {
     cudaGetLastError();
     return cached;
   }
-  for (int P : {16, 8}) {
+  const char* pe = getenv("GB2D_CLUSTER_CTAS");
+  const int want = pe ? atoi(pe) : 0;
+  const int sizes[2] = {want >= 2 && want <= kClusterMax ? want : 16, want >= 2 && want <= kClusterMax ? want : 8};
+  for (int P : sizes) {
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;

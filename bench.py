@@ -149,14 +149,19 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch():
-    """DRAM bytes per launch of the probed kernel from the committed ncu summary, if any."""
+def ncu_traffic(key="smooth_f32_level0_bytes_per_launch"):
+    """A DRAM-traffic figure from the committed ncu summary (profiles/traffic.json), if any."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get("smooth_f32_level0_bytes_per_launch")
+            return json.load(f).get(key)
     except (OSError, ValueError):
         return None
+
+
+def ncu_traffic_per_launch():
+    """DRAM bytes per launch of the probed kernel from the committed ncu summary, if any."""
+    return ncu_traffic()
 
 
 TOL_ORACLE = 3e-10
@@ -331,6 +336,14 @@ def run_batch(gb, n, frames, cpu=True, dist=None, rank=0, ws=1):
                         "cg_iterations_per_projection": st.cg_iterations / (3.0 * n * f),
                         "max_rel_residual": st.max_rel_residual,
                         "path": "gb2d_batch_run_graph: one graph launch per run, every instance a WHILE node over its frames"})
+            per_cell = ncu_traffic("batch_graph_dram_bytes_per_cell_frame")
+            if per_cell:
+                peak, peak_kind = measured_peaks()
+                gbs = per_cell * out["cell_frames_per_s"] / 1e9
+                out["hbm"] = {"dram_gbs": gbs, "frac": gbs / peak, "peak_gbs": peak, "peak_source": peak_kind,
+                              "dram_bytes_per_cell_frame": per_cell,
+                              "source": "DRAM bytes per cell-frame from the whole-graph ncu capture of a 64-instance batch "
+                                        "(profiles/batch_graph_64.md) times this run's cell-frames/s"}
         b.close()
     out["one_worker_ms_per_frame_all_instances"] = walls[1]
     out["graph_speedup_vs_one_worker"] = walls[1] / out["ms_per_frame_all_instances"]
