@@ -95,6 +95,20 @@ def test_create_rejects_non_positive_densities(gb):
         assert not h.value
 
 
+def test_batch_entry_points_reject_bad_arguments(gb):
+    """The batch run, its schedule query and the tile-plan knob check their arguments before any
+    device work (no GPU needed)."""
+    lib = gb.library()
+    st = gb.BatchStatsT()
+    o = gb.solve_opts()
+    dts = (ctypes.c_double * 1)()
+    assert lib.gb2d_batch_run_graph(None, 1, 1.0, dts, ctypes.byref(o), ctypes.byref(st)) == -1
+    assert lib.gb2d_batch_advance(None, 1, 1.0, dts, ctypes.byref(o), ctypes.byref(st)) == -1
+    sw, tp = ctypes.c_int(), ctypes.c_int()
+    assert lib.gb2d_batch_schedule(None, 0, ctypes.byref(sw), ctypes.byref(tp)) == -1
+    assert lib.gb2d_set_tile_plan(None, 1) == -1
+
+
 def test_reference_solver_links_with_the_dropin(gb):
     """The drop-in in the reference's own solver class: oracle/ref/patch_gpu_step.py applies
     the member hooks INTEGRATION.md describes to a copy of EULERIAN_FLUID_SOLVER_2D.h, and the
