@@ -188,9 +188,9 @@ def oracle_errors(c, gb):
     return out
 
 
-def make_case():
+def make_case(n=N):
     from tests.golden.cases import bubbles_case
-    return bubbles_case(N, seed=SEED)
+    return bubbles_case(n, seed=SEED)
 
 
 def _oracle():
@@ -730,17 +730,18 @@ def profile_batch(n):
     b.close()
 
 
-def profile_projection():
+def profile_projection(n=N):
     """The headline workload alone: 4 mixed-precision projections of the 1024^2 state (3 warm-up,
     1 as timed), each restored from a device checkpoint, then 1 FP64 projection: the workload of
-    the projection launch list and the smoothing-kernel capture in profiles/."""
+    the projection launch list and the smoothing-kernel capture in profiles/.  n: the same case
+    on an n^2 grid."""
     import importlib
     gb = importlib.import_module("2d_engine_gb300")
-    case = make_case()
-    dt = 0.5 / (N - 1)
-    out = {}
+    case = make_case(n)
+    dt = 0.5 / (n - 1)
+    out = {"n": n}
     for name, prec, reps in (("mixed", gb.PRECISION_MIXED, 4), ("fp64", gb.PRECISION_FP64, 1)):
-        c = gb.Context(N, N)
+        c = gb.Context(n, n)
         for f, k in ((gb.FIELD_PHI, "phi"), (gb.FIELD_U, "u"), (gb.FIELD_V, "v"), (gb.FIELD_P, "p")):
             c.set(f, case[k])
         c.checkpoint_save()
@@ -761,8 +762,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--profile-projection", action="store_true",
-                    help="only run the 1024^2 projections (4 mixed, 1 FP64), for profilers")
+    ap.add_argument("--profile-projection", type=int, nargs="?", const=N, default=0, metavar="N",
+                    help="only run the benchmark's projections (4 mixed, 1 FP64) on an N^2 grid (default 1024), for profilers")
     ap.add_argument("--profile-step", action="store_true",
                     help="only run two mixed-precision frames (CFL time steps, viscous term on) of the 1024^2 state, for profilers")
     ap.add_argument("--profile-batch", type=int, nargs="?", const=16, default=0, metavar="N",
@@ -772,7 +773,7 @@ def main():
         profile_batch(args.profile_batch)
         return
     if args.profile_projection:
-        profile_projection()
+        profile_projection(args.profile_projection)
         return
     if args.profile_step:
         profile_step()
