@@ -272,53 +272,203 @@ struct TileShape {
   static constexpr int QX = X / 2, QY = Y / 2;                        // its quads (coarse cells)
 };
 
+// The staged window holds W x HH cells per array.  FP64 levels keep it in the
+// natural layout (cell (c, r) is element c + r W).  FP32 levels hold it split by
+// colour: cell (c, r) is element r WH + c / 2 (WH = W / 2) of plane (c + r) & 1.
+// A half sweep then updates one plane and reads its neighbours from the other, so
+// consecutive threads touch consecutive elements of each plane; in the natural
+// layout the cells of one colour lie two elements apart and every shared-memory
+// access of a half sweep takes two bank wavefronts.  FP64 half sweeps are bound by
+// the FP64 pipe instead, and the split layout's sweeps run over whole plane rows
+// (below), which costs FP64 issue slots.  Where plane 1 starts depends on how the
+// window is staged (below): for pair staging at a 128-byte boundary, for cell
+// staging 64 bytes past one, so that each warp's staging stores fall in distinct
+// banks.
 template <typename T, int H, int SH>
 struct Win {
-  static constexpr int W = TileShape<SH>::X + 2 * H, HH = TileShape<SH>::Y + 2 * H, N = W * HH;
+  static constexpr bool SPLIT = sizeof(T) == 4, PAIRS = SPLIT && SH == 3;
+  static constexpr int W = TileShape<SH>::X + 2 * H, HH = TileShape<SH>::Y + 2 * H, N = W * HH, WH = W / 2;
+  static constexpr int E = 128 / (int)sizeof(T), PLANE = HH * WH;
+  static constexpr int PO = PAIRS ? (PLANE + E - 1) / E * E : PLANE + (E / 2 - PLANE % E + E) % E;  // plane 1 (elements)
+  static constexpr int NA = SPLIT ? 2 * PO : N;  // elements per staged array (a multiple of E when split)
+  static_assert(W % 2 == 0, "window rows must hold an even number of cells");
 };
 
 template <typename T, int H, bool DG, int SH>
 constexpr size_t sweep_smem() {
-  return sizeof(T) * (size_t)Win<T, H, SH>::N * (DG ? 6 : 5);
+  return sizeof(T) * (size_t)Win<T, H, SH>::NA * (DG ? 6 : 5);
+}
+
+// Element offsets of window cell (c, r) and of its left, right, lower and upper
+// neighbours.
+struct CellOff {
+  int s, l, r, b, t;
+};
+template <typename T, int H, int SH>
+__device__ __forceinline__ CellOff cell_off(int c, int r) {
+  using Wn = Win<T, H, SH>;
+  if constexpr (Wn::SPLIT) {
+    const int m = r * Wn::WH + (c >> 1), pl = (c + r) & 1, o = c & 1, t = (pl ^ 1) * Wn::PO + m;
+    return CellOff{pl * Wn::PO + m, t - 1 + o, t + o, t - Wn::WH, t + Wn::WH};
+  } else {
+    const int e = c + r * Wn::W;
+    return CellOff{e, e - 1, e + 1, e - Wn::W, e + Wn::W};
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void cp_async(T* dst, const T* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"((int)sizeof(T)) : "memory");
+}
+// The same, or zeros when !valid (src-size 0: nothing is read).
+template <typename T>
+__device__ __forceinline__ void cp_async_zfill(T* dst, const T* src, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const unsigned n = valid ? (unsigned)sizeof(T) : 0u;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src), "n"((int)sizeof(T)), "r"(n) : "memory");
 }
 
 // Stage the window.  LOAD_X: read x (else zero); PROLONG: add the coarse correction.
-// The window's cells are enumerated flat (division by compile-time constants
-// only), so every thread of the block has work in every pass.
+// The window is enumerated flat (division by compile-time constants only), so
+// every thread of the block has work in every pass.
+//   Natural layout: one cell per thread and pass, loaded through registers.
+//   Split layout: the coefficients (and x without a correction) are copied with
+//   cp.async, so that all of a thread's copies are in flight at once,
+//   zero-filled outside the domain by the copy itself.  32x32 tiles (the FP32
+//   levels of 2048^2 and more) copy one pair of cells (2m, r), (2m + 1, r) per
+//   thread and pass, which land at the same element r WH + m of planes r & 1 and
+//   (r + 1) & 1 (half the index arithmetic per cell); the other tiles one cell
+//   per thread and pass (one contiguous row segment per warp and copy).
+//   Measured on the finest level's two launches, mixed projection: pairs 21.7 /
+//   54.0 / 185.8 us against cells 20.7 / 57.5 / 196.0 us at 1024^2 (32x16 tiles),
+//   2048^2 and 4096^2 (32x32).
 template <typename T, int H, bool LOAD_X, bool PROLONG, bool DG, int SH>
 __device__ __forceinline__ void stage_window(const Level<T>& L, const Level<T>& C, T* sm, int i0, int j0) {
   using Wn = Win<T, H, SH>;
-  constexpr int W = Wn::W, HH = Wn::HH, N = Wn::N;
-  T *xs = sm, *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N, *ds = sm + 5 * N;
+  constexpr int W = Wn::W, HH = Wn::HH, N = Wn::N, NA = Wn::NA;
+  T *xs = sm, *bs = sm + NA, *is = sm + 2 * NA, *cxs = sm + 3 * NA, *cys = sm + 4 * NA, *ds = sm + 5 * NA;
   const int gi0 = i0 - H, gj0 = j0 - H;
   const bool inner = gi0 >= 0 && gj0 >= 0 && gi0 + W <= L.nI && gj0 + HH <= L.nJ;
   const size_t base = (size_t)(gi0 + 1) + (size_t)(gj0 + 1) * L.ld;
   const int tid = threadIdx.x + threadIdx.y * BXT;
+  if constexpr (Wn::SPLIT) {
+    if constexpr (Wn::PAIRS) {
+      constexpr int WH = Wn::WH, PO = Wn::PO, PLANE = Wn::PLANE;
 #pragma unroll
-  for (int u0 = 0; u0 < N; u0 += BXT * BYT) {
-    const int q = u0 + tid;
-    if (q >= N) continue;
-    const int r = q / W, c = q - r * W;
-    const int gi = gi0 + c, gj = gj0 + r;
-    T x = 0, b = 0, id = 0, cx = 0, cy = 0, dg = 0;
-    if (inner || (gi >= 0 && gi < L.nI && gj >= 0 && gj < L.nJ)) {
-      const size_t k = base + c + (size_t)r * L.ld;
-      if (LOAD_X) {
-        x = L.x[k];
-        if (PROLONG) x += C.x[(size_t)(gi / 2 + 1) + (size_t)(gj / 2 + 1) * C.ld];
+      for (int u0 = 0; u0 < PLANE; u0 += BXT * BYT) {
+        const int q = u0 + tid;  // = r WH + m
+        if (u0 + BXT * BYT > PLANE && q >= PLANE) continue;
+        const int r = q / WH, c = 2 * (q - r * WH);
+        const int ea = (r & 1) * PO + q, eb = ((r & 1) ^ 1) * PO + q;
+        const int gi = gi0 + c, gj = gj0 + r;
+        const bool rok = gj >= 0 && gj < L.nJ;
+        const bool ina = inner || (rok && gi >= 0 && gi < L.nI), inb = inner || (rok && gi + 1 >= 0 && gi + 1 < L.nI);
+        const size_t k = base + c + (size_t)r * L.ld, ka = ina ? k : 0, kb = inb ? k + 1 : 0;
+        if (PROLONG) {
+          T xa = 0, xb = 0;
+          if (ina) xa = L.x[ka] + C.x[(size_t)(gi / 2 + 1) + (size_t)(gj / 2 + 1) * C.ld];
+          if (inb) xb = L.x[kb] + C.x[(size_t)((gi + 1) / 2 + 1) + (size_t)(gj / 2 + 1) * C.ld];
+          xs[ea] = xa;
+          xs[eb] = xb;
+        } else if (LOAD_X) {
+          cp_async_zfill(xs + ea, L.x + ka, ina);
+          cp_async_zfill(xs + eb, L.x + kb, inb);
+        } else {
+          xs[ea] = 0;
+          xs[eb] = 0;
+        }
+        if (inner) {
+          cp_async(bs + ea, L.b + k);
+          cp_async(bs + eb, L.b + k + 1);
+          cp_async(is + ea, L.idg + k);
+          cp_async(is + eb, L.idg + k + 1);
+          cp_async(cxs + ea, L.cx + k);
+          cp_async(cxs + eb, L.cx + k + 1);
+          cp_async(cys + ea, L.cy + k);
+          cp_async(cys + eb, L.cy + k + 1);
+          if (DG) {
+            cp_async(ds + ea, L.dg + k);
+            cp_async(ds + eb, L.dg + k + 1);
+          }
+        } else {
+          cp_async_zfill(bs + ea, L.b + ka, ina);
+          cp_async_zfill(bs + eb, L.b + kb, inb);
+          cp_async_zfill(is + ea, L.idg + ka, ina);
+          cp_async_zfill(is + eb, L.idg + kb, inb);
+          cp_async_zfill(cxs + ea, L.cx + ka, ina);
+          cp_async_zfill(cxs + eb, L.cx + kb, inb);
+          cp_async_zfill(cys + ea, L.cy + ka, ina);
+          cp_async_zfill(cys + eb, L.cy + kb, inb);
+          if (DG) {
+            cp_async_zfill(ds + ea, L.dg + ka, ina);
+            cp_async_zfill(ds + eb, L.dg + kb, inb);
+          }
+        }
       }
-      b = L.b[k];
-      id = L.idg[k];
-      cx = L.cx[k];
-      cy = L.cy[k];
-      if (DG) dg = L.dg[k];
+    } else {
+      constexpr int WH = Wn::WH, PO = Wn::PO;
+#pragma unroll
+      for (int u0 = 0; u0 < N; u0 += BXT * BYT) {
+        const int q = u0 + tid;
+        if (u0 + BXT * BYT > N && q >= N) continue;
+        const int r = q / W, c = q - r * W;
+        const int e = ((c + r) & 1) * PO + r * WH + (c >> 1);
+        const int gi = gi0 + c, gj = gj0 + r;
+        const bool in = inner || (gi >= 0 && gi < L.nI && gj >= 0 && gj < L.nJ);
+        const size_t k = base + c + (size_t)r * L.ld, kz = in ? k : 0;
+        if (PROLONG) {
+          T x = 0;
+          if (in) x = L.x[k] + C.x[(size_t)(gi / 2 + 1) + (size_t)(gj / 2 + 1) * C.ld];
+          xs[e] = x;
+        } else if (LOAD_X) {
+          cp_async_zfill(xs + e, L.x + kz, in);
+        } else {
+          xs[e] = 0;
+        }
+        if (inner) {
+          cp_async(bs + e, L.b + k);
+          cp_async(is + e, L.idg + k);
+          cp_async(cxs + e, L.cx + k);
+          cp_async(cys + e, L.cy + k);
+          if (DG) cp_async(ds + e, L.dg + k);
+        } else {
+          cp_async_zfill(bs + e, L.b + kz, in);
+          cp_async_zfill(is + e, L.idg + kz, in);
+          cp_async_zfill(cxs + e, L.cx + kz, in);
+          cp_async_zfill(cys + e, L.cy + kz, in);
+          if (DG) cp_async_zfill(ds + e, L.dg + kz, in);
+        }
+      }
     }
-    xs[q] = x;
-    bs[q] = b;
-    is[q] = id;
-    cxs[q] = cx;
-    cys[q] = cy;
-    if (DG) ds[q] = dg;
+    asm volatile("cp.async.wait_all;" ::: "memory");
+  } else {
+#pragma unroll
+    for (int u0 = 0; u0 < N; u0 += BXT * BYT) {
+      const int q = u0 + tid;
+      if (q >= N) continue;
+      const int r = q / W, c = q - r * W;
+      const int gi = gi0 + c, gj = gj0 + r;
+      T x = 0, b = 0, id = 0, cx = 0, cy = 0, dg = 0;
+      if (inner || (gi >= 0 && gi < L.nI && gj >= 0 && gj < L.nJ)) {
+        const size_t k = base + c + (size_t)r * L.ld;
+        if (LOAD_X) {
+          x = L.x[k];
+          if (PROLONG) x += C.x[(size_t)(gi / 2 + 1) + (size_t)(gj / 2 + 1) * C.ld];
+        }
+        b = L.b[k];
+        id = L.idg[k];
+        cx = L.cx[k];
+        cy = L.cy[k];
+        if (DG) dg = L.dg[k];
+      }
+      xs[q] = x;
+      bs[q] = b;
+      is[q] = id;
+      cxs[q] = cx;
+      cys[q] = cy;
+      if (DG) ds[q] = dg;
+    }
   }
 }
 
@@ -342,32 +492,62 @@ __device__ __forceinline__ T gs_residual(T b, T dg, T x, T cxl, T xl, T cxr, T x
   return b - fmad(-cyt, xt, fmad(-cyb, xb, fmad(-cxr, xr, fmad(-cxl, xl, mulr(dg, x)))));
 }
 
-// Half sweep of one colour over the window shrunk by R cells per side: the
-// colour's RH x RW/2 cells are enumerated flat over the block's threads.
-template <typename T, int H, int R, int SH>
-__device__ __forceinline__ void window_half(T* sm, int i0, int j0, int nI, int nJ, int color) {
+// Half sweep of one colour over the window shrunk by R cells per side.
+//   Natural layout: the colour's RH x RW/2 cells are enumerated flat over the
+//   block's threads.
+//   Split layout: the threads walk the colour's plane element by element over
+//   rows R .. HH-R-1, whole rows, so that a warp's accesses to each plane are
+//   consecutive elements; with o = c & 1 the left and right neighbours of
+//   element e are elements e - 1 + o and e + o of the other plane, the lower and
+//   upper ones e - WH and e + WH.  Tile origins are even, so the colour's plane
+//   is the colour itself.  The cells of those rows outside the shrunk window,
+//   and the cells outside the domain, are updated too, without a test: a cell
+//   outside the domain is staged with b, 1/dg and both of its faces' conductances
+//   zero (as are the wall faces of the cells next to it), so it stays zero; a
+//   cell in the margin (column c < R or c >= W - R) gets a value from its staged
+//   neighbours (at the row ends, elements of the adjacent row) that nothing
+//   exact reads: after half sweep k the cells of columns k .. W-k-1 hold the
+//   exact values, since half sweep k + 1 updates columns k+1 .. W-k-2 from
+//   neighbours in columns k .. W-k-1, and the tile with its one-cell ring lies
+//   in columns 2 NS .. W-2NS-1.
+template <typename T, int H, int R, int SH, int COLOR>
+__device__ __forceinline__ void window_half(T* sm, int i0, int j0, int nI, int nJ) {
   using Wn = Win<T, H, SH>;
-  constexpr int W = Wn::W, HH = Wn::HH, N = Wn::N;
-  constexpr int RW = W - 2 * R, RH = HH - 2 * R, HALF = RW / 2, TOT = RH * HALF;
-  static_assert(RW % 2 == 0, "window rows must hold an even number of cells");
-  T* xs = sm;
-  const T *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N;
-  const int gi0 = i0 - H, gj0 = j0 - H;
-  const bool inner = gi0 + R >= 0 && gj0 + R >= 0 && gi0 + W - R <= nI && gj0 + HH - R <= nJ;
+  constexpr int W = Wn::W, HH = Wn::HH, NA = Wn::NA;
   const int tid = threadIdx.x + threadIdx.y * BXT;
+  if constexpr (Wn::SPLIT) {
+    constexpr int WH = Wn::WH, PO = Wn::PO, E0 = R * WH, TOT = (HH - 2 * R) * WH;
+    constexpr int p = COLOR, pq = COLOR ^ 1;
+    T* xp = sm + p * PO;
+    const T *xq = sm + pq * PO, *bp = sm + NA + p * PO, *ip = sm + 2 * NA + p * PO;
+    const T *cxp = sm + 3 * NA + p * PO, *cxq = sm + 3 * NA + pq * PO, *cyp = sm + 4 * NA + p * PO, *cyq = sm + 4 * NA + pq * PO;
 #pragma unroll
-  for (int u0 = 0; u0 < TOT; u0 += BXT * BYT) {
-    const int u = u0 + tid;
-    if (u >= TOT) continue;
-    const int rr = u / HALF, m = u - rr * HALF;
-    const int r = R + rr, gj = gj0 + r;
-    const int c = R + 2 * m + ((color - (gi0 + R) - gj) & 1);
-    if (!inner) {
-      const int gi = gi0 + c;
-      if (gi < 0 || gi >= nI || gj < 0 || gj >= nJ) continue;
+    for (int u0 = 0; u0 < TOT; u0 += BXT * BYT) {
+      const int e = E0 + u0 + tid;
+      if (u0 + BXT * BYT > TOT && e >= E0 + TOT) continue;
+      const int o = (p + e / WH) & 1;
+      xp[e] = gs_update(bp[e], cxp[e], xq[e - 1 + o], cxq[e + o], xq[e + o], cyp[e], xq[e - WH], cyq[e + WH], xq[e + WH], ip[e]);
     }
-    const int s = c + r * W;
-    xs[s] = gs_update(bs[s], cxs[s], xs[s - 1], cxs[s + 1], xs[s + 1], cys[s], xs[s - W], cys[s + W], xs[s + W], is[s]);
+  } else {
+    constexpr int RW = W - 2 * R, RH = HH - 2 * R, HALF = RW / 2, TOT = RH * HALF;
+    T* xs = sm;
+    const T *bs = sm + NA, *is = sm + 2 * NA, *cxs = sm + 3 * NA, *cys = sm + 4 * NA;
+    const int gi0 = i0 - H, gj0 = j0 - H;
+    const bool inner = gi0 + R >= 0 && gj0 + R >= 0 && gi0 + W - R <= nI && gj0 + HH - R <= nJ;
+#pragma unroll
+    for (int u0 = 0; u0 < TOT; u0 += BXT * BYT) {
+      const int u = u0 + tid;
+      if (u >= TOT) continue;
+      const int rr = u / HALF, m = u - rr * HALF;
+      const int r = R + rr, gj = gj0 + r;
+      const int c = R + 2 * m + ((COLOR - (gi0 + R) - gj) & 1);
+      if (!inner) {
+        const int gi = gi0 + c;
+        if (gi < 0 || gi >= nI || gj < 0 || gj >= nJ) continue;
+      }
+      const int s = c + r * W;
+      xs[s] = gs_update(bs[s], cxs[s], xs[s - 1], cxs[s + 1], xs[s + 1], cys[s], xs[s - W], cys[s + W], xs[s + W], is[s]);
+    }
   }
 }
 
@@ -427,7 +607,7 @@ __device__ __forceinline__ void publish_rz(Scalars* sc, double rz) {
 template <typename T, int H, int R, int R1, int C0, int SH>
 __device__ __forceinline__ void window_halves(T* sm, int i0, int j0, int nI, int nJ) {
   if constexpr (R <= R1) {
-    window_half<T, H, R, SH>(sm, i0, j0, nI, nJ, (C0 + R - 1) & 1);
+    window_half<T, H, R, SH, (C0 + R - 1) & 1>(sm, i0, j0, nI, nJ);
     __syncthreads();
     window_halves<T, H, R + 1, R1, C0, SH>(sm, i0, j0, nI, nJ);
   }
@@ -458,14 +638,14 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C,
   constexpr int H = 2 * NS + 1;
   using Wn = Win<T, H, SH>;
   using Ts = TileShape<SH>;
-  constexpr int W = Wn::W, N = Wn::N;
+  constexpr int NA = Wn::NA;
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int i0 = blockIdx.x * Ts::X, j0 = blockIdx.y * Ts::Y;
   stage_window<T, H, false, false, false, SH>(L, C, sm, i0, j0);
   __syncthreads();
   window_halves<T, H, 1, 2 * NS, 0, SH>(sm, i0, j0, L.nI, L.nJ);
-  const T *xs = sm, *bs = sm + N, *is = sm + 2 * N, *cxs = sm + 3 * N, *cys = sm + 4 * N;
+  const T *xs = sm, *bs = sm + NA, *is = sm + 2 * NA, *cxs = sm + 3 * NA, *cys = sm + 4 * NA;
   const int tid = threadIdx.x + threadIdx.y * BXT;
 #pragma unroll
   for (int q0 = 0; q0 < Ts::QX * Ts::QY; q0 += BXT * BYT) {
@@ -480,11 +660,11 @@ __global__ void __launch_bounds__(BXT* BYT) k_pre_smooth(Level<T> L, Level<T> C,
         const int ti = 2 * qx + dc, tj = 2 * qy + dr;
         const int gi = i0 + ti, gj = j0 + tj;
         if (gi >= L.nI || gj >= L.nJ) continue;
-        const int s = (ti + H) + (tj + H) * W;
-        xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
+        const CellOff w = cell_off<T, H, SH>(ti + H, tj + H);
+        xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[w.s];
         if (!((gi + gj) & 1)) {  // red cells: black residuals are zero after the black half sweep
-          acc += gs_residual(bs[s], diag_of(is[s]), xs[s], cxs[s], xs[s - 1], cxs[s + 1], xs[s + 1], cys[s], xs[s - W], cys[s + W],
-                             xs[s + W]);
+          acc += gs_residual(bs[w.s], diag_of(is[w.s]), xs[w.s], cxs[w.s], xs[w.l], cxs[w.r], xs[w.r], cys[w.s], xs[w.b], cys[w.t],
+                             xs[w.t]);
         }
       }
     const int I = i0 / 2 + qx, J = j0 / 2 + qy;
@@ -503,14 +683,14 @@ __global__ void __launch_bounds__(BXT* BYT) k_post_smooth(Level<T> L, Level<T> C
   constexpr int H = 2 * NS;
   using Wn = Win<T, H, SH>;
   using Ts = TileShape<SH>;
-  constexpr int W = Wn::W, N = Wn::N;
+  constexpr int NA = Wn::NA;
   extern __shared__ unsigned char smem_raw[];
   T* sm = reinterpret_cast<T*>(smem_raw);
   const int i0 = blockIdx.x * Ts::X, j0 = blockIdx.y * Ts::Y;
   stage_window<T, H, true, true, false, SH>(L, C, sm, i0, j0);
   __syncthreads();
   window_halves<T, H, 1, 2 * NS, 1, SH>(sm, i0, j0, L.nI, L.nJ);
-  const T *xs = sm, *bs = sm + N;
+  const T *xs = sm, *bs = sm + NA;
   Acc<T> acc;
   const int tid = threadIdx.x + threadIdx.y * BXT;
 #pragma unroll
@@ -525,9 +705,9 @@ __global__ void __launch_bounds__(BXT* BYT) k_post_smooth(Level<T> L, Level<T> C
         const int ti = 2 * qx + dc, tj = 2 * qy + dr;
         const int gi = i0 + ti, gj = j0 + tj;
         if (gi >= L.nI || gj >= L.nJ) continue;
-        const int s = (ti + H) + (tj + H) * W;
-        xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[s];
-        if (part_rz) acc.add(bs[s] * xs[s]);
+        const int e = cell_off<T, H, SH>(ti + H, tj + H).s;
+        xout[(size_t)(gi + 1) + (size_t)(gj + 1) * L.ld] = xs[e];
+        if (part_rz) acc.add(bs[e] * xs[e]);
       }
   }
   if (part_rz) {
@@ -1244,11 +1424,12 @@ void build_level0_f64(cudaStream_t s, Hierarchy<double>& H, const gb2d_ctx* c, d
 }
 
 // Algorithmic bytes of one tiled smoothing launch on a level (every array read
-// or written once): pre-smoothing reads b, 1/dg, cx, cy, dg, writes x and the
-// coarse b; post-smoothing reads x, b, 1/dg, cx, cy and the coarse x, writes x.
+// or written once): pre-smoothing reads b, 1/dg, cx, cy, writes x and the
+// coarse b (5.25 arrays); post-smoothing reads x, b, 1/dg, cx, cy and the coarse
+// x, writes x (6.25 arrays).
 template <typename T>
-double smooth_bytes(const Level<T>& L) {
-  return sizeof(T) * (double)L.nI * L.nJ * 6.25;
+double smooth_bytes(const Level<T>& L, bool pre) {
+  return sizeof(T) * (double)L.nI * L.nJ * (pre ? 5.25 : 6.25);
 }
 
 // Launch with programmatic stream serialization (see pdl_enter).
@@ -1411,7 +1592,7 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
     else
       launch_pre<T, 3>(s, sh, L, H.L[l + 1], L.xa, done);
     GB_LAUNCHED(1);
-    probe_end(pr, s, on, smooth_bytes(L));
+    probe_end(pr, s, on, smooth_bytes(L, true));
   }
   if (cluster) {
     launch_ctail<T>(s, H, ainv, nu, done, S->sc);
@@ -1445,7 +1626,7 @@ void vcycle(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv, int 
     else
       launch_post<T, 3>(s, sh, Lin, H.L[l + 1], L.x, prz, S);
     GB_LAUNCHED(1);
-    probe_end(pr, s, on, smooth_bytes(L));
+    probe_end(pr, s, on, smooth_bytes(L, false));
   }
 }
 
