@@ -55,10 +55,18 @@ __device__ __forceinline__ double warp_sum(double v) {
 __device__ __forceinline__ int linear_tid() { return threadIdx.x + threadIdx.y * blockDim.x; }
 __device__ __forceinline__ int block_threads() { return blockDim.x * blockDim.y; }
 
+// Shared scratch of the block reductions: one array for every reduction helper
+// that a kernel uses, so that they add 264 bytes of static shared memory once
+// (one byte more can cost a resident block on the smoothing kernels).
+__device__ __forceinline__ double* reduce_scratch() {
+  __shared__ double buf[33];
+  return buf;
+}
+
 // Deterministic block sum (block size a multiple of 32, <= 1024); result valid in every thread.
 __device__ double block_sum(double v) {
-  __shared__ double sm[32];
-  __shared__ double total;
+  double* sm = reduce_scratch();
+  double& total = sm[32];
   int tid = linear_tid();
   int lane = tid & 31, w = tid >> 5, nw = block_threads() >> 5;
   v = warp_sum(v);
@@ -69,6 +77,52 @@ __device__ double block_sum(double v) {
     double x = lane < nw ? sm[lane] : 0.0;
     x = warp_sum(x);
     if (lane == 0) total = x;
+  }
+  __syncthreads();
+  return total;
+}
+
+// Double-float values (two FP32 words, about 48 significant bits) summed on the
+// FP32 pipe: GB300 issues FP64 at a small fraction of its FP32 rate, and an FP64
+// shuffle tree in every warp cost as many FP64 instructions as the vector update
+// it reduced.  Every operation rounds as written (no contraction), so a sum is
+// fixed by the order of its operands.  df_add: Knuth's TwoSum of the leading
+// words, the trailing words added to its error, then Dekker's Fast2Sum.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  const float t = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  const float h = __fadd_rn(s, t);
+  return DF{h, __fsub_rn(t, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ DF warp_sum_df(DF v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = df_add(v, DF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
+  return v;
+}
+// Deterministic block sum of double-float values, as FP64 (valid in every thread).
+__device__ double block_sum_df(DF v) {
+  double* sm = reduce_scratch();
+  float* shi = reinterpret_cast<float*>(sm);
+  float* slo = shi + 32;
+  double& total = sm[32];
+  int tid = linear_tid();
+  int lane = tid & 31, w = tid >> 5, nw = block_threads() >> 5;
+  v = warp_sum_df(v);
+  __syncthreads();
+  if (lane == 0) {
+    shi[w] = v.hi;
+    slo[w] = v.lo;
+  }
+  __syncthreads();
+  if (w == 0) {
+    DF x = lane < nw ? DF{shi[lane], slo[lane]} : DF{0.f, 0.f};
+    x = warp_sum_df(x);
+    if (lane == 0) total = widen(x.hi) + widen(x.lo);
   }
   __syncthreads();
   return total;
@@ -552,7 +606,8 @@ __device__ __forceinline__ void window_half(T* sm, int i0, int j0, int nI, int n
 }
 
 // FP32-friendly accumulation of a few products per thread (Kahan-compensated in
-// the vector precision); the block and grid reductions are FP64.
+// the vector precision, s - c); the block reduction continues in double-float on
+// the FP32 pipe, the grid reduction in FP64.
 template <typename T>
 struct Acc {
   T s = 0, c = 0;
@@ -562,21 +617,20 @@ struct Acc {
     c = (t - s) - y;
     s = t;
   }
-  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+  __device__ __forceinline__ double block_total() const { return block_sum_df(DF{s, -c}); }
 };
 template <>
 struct Acc<double> {  // FP64 vectors: plain accumulation (FP64 issue slots are scarce)
   double s = 0;
   __device__ __forceinline__ void add(double v) { s += v; }
-  __device__ __forceinline__ double value() const { return s; }
+  __device__ __forceinline__ double block_total() const { return block_sum(s); }
 };
 
-// Last-block finalisation of a reduction: every block stores its partial, the
-// block that arrives last sums them in a fixed order.  Returns true in that block
-// (every thread), with *total set.
-__device__ __forceinline__ bool last_block_sum(double acc, double* part, unsigned nblocks, unsigned* counter, double* total) {
+// Last-block finalisation of a reduction: every block stores its partial (acc
+// already summed over the block), the block that arrives last sums them in a
+// fixed order.  Returns true in that block (every thread), with *total set.
+__device__ __forceinline__ bool last_block_total(double acc, double* part, unsigned nblocks, unsigned* counter, double* total) {
   __shared__ bool last;
-  acc = block_sum(acc);
   unsigned bid = block_linear();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     part[bid] = acc;
@@ -588,6 +642,10 @@ __device__ __forceinline__ bool last_block_sum(double acc, double* part, unsigne
   *total = sum_partials(part, nblocks);
   if (threadIdx.x == 0 && threadIdx.y == 0) *counter = 0u;
   return true;
+}
+template <typename T>
+__device__ __forceinline__ bool last_block_sum(const Acc<T>& acc, double* part, unsigned nblocks, unsigned* counter, double* total) {
+  return last_block_total(acc.block_total(), part, nblocks, counter, total);
 }
 
 // z = M r is complete: record r.z and beta = rz_new / rz_cur (Fletcher-Reeves).
@@ -712,7 +770,7 @@ __global__ void __launch_bounds__(BXT* BYT) k_post_smooth(Level<T> L, Level<T> C
   }
   if (part_rz) {
     double rz;
-    if (last_block_sum(acc.value(), part_rz, gridDim.x * gridDim.y, counter, &rz)) publish_rz(sc, rz);
+    if (last_block_sum(acc, part_rz, gridDim.x * gridDim.y, counter, &rz)) publish_rz(sc, rz);
   }
 }
 
@@ -949,7 +1007,12 @@ __global__ void k_direction(Level<double> L, const TZ* __restrict__ z, double* _
 
 // Ap = A p (reference entries) and p.Ap; the last block publishes
 // alpha = rz_new / p.Ap and rz_cur = rz_new.  With an even row length two
-// neighbouring cells per thread (16-byte loads), else one.
+// neighbouring cells per thread (16-byte loads), else one.  With the FP32
+// preconditioner (TZ = float, whose r.z and ||r||^2 are FP32 sums already) each
+// thread's FP64 partial is split into two FP32 words (one FP64 subtraction) and
+// the block sum runs in double-float on the FP32 pipe; with the FP64 one the
+// block sum stays FP64.
+template <typename TZ>
 __global__ void k_apply_pap(Level<double> L, const double* __restrict__ p, double* __restrict__ ap, Scalars* sc, double* __restrict__ part,
                             unsigned* __restrict__ counter, const int* __restrict__ done) {
   pdl_enter();
@@ -975,8 +1038,14 @@ __global__ void k_apply_pap(Level<double> L, const double* __restrict__ p, doubl
       acc += pc * y;
     }
   }
-  double pap;
-  if (last_block_sum(acc, part, gridDim.x, counter, &pap) && threadIdx.x == 0) {
+  double pap, blk;
+  if constexpr (sizeof(TZ) == 4) {
+    const float hi = narrow(acc);
+    blk = block_sum_df(DF{hi, narrow(acc - widen(hi))});
+  } else {
+    blk = block_sum(acc);
+  }
+  if (last_block_total(blk, part, gridDim.x, counter, &pap) && threadIdx.x == 0) {
     double rz = sc->rz_new;
     sc->rz_cur = rz;
     sc->alpha = rz / pap;
@@ -1011,7 +1080,7 @@ __global__ void k_update(Level<double> L, double* __restrict__ x, double* __rest
     }
   }
   double rr;
-  if (last_block_sum(acc.value(), part, gridDim.x, counter, &rr) && threadIdx.x == 0) {
+  if (last_block_sum(acc, part, gridDim.x, counter, &rr) && threadIdx.x == 0) {
     sc->rr = rr;
     if (!(rr > sc->thr2)) {
       *done = 1;
@@ -1035,7 +1104,7 @@ __global__ void k_jacobi(Level<T> L, const T* __restrict__ r, T* __restrict__ z,
     acc.add(r[k] * zv);
   }
   double rz;
-  if (last_block_sum(acc.value(), part_rz, gridDim.x, counter, &rz)) publish_rz(sc, rz);
+  if (last_block_sum(acc, part_rz, gridDim.x, counter, &rz)) publish_rz(sc, rz);
 }
 
 __global__ void k_begin_inner(Scalars* sc, int* done, double thr2) {
@@ -1648,7 +1717,7 @@ void enqueue_init(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv
   const Level<double>& L = S->h64.L[0];
   precondition<T>(s, S, H, ainv, use_mg, nu, pr);
   pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_direction<T>, L, (const T*)H.L[0].x, S->p, (const Scalars*)S->sc, 1, (const int*)S->done);
-  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_apply_pap, L, (const double*)S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter,
+  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_apply_pap<T>, L, (const double*)S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter,
              (const int*)S->done);
   GB_LAUNCHED(2);
 }
@@ -1664,7 +1733,7 @@ void enqueue_iter(cudaStream_t s, Solver* S, Hierarchy<T>& H, const double* ainv
   GB_LAUNCHED(1);
   precondition<T>(s, S, H, ainv, use_mg, nu, pr);
   pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_direction<T>, L, (const T*)H.L[0].x, S->p, (const Scalars*)S->sc, 0, (const int*)S->done);
-  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_apply_pap, L, (const double*)S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter,
+  pdl_launch(s, dim3(S->G), dim3(kThreads), 0, k_apply_pap<T>, L, (const double*)S->p, S->ap, S->sc, slot(S, kSlotPap), S->counter,
              (const int*)S->done);
   GB_LAUNCHED(2);
 }

@@ -313,6 +313,6 @@ __global__ void __launch_bounds__(32 * st::Geo<NS, POST>::WARPS)
   cp_wait<0>();
   if (POST && part_rz) {
     double rz;
-    if (last_block_sum(acc.value(), part_rz, gridDim.x, counter, &rz)) publish_rz(sc, rz);
+    if (last_block_sum(acc, part_rz, gridDim.x, counter, &rz)) publish_rz(sc, rz);
   }
 }
