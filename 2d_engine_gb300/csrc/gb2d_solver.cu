@@ -104,12 +104,12 @@ __device__ __forceinline__ DF warp_sum_df(DF v) {
   for (int o = 16; o > 0; o >>= 1) v = df_add(v, DF{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)});
   return v;
 }
-// Deterministic block sum of double-float values (valid in every thread).
-__device__ DF block_sum_df(DF v) {
+// Deterministic block sum of double-float values, as FP64 (valid in every thread).
+__device__ double block_sum_df(DF v) {
   double* sm = reduce_scratch();
   float* shi = reinterpret_cast<float*>(sm);
   float* slo = shi + 32;
-  float* tot = reinterpret_cast<float*>(sm + 32);
+  double& total = sm[32];
   int tid = linear_tid();
   int lane = tid & 31, w = tid >> 5, nw = block_threads() >> 5;
   v = warp_sum_df(v);
@@ -122,30 +122,17 @@ __device__ DF block_sum_df(DF v) {
   if (w == 0) {
     DF x = lane < nw ? DF{shi[lane], slo[lane]} : DF{0.f, 0.f};
     x = warp_sum_df(x);
-    if (lane == 0) {
-      tot[0] = x.hi;
-      tot[1] = x.lo;
-    }
+    if (lane == 0) total = widen(x.hi) + widen(x.lo);
   }
   __syncthreads();
-  return DF{tot[0], tot[1]};
+  return total;
 }
-__device__ __forceinline__ double df_value(DF v) { return widen(v.hi) + widen(v.lo); }
 
 // Partials written by other blocks: read through L2 (__ldcg), never a stale L1 line.
 __device__ double sum_partials(const double* part, int n) {
   double v = 0.0;
   for (int k = linear_tid(); k < n; k += block_threads()) v += __ldcg(&part[k]);
   return block_sum(v);
-}
-// The same for double-float partials, each stored as two FP32 words in one slot.
-__device__ DF sum_partials_df(const double* part, int n) {
-  DF v{0.f, 0.f};
-  for (int k = linear_tid(); k < n; k += block_threads()) {
-    const float2 q = __ldcg(reinterpret_cast<const float2*>(part) + k);
-    v = df_add(v, DF{q.x, q.y});
-  }
-  return block_sum_df(v);
 }
 
 __device__ __forceinline__ unsigned block_linear() { return blockIdx.x + blockIdx.y * gridDim.x; }
@@ -619,8 +606,8 @@ __device__ __forceinline__ void window_half(T* sm, int i0, int j0, int nI, int n
 }
 
 // FP32-friendly accumulation of a few products per thread (Kahan-compensated in
-// the vector precision, s - c); the block and grid reductions continue in
-// double-float on the FP32 pipe.
+// the vector precision, s - c); the block reduction continues in double-float on
+// the FP32 pipe, the grid reduction in FP64.
 template <typename T>
 struct Acc {
   T s = 0, c = 0;
@@ -630,7 +617,7 @@ struct Acc {
     c = (t - s) - y;
     s = t;
   }
-  __device__ __forceinline__ DF block_total() const { return block_sum_df(DF{s, -c}); }
+  __device__ __forceinline__ double block_total() const { return block_sum_df(DF{s, -c}); }
 };
 template <>
 struct Acc<double> {  // FP64 vectors: plain accumulation (FP64 issue slots are scarce)
@@ -653,22 +640,6 @@ __device__ __forceinline__ bool last_block_total(double acc, double* part, unsig
   __syncthreads();
   if (!last) return false;
   *total = sum_partials(part, nblocks);
-  if (threadIdx.x == 0 && threadIdx.y == 0) *counter = 0u;
-  return true;
-}
-// The same with double-float partials (two FP32 words per slot), summed on the
-// FP32 pipe; *total = their FP64 value.
-__device__ __forceinline__ bool last_block_total(DF acc, double* part, unsigned nblocks, unsigned* counter, double* total) {
-  __shared__ bool last;
-  unsigned bid = block_linear();
-  if (threadIdx.x == 0 && threadIdx.y == 0) {
-    reinterpret_cast<float2*>(part)[bid] = make_float2(acc.hi, acc.lo);
-    __threadfence();
-    last = atomicAdd(counter, 1u) == nblocks - 1;
-  }
-  __syncthreads();
-  if (!last) return false;
-  *total = df_value(sum_partials_df(part, nblocks));
   if (threadIdx.x == 0 && threadIdx.y == 0) *counter = 0u;
   return true;
 }
@@ -1067,15 +1038,14 @@ __global__ void k_apply_pap(Level<double> L, const double* __restrict__ p, doubl
       acc += pc * y;
     }
   }
-  double pap;
-  bool last;
+  double pap, blk;
   if constexpr (sizeof(TZ) == 4) {
     const float hi = narrow(acc);
-    last = last_block_total(block_sum_df(DF{hi, narrow(acc - widen(hi))}), part, gridDim.x, counter, &pap);
+    blk = block_sum_df(DF{hi, narrow(acc - widen(hi))});
   } else {
-    last = last_block_total(block_sum(acc), part, gridDim.x, counter, &pap);
+    blk = block_sum(acc);
   }
-  if (last && threadIdx.x == 0) {
+  if (last_block_total(blk, part, gridDim.x, counter, &pap) && threadIdx.x == 0) {
     double rz = sc->rz_new;
     sc->rz_cur = rz;
     sc->alpha = rz / pap;
