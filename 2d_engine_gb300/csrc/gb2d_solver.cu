@@ -390,7 +390,7 @@ __device__ __forceinline__ void cp_async_zfill(T* dst, const T* src, bool valid)
 //   Split layout: the coefficients (and x without a correction) are copied with
 //   cp.async, so that all of a thread's copies are in flight at once,
 //   zero-filled outside the domain by the copy itself.  32x32 tiles (the FP32
-//   levels of 2048^2 and more) copy one pair of cells (2m, r), (2m + 1, r) per
+//   levels of 1024^2 and more) copy one pair of cells (2m, r), (2m + 1, r) per
 //   thread and pass, which land at the same element r WH + m of planes r & 1 and
 //   (r + 1) & 1 (half the index arithmetic per cell); the other tiles one cell
 //   per thread and pass (one contiguous row segment per warp and copy).
@@ -1936,13 +1936,15 @@ cudaError_t set_smooth_smem() {
 }
 
 // Tile shape per tiled level: 32x16 where that gives at least 8 blocks per SM,
-// else 32x8; FP32 levels of 2048^2 cells and more take 32x32.  Measured on GB300
+// else 32x8; FP32 levels of 1024^2 cells and more take 32x32.  Measured on GB300
 // (MG-PCG projection to 1e-8, 512^2-4096^2): the 32x16 tile beats 64x16 on every
 // level size, its 22 KB window (FP32, two sweeps) letting 8 blocks share an SM
 // against 5, and the extra warps hide the staging loads' latency better than the
 // larger tile saves halo work; below 1024^2 the 32x8 tile's shorter per-block
-// pipeline wins; on the largest FP32 levels the 32x32 tile's smaller halo share
-// wins by 1-3% (not in FP64, nor at 1024^2).  GB2D_TILE_SHAPES="s0,s1,..." (0-3
+// pipeline wins; on the large FP32 levels, with the colour-split window staged
+// by pairs of cells, the 32x32 tile's smaller halo share wins (mixed projection
+// 2.280 -> 2.249 ms at 1024^2, 6.000 -> 5.973 ms at 2048^2 from its 1024^2
+// level); not in FP64.  GB2D_TILE_SHAPES="s0,s1,..." (0-3
 // per level from the finest) overrides the rule, for tuning.
 template <typename T>
 void plan_shapes(Hierarchy<T>& H, int nsm) {
@@ -1950,7 +1952,7 @@ void plan_shapes(Hierarchy<T>& H, int nsm) {
   for (int l = 0; l < H.nlev; ++l) {
     const dim3 t = tiles(H.L[l].nI, H.L[l].nJ, 1);
     int sh = (long long)t.x * t.y >= 8LL * nsm ? 1 : 2;
-    if (sizeof(T) == 4 && (long long)H.L[l].nI * H.L[l].nJ >= 2048LL * 2048) sh = 3;
+    if (sizeof(T) == 4 && (long long)H.L[l].nI * H.L[l].nJ >= 1024LL * 1024) sh = 3;
     H.shape[l] = sh;
   }
   for (int l = 0; env && *env && l < H.nlev; ++l) {
